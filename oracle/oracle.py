@@ -1,0 +1,460 @@
+"""numpy front-end for the CPU oracle (cs_oracle.c) and, where it was built, for the reference's own CPU code
+(oracle/_ref/libcsref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by the CPU-baseline leg of bench.py.
+The product path never imports it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcsoracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libcsref.so")
+
+MORTON, HILBERT = 0, 1
+OPEN, PERIODIC = 0, 1
+
+
+class CsoBox(C.Structure):
+    _fields_ = [("lo", C.c_double * 3), ("hi", C.c_double * 3), ("boundary", C.c_int * 3)]
+
+
+def make_box(lo, hi, boundary=(0, 0, 0)):
+    lo = [float(v) for v in (lo if np.ndim(lo) else [lo] * 3)]
+    hi = [float(v) for v in (hi if np.ndim(hi) else [hi] * 3)]
+    b = list(boundary) if np.ndim(boundary) else [int(boundary)] * 3
+    return CsoBox((C.c_double * 3)(*lo), (C.c_double * 3)(*hi), (C.c_int * 3)(*b))
+
+
+def build(force=False):
+    """Compile the restatement with the committed Makefile (gcc, OpenMP)."""
+    if force or not os.path.exists(LIB_PATH) or _stale(LIB_PATH, ["cs_oracle.c", "cs_oracle_real.inc", "cs_oracle.h"]):
+        subprocess.check_call(["make", "-s", "-C", HERE, "libcsoracle.so"])
+
+
+def build_ref(reference_root="/root/reference"):
+    """Compile the reference's CPU code in place (only where its sources exist). Returns True if available."""
+    if not os.path.isdir(os.path.join(reference_root, "include", "cstone")):
+        return os.path.exists(REF_PATH)
+    if not os.path.exists(REF_PATH) or _stale(REF_PATH, ["ref_driver.cpp"]):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFERENCE={reference_root}"])
+    return True
+
+
+def _stale(target, sources):
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(os.path.join(HERE, s)) > t for s in sources)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB_PATH)
+        _lib.cso_imorton.restype = C.c_uint64
+        _lib.cso_ihilbert.restype = C.c_uint64
+        _lib.cso_rebalance_decision.restype = C.c_int
+        _lib.cso_rebalance_tree.restype = C.c_int32
+        _lib.cso_update_octree.restype = C.c_int
+        _lib.cso_compute_octree.restype = C.c_int32
+        _lib.cso_binary_key_weight.restype = C.c_int32
+        _lib.cso_num_threads.restype = C.c_int
+    return _lib
+
+
+def ref():
+    """The reference's own CPU implementation, or None where it cannot be built."""
+    global _ref
+    if _ref is None:
+        if not build_ref():
+            return None
+        _ref = C.CDLL(REF_PATH)
+        _ref.csr_imorton.restype = C.c_uint64
+        _ref.csr_ihilbert.restype = C.c_uint64
+        _ref.csr_rebalance_decision.restype = C.c_int
+        _ref.csr_compute_octree.restype = C.c_int32
+        _ref.csr_update_octree.restype = C.c_int
+        _ref.csr_binary_key_weight.restype = C.c_int32
+    return _ref
+
+
+def num_threads():
+    return lib().cso_num_threads()
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# restatement API (numpy in / numpy out)
+# ---------------------------------------------------------------------------------------------------------------
+
+def imorton(ix, iy, iz, key_bits):
+    return lib().cso_imorton(C.c_uint(ix), C.c_uint(iy), C.c_uint(iz), key_bits)
+
+
+def ihilbert(ix, iy, iz, key_bits):
+    return lib().cso_ihilbert(C.c_uint(ix), C.c_uint(iy), C.c_uint(iz), key_bits)
+
+
+def decode_hilbert(key, key_bits):
+    out = (C.c_uint * 3)()
+    lib().cso_decode_hilbert(C.c_uint64(key), key_bits, out)
+    return tuple(out)
+
+
+def decode_morton(key, key_bits):
+    out = (C.c_uint * 3)()
+    lib().cso_decode_morton(C.c_uint64(key), key_bits, out)
+    return tuple(out)
+
+
+def sfc_keys(x, y, z, box, kind=HILBERT, key_bits=64, keys=None, respect_remove_key=False):
+    x, y, z = (np.ascontiguousarray(a) for a in (x, y, z))
+    n = x.size
+    keys = np.zeros(n, np.uint64) if keys is None else np.ascontiguousarray(keys, dtype=np.uint64).copy()
+    fn = lib().cso_sfc_keys_f64 if x.dtype == np.float64 else lib().cso_sfc_keys_f32
+    fn(_p(x), _p(y), _p(z), _p(keys), C.c_size_t(n), C.byref(box), kind, key_bits, int(respect_remove_key))
+    return keys
+
+
+def sort_by_key(keys, values=None):
+    k = np.ascontiguousarray(keys, dtype=np.uint64).copy()
+    v = np.arange(k.size, dtype=np.uint32) if values is None else np.ascontiguousarray(values, np.uint32).copy()
+    lib().cso_sort_by_key(_p(k), _p(v), C.c_size_t(k.size))
+    return k, v
+
+
+def find_search_bounds(guess, target, codes, key_bits=64):
+    codes = np.ascontiguousarray(codes, np.uint64)
+    lo, hi = C.c_int64(), C.c_int64()
+    lib().cso_find_search_bounds(C.c_int64(guess), C.c_uint64(target), _p(codes), C.c_int64(codes.size), key_bits,
+                                 C.byref(lo), C.byref(hi))
+    return lo.value, hi.value
+
+
+def node_counts(tree, keys, key_bits=64, max_count=0xFFFFFFFF, guess_counts=None):
+    tree = np.ascontiguousarray(tree, np.uint64)
+    keys = np.ascontiguousarray(keys, np.uint64)
+    L = tree.size - 1
+    counts = np.zeros(L, np.uint32) if guess_counts is None else np.ascontiguousarray(guess_counts, np.uint32).copy()
+    lib().cso_node_counts(_p(tree), _p(counts), L, _p(keys), C.c_size_t(keys.size), C.c_uint32(max_count),
+                          int(guess_counts is not None), key_bits)
+    return counts
+
+
+def rebalance_decision(tree, counts, bucket, key_bits=64):
+    tree = np.ascontiguousarray(tree, np.uint64)
+    counts = np.ascontiguousarray(counts, np.uint32)
+    L = tree.size - 1
+    ops = np.zeros(L + 1, np.int32)
+    conv = lib().cso_rebalance_decision(_p(tree), _p(counts), L, bucket, _p(ops), key_bits)
+    return ops[:L], bool(conv)
+
+
+def rebalance_tree(tree, ops, key_bits=64):
+    tree = np.ascontiguousarray(tree, np.uint64)
+    L = tree.size - 1
+    o = np.zeros(L + 1, np.int32)
+    o[:L] = ops[:L]
+    cap = int(np.sum(o, dtype=np.int64))
+    nt = np.zeros(cap + 1, np.uint64)
+    nn = lib().cso_rebalance_tree(_p(tree), L, _p(o), _p(nt), cap, key_bits)
+    return nt[: nn + 1]
+
+
+def compute_octree(keys, bucket, key_bits=64, max_count=0xFFFFFFFF):
+    keys = np.ascontiguousarray(keys, np.uint64)
+    cap = max(64, 8 * (keys.size // max(bucket, 1) + 1) * 8)
+    while True:
+        tree = np.zeros(cap + 1, np.uint64)
+        counts = np.zeros(cap, np.uint32)
+        it = C.c_int()
+        L = lib().cso_compute_octree(_p(keys), C.c_size_t(keys.size), bucket, C.c_uint32(max_count), _p(tree),
+                                     _p(counts), cap, key_bits, C.byref(it))
+        if L > 0:
+            return tree[: L + 1].copy(), counts[:L].copy(), it.value
+        cap = 2 * max(cap, -L)
+
+
+def update_octree(keys, bucket, tree, counts, key_bits=64, max_count=0xFFFFFFFF):
+    keys = np.ascontiguousarray(keys, np.uint64)
+    L0 = np.asarray(tree).size - 1
+    cap = max(64, 4096 * L0 + 8)
+    t = np.zeros(cap + 1, np.uint64)
+    c = np.zeros(cap, np.uint32)
+    t[: L0 + 1] = tree
+    c[:L0] = counts
+    L = C.c_int32(L0)
+    conv = lib().cso_update_octree(_p(keys), C.c_size_t(keys.size), bucket, C.c_uint32(max_count), _p(t), _p(c),
+                                   C.byref(L), cap, key_bits)
+    assert conv >= 0
+    return t[: L.value + 1].copy(), c[: L.value].copy(), bool(conv)
+
+
+def binary_key_weight(key, level, key_bits=64):
+    return lib().cso_binary_key_weight(C.c_uint64(key), level, key_bits)
+
+
+class Octree:
+    """Linked octree arrays (OctreeData, tree/octree.hpp:285-360)."""
+
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def octree_sizes(L):
+    I = (L - 1) // 7
+    N = L + I
+    return I, N, max(1, (N - 1) // 8)
+
+
+def build_octree(leaves, key_bits=64):
+    leaves = np.ascontiguousarray(leaves, np.uint64)
+    L = leaves.size - 1
+    I, N, P = octree_sizes(L)
+    prefixes = np.zeros(N, np.uint64)
+    child = np.zeros(N + 1, np.int32)
+    parents = np.zeros(P, np.int32)
+    lr = np.zeros((10 if key_bits == 32 else 21) + 2, np.int32)
+    i2l = np.zeros(N, np.int32)
+    l2i = np.zeros(N, np.int32)
+    lib().cso_build_octree(_p(leaves), L, key_bits, _p(prefixes), _p(child), _p(parents), _p(lr), _p(i2l), _p(l2i))
+    return Octree(num_leaves=L, num_internal=I, num_nodes=N, prefixes=prefixes, child_offsets=child[:N],
+                  parents=parents, level_range=lr, internal_to_leaf=i2l, leaf_to_internal=l2i, leaves=leaves)
+
+
+def node_fp_centers(prefixes, box, dtype=np.float64, kind=HILBERT, key_bits=64):
+    prefixes = np.ascontiguousarray(prefixes, np.uint64)
+    N = prefixes.size
+    c = np.zeros((N, 3), dtype)
+    s = np.zeros((N, 3), dtype)
+    fn = lib().cso_node_fp_centers_f64 if dtype == np.float64 else lib().cso_node_fp_centers_f32
+    fn(_p(prefixes), N, kind, key_bits, C.byref(box), _p(c), _p(s))
+    return c, s
+
+
+def search_boxes(x, y, z, h, layout, first, last, scale, leaf_to_internal_leaves, node_centers):
+    dt = x.dtype
+    L = layout.size - 1
+    sc = np.zeros((L, 3), dt)
+    ss = np.zeros((L, 3), dt)
+    fn = lib().cso_search_boxes_f64 if dt == np.float64 else lib().cso_search_boxes_f32
+    cs = C.c_double(scale) if dt == np.float64 else C.c_float(scale)
+    l2i = np.ascontiguousarray(leaf_to_internal_leaves, np.int32)
+    fn(_p(x), _p(y), _p(z), _p(h), _p(np.ascontiguousarray(layout, np.uint32)), first, last, cs, _p(l2i),
+       _p(np.ascontiguousarray(node_centers, dt)), _p(sc), _p(ss))
+    return sc, ss
+
+
+def find_halos(tree, node_centers, node_sizes, search_centers, search_sizes, box, first, last, key_bits=64):
+    dt = node_centers.dtype
+    flags = np.zeros(tree.num_nodes, np.uint8)
+    fn = lib().cso_find_halos_f64 if dt == np.float64 else lib().cso_find_halos_f32
+    fn(_p(tree.prefixes), _p(tree.child_offsets), _p(tree.parents), _p(node_centers), _p(node_sizes),
+       _p(tree.leaves), _p(np.ascontiguousarray(search_centers, dt)), _p(np.ascontiguousarray(search_sizes, dt)),
+       C.byref(box), first, last, key_bits, _p(flags))
+    return flags
+
+
+def find_neighbors(x, y, z, h, first, last, box, tree, layout, centers, sizes, ngmax, search_ext=1.0):
+    dt = x.dtype
+    n = last - first
+    nb = np.zeros(n * ngmax, np.uint32)
+    nc = np.zeros(n, np.uint32)
+    fn = lib().cso_find_neighbors_f64 if dt == np.float64 else lib().cso_find_neighbors_f32
+    fn(_p(x), _p(y), _p(z), _p(h), C.c_uint32(first), C.c_uint32(last), C.byref(box), _p(tree.child_offsets),
+       _p(tree.parents), _p(tree.internal_to_leaf), _p(np.ascontiguousarray(layout, np.uint32)), _p(centers),
+       _p(sizes), C.c_float(search_ext), C.c_uint(ngmax), _p(nb), _p(nc))
+    return nb.reshape(n, ngmax), nc
+
+
+def philox_uniform(seed, stream, n, lo, hi):
+    out = np.empty(n, np.float64)
+    lib().cso_philox_uniform_f64(C.c_uint64(seed), C.c_uint64(stream), _p(out), C.c_size_t(n), C.c_double(lo),
+                                 C.c_double(hi))
+    return out
+
+
+def plummer(seed, n, rmax=100.0):
+    x, y, z = (np.empty(n, np.float64) for _ in range(3))
+    lib().cso_plummer_f64(C.c_uint64(seed), _p(x), _p(y), _p(z), C.c_size_t(n), C.c_double(rmax))
+    return x, y, z
+
+
+def layout_from_counts(counts):
+    layout = np.zeros(counts.size + 1, np.uint32)
+    np.cumsum(counts, out=layout[1:])
+    return layout
+
+
+def pipeline(x, y, z, h, box, bucket, ngmax, kind=HILBERT, key_bits=64, search_ext=1.0, with_neighbors=True):
+    """keys -> stable sort -> gather -> computeOctree -> link -> node geometry -> findNeighbors (all CPU)."""
+    keys = sfc_keys(x, y, z, box, kind, key_bits)
+    skeys, perm = sort_by_key(keys)
+    xs, ys, zs, hs = (a[perm] for a in (x, y, z, h))
+    leaves, counts, iters = compute_octree(skeys, bucket, key_bits)
+    tree = build_octree(leaves, key_bits)
+    centers, sizes = node_fp_centers(tree.prefixes, box, x.dtype, kind, key_bits)
+    layout = layout_from_counts(counts)
+    out = dict(keys=keys, sorted_keys=skeys, perm=perm, x=xs, y=ys, z=zs, h=hs, leaves=leaves, counts=counts,
+               iterations=iters, tree=tree, centers=centers, sizes=sizes, layout=layout)
+    if with_neighbors:
+        nb, nc = find_neighbors(xs, ys, zs, hs, 0, x.size, box, tree, layout, centers, sizes, ngmax, search_ext)
+        out.update(nb=nb, nc=nc)
+    return out
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# the reference's own CPU code (oracle/_ref), same call shapes as above; used to pin the restatement
+# ---------------------------------------------------------------------------------------------------------------
+
+def _box_arrays(box):
+    lo = np.array(box.lo[:], np.float64)
+    hi = np.array(box.hi[:], np.float64)
+    b = np.array(box.boundary[:], np.int32)
+    return lo, hi, b
+
+
+def ref_sfc_keys(x, y, z, box, kind=HILBERT, key_bits=64, keys=None):
+    r = ref()
+    n = x.size
+    keys = np.zeros(n, np.uint64) if keys is None else np.ascontiguousarray(keys, np.uint64).copy()
+    lo, hi, b = _box_arrays(box)
+    fn = r.csr_sfc_keys_f64 if x.dtype == np.float64 else r.csr_sfc_keys_f32
+    fn(_p(x), _p(y), _p(z), _p(keys), C.c_size_t(n), _p(lo), _p(hi), _p(b), kind, key_bits)
+    return keys
+
+
+def ref_sort_by_key(keys, values=None):
+    k = np.ascontiguousarray(keys, np.uint64).copy()
+    v = np.arange(k.size, dtype=np.uint32) if values is None else np.ascontiguousarray(values, np.uint32).copy()
+    ref().csr_sort_by_key(_p(k), _p(v), C.c_size_t(k.size))
+    return k, v
+
+
+def ref_find_search_bounds(guess, target, codes):
+    codes = np.ascontiguousarray(codes, np.uint64)
+    lo, hi = C.c_int64(), C.c_int64()
+    ref().csr_find_search_bounds(C.c_int64(guess), C.c_uint64(target), _p(codes), C.c_int64(codes.size),
+                                 C.byref(lo), C.byref(hi))
+    return lo.value, hi.value
+
+
+def ref_node_counts(tree, keys, key_bits=64, max_count=0xFFFFFFFF, guess_counts=None):
+    tree = np.ascontiguousarray(tree, np.uint64)
+    keys = np.ascontiguousarray(keys, np.uint64)
+    L = tree.size - 1
+    counts = np.zeros(L, np.uint32) if guess_counts is None else np.ascontiguousarray(guess_counts, np.uint32).copy()
+    ref().csr_node_counts(_p(tree), _p(counts), L, _p(keys), C.c_size_t(keys.size), C.c_uint32(max_count),
+                          int(guess_counts is not None), key_bits)
+    return counts
+
+
+def ref_rebalance_decision(tree, counts, bucket, key_bits=64):
+    tree = np.ascontiguousarray(tree, np.uint64)
+    counts = np.ascontiguousarray(counts, np.uint32)
+    L = tree.size - 1
+    ops = np.zeros(L + 1, np.int32)
+    conv = ref().csr_rebalance_decision(_p(tree), _p(counts), L, bucket, _p(ops), key_bits)
+    return ops[:L], bool(conv)
+
+
+def ref_compute_octree(keys, bucket, key_bits=64, max_count=0xFFFFFFFF):
+    keys = np.ascontiguousarray(keys, np.uint64)
+    cap = max(64, 64 * (keys.size // max(bucket, 1) + 1))
+    while True:
+        tree = np.zeros(cap + 1, np.uint64)
+        counts = np.zeros(cap, np.uint32)
+        it = C.c_int()
+        L = ref().csr_compute_octree(_p(keys), C.c_size_t(keys.size), bucket, C.c_uint32(max_count), _p(tree),
+                                     _p(counts), cap, key_bits, C.byref(it))
+        if L > 0:
+            return tree[: L + 1].copy(), counts[:L].copy(), it.value
+        cap = 2 * max(cap, -L)
+
+
+def ref_update_octree(keys, bucket, tree, counts, key_bits=64, max_count=0xFFFFFFFF):
+    keys = np.ascontiguousarray(keys, np.uint64)
+    L0 = np.asarray(tree).size - 1
+    cap = max(64, 4096 * L0 + 8)
+    t = np.zeros(cap + 1, np.uint64)
+    c = np.zeros(cap, np.uint32)
+    t[: L0 + 1] = tree
+    c[:L0] = counts
+    L = C.c_int32(L0)
+    conv = ref().csr_update_octree(_p(keys), C.c_size_t(keys.size), bucket, C.c_uint32(max_count), _p(t), _p(c),
+                                   C.byref(L), cap, key_bits)
+    return t[: L.value + 1].copy(), c[: L.value].copy(), bool(conv)
+
+
+def ref_build_octree(leaves, key_bits=64):
+    leaves = np.ascontiguousarray(leaves, np.uint64)
+    L = leaves.size - 1
+    I, N, P = octree_sizes(L)
+    prefixes = np.zeros(N, np.uint64)
+    child = np.zeros(N + 1, np.int32)
+    parents = np.zeros(P, np.int32)
+    lr = np.zeros((10 if key_bits == 32 else 21) + 2, np.int32)
+    i2l = np.zeros(N, np.int32)
+    l2i = np.zeros(N, np.int32)
+    ref().csr_build_octree(_p(leaves), L, key_bits, _p(prefixes), _p(child), _p(parents), _p(lr), _p(i2l), _p(l2i))
+    return Octree(num_leaves=L, num_internal=I, num_nodes=N, prefixes=prefixes, child_offsets=child[:N],
+                  parents=parents, level_range=lr, internal_to_leaf=i2l, leaf_to_internal=l2i, leaves=leaves)
+
+
+def ref_node_fp_centers(prefixes, box, dtype=np.float64, key_bits=64):
+    prefixes = np.ascontiguousarray(prefixes, np.uint64)
+    N = prefixes.size
+    c = np.zeros((N, 3), dtype)
+    s = np.zeros((N, 3), dtype)
+    lo, hi, b = _box_arrays(box)
+    fn = ref().csr_node_fp_centers_f64 if dtype == np.float64 else ref().csr_node_fp_centers_f32
+    fn(_p(prefixes), N, key_bits, _p(lo), _p(hi), _p(b), _p(c), _p(s))
+    return c, s
+
+
+def ref_search_boxes(x, y, z, h, layout, first, last, scale, leaf_to_internal_leaves, node_centers):
+    dt = x.dtype
+    L = layout.size - 1
+    sc = np.zeros((L, 3), dt)
+    ss = np.zeros((L, 3), dt)
+    fn = ref().csr_search_boxes_f64 if dt == np.float64 else ref().csr_search_boxes_f32
+    cs = C.c_double(scale) if dt == np.float64 else C.c_float(scale)
+    l2i = np.ascontiguousarray(leaf_to_internal_leaves, np.int32)
+    fn(_p(x), _p(y), _p(z), _p(h), _p(np.ascontiguousarray(layout, np.uint32)), first, last, cs, _p(l2i),
+       _p(np.ascontiguousarray(node_centers, dt)), _p(sc), _p(ss))
+    return sc, ss
+
+
+def ref_find_halos(tree, node_centers, node_sizes, search_centers, search_sizes, box, first, last, key_bits=64):
+    dt = node_centers.dtype
+    flags = np.zeros(tree.num_nodes, np.uint8)
+    lo, hi, b = _box_arrays(box)
+    fn = ref().csr_find_halos_f64 if dt == np.float64 else ref().csr_find_halos_f32
+    fn(_p(tree.prefixes), _p(tree.child_offsets), _p(tree.parents), _p(node_centers), _p(node_sizes),
+       _p(tree.leaves), tree.num_nodes, tree.num_leaves, _p(np.ascontiguousarray(search_centers, dt)),
+       _p(np.ascontiguousarray(search_sizes, dt)), _p(lo), _p(hi), _p(b), first, last, key_bits, _p(flags))
+    return flags
+
+
+def ref_find_neighbors(x, y, z, h, first, last, box, tree, layout, centers, sizes, ngmax, search_ext=1.0):
+    dt = x.dtype
+    n = last - first
+    nb = np.zeros(n * ngmax, np.uint32)
+    nc = np.zeros(n, np.uint32)
+    lo, hi, b = _box_arrays(box)
+    fn = ref().csr_find_neighbors_f64 if dt == np.float64 else ref().csr_find_neighbors_f32
+    fn(_p(x), _p(y), _p(z), _p(h), C.c_uint32(first), C.c_uint32(last), _p(lo), _p(hi), _p(b), tree.num_leaves,
+       tree.num_nodes, _p(tree.child_offsets), _p(tree.parents), _p(tree.internal_to_leaf),
+       _p(np.ascontiguousarray(layout, np.uint32)), _p(centers), _p(sizes), C.c_float(search_ext), C.c_uint(ngmax),
+       _p(nb), _p(nc))
+    return nb.reshape(n, ngmax), nc
