@@ -1,0 +1,347 @@
+"""Benchmark: keys -> neighbours throughput (Mparticles/s) of the whole octree path on N Plummer particles.
+
+Workload (default): 16M FP64 particles from a Plummer sphere (scale radius 1, truncated at r = 100, seeded, centre of
+mass at the origin), tight bounding box, 64-bit Hilbert keys, bucketSize 64, findHalos for the leaves in the first
+quarter of the key space [0, 2^61), findNeighbors with ngmax 200, per-particle h such that exactly 100 neighbours lie
+within 2h (set once before timing by bisection on neighbour counts). One step = one full pass of the path over the
+particles: keys, stable sort, gather of x/y/z/h, computeOctree from the root, internal-tree link, node geometry,
+search boxes + halo flags, neighbour search.
+
+Reports (one JSON line on rank 0):
+  value     device throughput, inputs resident in HBM (particles of all ranks / max-over-ranks step time)
+  e2e       the same through the host-buffer C-ABI call: pinned host inputs copied in, neighbour counts and halo
+            flags copied back every step
+  roofline  for the dominant kernel (neighbour search): algorithmic bytes per launch / its event-timed duration
+  cpu_baseline  the CPU oracle of the same path on the host cores, on a bounded sample of the workload
+
+--impl reference times the reference's CPU implementation of the path (the oracle port; the reference's own build
+cannot run on the GPU host) on the same workload family, one bounded sample per step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "cornerstone-octree_gb300"))
+
+METRIC = "Mparticles/s keys->neighbors (16M Plummer)"
+UNIT = "Mparticles/s"
+NGMAX = 200
+BUCKET = 64
+K_NEIGHBORS = 100
+FOCUS = (0, 1 << 61)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=16 * 1024 * 1024)
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--cpu-sample", type=int, default=1 << 20, help="particles of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs"""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(n):
+    """DRAM bytes per neighbour-search launch from the committed ncu summary, scaled to n particles, or None"""
+    path = os.path.join(ROOT, "profiles", "neighbors_plummer.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_particle:"):
+                    return float(line.split(":")[1]) * n
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# CPU side (oracle): bounded sample of the workload
+# ---------------------------------------------------------------------------------------------------------------
+
+def cpu_sample(n_sample, seed):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    from cstone_gb300 import workloads as W
+
+    x, y, z = W.plummer(n_sample, seed)
+    lo, hi = W.tight_box(x, y, z)
+    box = O.make_box(lo, hi)
+    h = O.h_for_k_neighbors_cpu(x, y, z, box, K_NEIGHBORS)
+    return O, x, y, z, h, box
+
+
+def cpu_time(O, x, y, z, h, box):
+    t, _ = O.timed_pipeline(x, y, z, h, box, BUCKET, NGMAX, FOCUS)
+    return t
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    O, x, y, z, h, box = cpu_sample(args.cpu_sample, args.seed)
+    for _ in range(args.warmup):
+        cpu_time(O, x, y, z, h, box)
+    t0 = time.perf_counter()
+    stages = []
+    for _ in range(args.steps):
+        stages.append(cpu_time(O, x, y, z, h, box))
+    dt = (time.perf_counter() - t0) / args.steps
+    value = args.cpu_sample / dt / 1e6
+    cores = O.num_threads()
+    sample = (f"{args.cpu_sample} particles of the same Plummer workload (k=100 neighbours, h within 10% of the "
+              f"k-distance), full path per step")
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "plummer-keys-to-neighbors", "n_particles": args.cpu_sample, "ngmax": NGMAX,
+                       "bucket_size": BUCKET, "keys": "hilbert64", "focus": "[0, 2^61)"},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "stage_seconds": {k: round(statistics.mean(s[k] for s in stages), 4) for k in stages[0]}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------------------------------------------
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    import cstone_gb300 as cs
+    from cstone_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.n
+    x, y, z = W.plummer(n, args.seed + rank)
+    lo, hi = W.tight_box(x, y, z)
+    box = cs.make_box(lo, hi)
+    tx, ty, tz = (torch.from_numpy(a).to(dev) for a in (x, y, z))
+    th, hnc = W.h_for_k_neighbors(tx, ty, tz, box, K_NEIGHBORS, BUCKET)
+    torch.cuda.synchronize()
+
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, BUCKET, NGMAX, 1.0, 1.0, True, True)
+    for _ in range(args.warmup):
+        pipe.run(tx, ty, tz, th, box, FOCUS)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stage_acc = {k: 0.0 for k in cs.STAGES}
+    with ClockSampler(local) as clocks:
+        barrier(world)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            pipe.run(tx, ty, tz, th, box, FOCUS)
+            st = pipe.stage_times()
+            for k in st:
+                stage_acc[k] += st[k]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(ms, world)
+    value = world * n / (ms * 1e-3) / 1e6
+    stages = {k: v / args.steps for k, v in stage_acc.items()}
+    res = pipe.result
+    nc = pipe.outputs()["neighbor_counts"]
+    mean_nc = float(nc.double().mean())
+    stored = float(nc.clamp(max=NGMAX).double().sum())
+
+    # ---- end to end through the host-buffer call ----
+    e2e = None
+    if not args.no_e2e:
+        hx, hy, hz, hh = (t.cpu().pin_memory() for t in (tx, ty, tz, th))
+        nc_host = torch.empty(n, dtype=torch.int32).pin_memory()
+        flags_host = torch.empty(res.num_nodes * 2 + 1024, dtype=torch.uint8).pin_memory()
+        for _ in range(max(1, args.warmup)):
+            pipe.run_host(hx, hy, hz, hh, box, FOCUS, nc_host, flags_host)
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(args.steps):
+            pipe.run_host(hx, hy, hz, hh, box, FOCUS, nc_host, flags_host)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
+        e2e = {"value": round(world * n / (e2e_ms * 1e-3) / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": 4 * n * 8, "d2h_bytes_per_step": n * 4 + pipe.result.num_nodes,
+               "ms_per_step": round(e2e_ms, 3),
+               "wall_ms_per_step": round((time.perf_counter() - t0) * 1e3 / args.steps, 3)}
+
+    # ---- roofline of the dominant kernel (neighbour search) ----
+    peak, peak_kind = measured_hbm_peak()
+    nb_bytes = n * (4 * 8 + 4) + 4.0 * stored  # x,y,z,h read + count written + stored neighbour indices
+    nb_ms = stages["neighbors"]
+    achieved = nb_bytes / (nb_ms * 1e-3) / 1e9
+    roofline = {"kernel": "findNeighborsKernel<double>", "bound": "hbm", "achieved": round(achieved, 1),
+                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": profiled_traffic(n), "algorithmic_bytes": nb_bytes, "ms": round(nb_ms, 4)}
+
+    # ---- CPU baseline on a bounded sample ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        O, sx, sy, sz, sh, sbox = cpu_sample(args.cpu_sample, args.seed)
+        t = cpu_time(O, sx, sy, sz, sh, sbox)
+        cpu = {"value": round(args.cpu_sample / t["total"] / 1e6, 3), "unit": UNIT, "cores": O.num_threads(),
+               "kind": "port",
+               "sample": f"{args.cpu_sample} particles of the same Plummer workload, one full pass",
+               "stage_seconds": {k: round(v, 4) for k, v in t.items()}}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "plummer-keys-to-neighbors", "n_particles_per_gpu": n, "ngmax": NGMAX,
+                           "bucket_size": BUCKET, "keys": "hilbert64", "focus": "[0, 2^61)",
+                           "neighbours_target": K_NEIGHBORS, "l2": "inputs (512 MB) larger than L2",
+                           "parallelism": f"replicas x{world}"},
+                "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
+                "gpu_launches": None,
+                "stages_ms": {k: round(v, 4) for k, v in stages.items()},
+                "tree": {"leaves": res.num_leaves, "nodes": res.num_nodes, "iterations": res.iterations,
+                         "max_depth": res.max_depth, "focus_leaves": res.focus_last - res.focus_first},
+                "mean_neighbors": round(mean_nc, 2), "h_converged_frac": float((hnc == K_NEIGHBORS).double().mean())}
+        line["gpu_launches"] = gpu_launches_per_step(res) * args.steps
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def gpu_launches_per_step(res):
+    """kernels this library launches in one pipeline step (memsets and copies not counted):
+    keys 1, sort 1 histogram + 1 scan + passes, gather 1, build 1 cooperative, link 1 layout + sort + invert +
+    levelRange + link, geometry 1, halos 2, neighbour prep 2 (f64), neighbours 1"""
+    key_passes = (63 + 7) // 8
+    prefix_passes = (3 * res.max_depth + 1 + 7) // 8
+    return 1 + (2 + key_passes) + 1 + 1 + (1 + 2 + prefix_passes + 3) + 1 + 2 + 2 + 1
+
+
+if __name__ == "__main__":
+    main()

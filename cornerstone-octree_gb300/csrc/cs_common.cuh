@@ -1,0 +1,421 @@
+// Shared device/host helpers for the GB300 octree library: SFC key algebra, exactly-rounded arithmetic wrappers,
+// the box parameter block, status codes and launch helpers.
+//
+// Parity rule for every floating-point expression that feeds a key, a node box or a distance test: it is written
+// with explicit round-to-nearest intrinsics (__dmul_rn, __dadd_rn, ... / __fmul_rn, ...) so nvcc cannot fuse it into
+// an FMA. The reference evaluates those expressions unfused (g++, x86-64), so only unfused arithmetic reproduces its
+// results bit for bit.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/cstone_gb300.h"
+
+namespace csg
+{
+
+using TreeNodeIndex = int32_t;
+using LocalIndex    = uint32_t;
+
+// ---------------------------------------------------------------------------------------------------------------
+// key width traits (tree/definitions.h:29-75)
+// ---------------------------------------------------------------------------------------------------------------
+template<class K>
+struct KeyTraits;
+template<>
+struct KeyTraits<uint32_t>
+{
+    static constexpr int maxLevel   = 10;
+    static constexpr int unusedBits = 2;
+    static constexpr int bits       = 32;
+};
+template<>
+struct KeyTraits<uint64_t>
+{
+    static constexpr int maxLevel   = 21;
+    static constexpr int unusedBits = 1;
+    static constexpr int bits       = 64;
+};
+
+template<class K>
+__host__ __device__ __forceinline__ int clzKey(K x)
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(K) == 4) return __clz(x);
+    else return __clzll((long long)x);
+#else
+    if (x == 0) return 8 * sizeof(K);
+    if constexpr (sizeof(K) == 4) return __builtin_clz(x);
+    else return __builtin_clzll(x);
+#endif
+}
+
+template<class K>
+__host__ __device__ __forceinline__ int ctzKey(K x)
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(K) == 4) return __ffs(x) - 1;
+    else return __ffsll((long long)x) - 1;
+#else
+    if constexpr (sizeof(K) == 4) return __builtin_ctz(x);
+    else return __builtin_ctzll(x);
+#endif
+}
+
+// nodeRange(level) = 8^(maxLevel - level)
+template<class K>
+__host__ __device__ __forceinline__ K nodeRange(unsigned level)
+{
+    return K(1) << (3u * (KeyTraits<K>::maxLevel - level));
+}
+template<class K>
+__host__ __device__ __forceinline__ K removeKey()
+{
+    return nodeRange<K>(0);
+}
+// level of a node whose key range is `range` (a power of 8)
+template<class K>
+__host__ __device__ __forceinline__ unsigned treeLevel(K range)
+{
+    return unsigned(clzKey<K>(range - 1) - KeyTraits<K>::unusedBits) / 3u;
+}
+template<class K>
+__host__ __device__ __forceinline__ unsigned octalDigit(K code, unsigned pos)
+{
+    return unsigned(code >> (3u * (KeyTraits<K>::maxLevel - pos))) & 7u;
+}
+template<class K>
+__host__ __device__ __forceinline__ int commonPrefix(K a, K b)
+{
+    return clzKey<K>(a ^ b) - KeyTraits<K>::unusedBits;
+}
+template<class K>
+__host__ __device__ __forceinline__ K encodePlaceholderBit(K code, int prefixLength)
+{
+    int nShifts = 3 * KeyTraits<K>::maxLevel - prefixLength;
+    return (K(1) << prefixLength) | (code >> nShifts);
+}
+template<class K>
+__host__ __device__ __forceinline__ unsigned decodePrefixLength(K code)
+{
+    return unsigned(8 * sizeof(K) - 1 - clzKey<K>(code));
+}
+template<class K>
+__host__ __device__ __forceinline__ K decodePlaceholderBit(K code)
+{
+    unsigned len = decodePrefixLength(code);
+    return (code ^ (K(1) << len)) << (3u * KeyTraits<K>::maxLevel - len);
+}
+template<class K>
+__host__ __device__ __forceinline__ K enclosingBoxCode(K key, unsigned level)
+{
+    return key & ~(nodeRange<K>(level) - 1);
+}
+__host__ __device__ __forceinline__ int digitWeight(int digit)
+{
+    int fourGeqMask = -int(digit >= 4);
+    return ((7 - digit) & fourGeqMask) - (digit & ~fourGeqMask);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Morton and Hilbert encoders/decoders (sfc/morton.hpp, sfc/hilbert.hpp)
+// ---------------------------------------------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint32_t spreadBits10(uint32_t v)
+{
+    // each of the 10 low bits of v moves to bit 3b
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+__host__ __device__ __forceinline__ uint64_t spreadBits21(uint64_t v)
+{
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x001f00000000ffffull;
+    v = (v | (v << 16)) & 0x001f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+__host__ __device__ __forceinline__ uint32_t compactBits10(uint32_t v)
+{
+    v &= 0x09249249u;
+    v = (v ^ (v >> 2)) & 0x030c30c3u;
+    v = (v ^ (v >> 4)) & 0x0300f00fu;
+    v = (v ^ (v >> 8)) & 0x030000ffu;
+    v = (v ^ (v >> 16)) & 0x000003ffu;
+    return v;
+}
+__host__ __device__ __forceinline__ uint32_t compactBits21(uint64_t v)
+{
+    v &= 0x1249249249249249ull;
+    v = (v ^ (v >> 2)) & 0x10c30c30c30c30c3ull;
+    v = (v ^ (v >> 4)) & 0x100f00f00f00f00full;
+    v = (v ^ (v >> 8)) & 0x001f0000ff0000ffull;
+    v = (v ^ (v >> 16)) & 0x001f00000000ffffull;
+    v = (v ^ (v >> 32)) & 0x00000000001fffffull;
+    return uint32_t(v);
+}
+
+template<class K>
+__host__ __device__ __forceinline__ K iMorton(unsigned ix, unsigned iy, unsigned iz)
+{
+    if constexpr (sizeof(K) == 4) return K(spreadBits10(ix) * 4u + spreadBits10(iy) * 2u + spreadBits10(iz));
+    else return K(spreadBits21(ix) * 4u + spreadBits21(iy) * 2u + spreadBits21(iz));
+}
+
+template<class K>
+__host__ __device__ __forceinline__ void decodeMorton(K key, unsigned& ix, unsigned& iy, unsigned& iz)
+{
+    if constexpr (sizeof(K) == 4)
+    {
+        ix = compactBits10(key >> 2);
+        iy = compactBits10(key >> 1);
+        iz = compactBits10(key);
+    }
+    else
+    {
+        ix = compactBits21(key >> 2);
+        iy = compactBits21(key >> 1);
+        iz = compactBits21(key);
+    }
+}
+
+// 3D Hilbert key, one octant per level from the most significant (the curve of sfc/hilbert.hpp:43-94). The octant of
+// the current (rotated) coordinates is mapped by the table 0,1,3,2,7,6,4,5 (packed 3 bits per entry); afterwards the
+// remaining lower bits of each coordinate are conditionally complemented and the axes permuted.
+template<class K>
+__host__ __device__ __forceinline__ K iHilbert(unsigned px, unsigned py, unsigned pz)
+{
+    constexpr uint32_t m2h = (0u) | (1u << 3) | (3u << 6) | (2u << 9) | (7u << 12) | (6u << 15) | (4u << 18) | (5u << 21);
+    K key = 0;
+#pragma unroll
+    for (int level = KeyTraits<K>::maxLevel - 1; level >= 0; --level)
+    {
+        unsigned xi     = (px >> level) & 1u;
+        unsigned yi     = (py >> level) & 1u;
+        unsigned zi     = (pz >> level) & 1u;
+        unsigned octant = (xi << 2) | (yi << 1) | zi;
+        key             = (key << 3) + ((m2h >> (3 * octant)) & 7u);
+
+        unsigned nyi = yi ^ 1u, nzi = zi ^ 1u;
+        px ^= 0u - (xi & (nyi | zi));
+        py ^= 0u - ((xi & (yi | zi)) | (yi & nzi));
+        pz ^= 0u - ((xi & nyi & nzi) | (yi & nzi));
+
+        unsigned t0 = px, t1 = py, t2 = pz;
+        // zi: (x,y,z) <- (y,z,x); !zi && !yi: swap x and z
+        px = zi ? t1 : (yi ? t0 : t2);
+        py = zi ? t2 : t1;
+        pz = zi ? t0 : (yi ? t2 : t0);
+    }
+    return key;
+}
+
+template<class K>
+__host__ __device__ __forceinline__ void decodeHilbert(K key, unsigned& ox, unsigned& oy, unsigned& oz)
+{
+    unsigned px = 0, py = 0, pz = 0;
+#pragma unroll
+    for (unsigned level = 0; level < unsigned(KeyTraits<K>::maxLevel); ++level)
+    {
+        unsigned octant = unsigned(key >> (3 * level)) & 7u;
+        unsigned xi     = octant >> 2u;
+        unsigned yi     = (octant >> 1u) & 1u;
+        unsigned zi     = octant & 1u;
+        unsigned t0 = px, t1 = py, t2 = pz;
+        if (yi ^ zi)
+        {
+            px = t2;
+            py = t0;
+            pz = t1;
+        }
+        else if ((!xi & !yi & !zi) || (xi & yi & zi))
+        {
+            px = t2;
+            pz = t0;
+        }
+        unsigned mask = (1u << level) - 1u;
+        unsigned nxi = xi ^ 1u, nyi = yi ^ 1u, nzi = zi ^ 1u;
+        px ^= mask & (0u - (xi & (yi | zi)));
+        py ^= mask & (0u - ((xi & (nyi | nzi)) | (nxi & yi & zi)));
+        pz ^= mask & (0u - ((xi & nyi & nzi) | (yi & zi)));
+        px |= (xi << level);
+        py |= ((xi ^ yi) << level);
+        pz |= ((yi ^ zi) << level);
+    }
+    ox = px;
+    oy = py;
+    oz = pz;
+}
+
+template<class K>
+__host__ __device__ __forceinline__ K iSfc(unsigned ix, unsigned iy, unsigned iz, int kind)
+{
+    return kind == CS_HILBERT ? iHilbert<K>(ix, iy, iz) : iMorton<K>(ix, iy, iz);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// exactly rounded scalar arithmetic (no FMA contraction)
+// ---------------------------------------------------------------------------------------------------------------
+template<class T>
+struct RN;
+template<>
+struct RN<double>
+{
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ int toIntRz(double a) { return __double2int_rz(a); }
+    static __device__ __forceinline__ double floor_(double a) { return floor(a); }
+    static __device__ __forceinline__ double rint_(double a) { return rint(a); }
+    static __device__ __forceinline__ double abs_(double a) { return fabs(a); }
+};
+template<>
+struct RN<float>
+{
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ int toIntRz(float a) { return __float2int_rz(a); }
+    static __device__ __forceinline__ float floor_(float a) { return floorf(a); }
+    static __device__ __forceinline__ float rint_(float a) { return rintf(a); }
+    static __device__ __forceinline__ float abs_(float a) { return fabsf(a); }
+};
+
+// ---------------------------------------------------------------------------------------------------------------
+// box parameters, derived on the host in T precision exactly as cstone::Box<T> does (sfc/box.hpp:96-122)
+// ---------------------------------------------------------------------------------------------------------------
+template<class T>
+struct BoxParams
+{
+    T lo[3], hi[3], len[3], ilen[3];
+    int pbc[3];
+};
+
+template<class T>
+inline BoxParams<T> makeBoxParams(const cs_box& b)
+{
+    BoxParams<T> p;
+    for (int k = 0; k < 3; ++k)
+    {
+        p.lo[k]   = T(b.lo[k]);
+        p.hi[k]   = T(b.hi[k]);
+        p.len[k]  = p.hi[k] - p.lo[k];
+        p.ilen[k] = T(1) / (p.hi[k] - p.lo[k]);
+        p.pbc[k]  = b.boundary[k] == CS_PERIODIC;
+    }
+    return p;
+}
+
+// sfc3D (sfc/sfc.hpp:142-179) parameters: mx = 2^L * ilx and xmin * mx, both rounded in T as the reference does
+template<class T, class K>
+struct KeyParams
+{
+    T m[3];
+    T o[3];
+};
+
+template<class T, class K>
+inline KeyParams<T, K> makeKeyParams(const BoxParams<T>& b)
+{
+    KeyParams<T, K> p;
+    unsigned cube = 1u << KeyTraits<K>::maxLevel;
+    for (int k = 0; k < 3; ++k)
+    {
+        p.m[k] = T(cube) * b.ilen[k];
+        p.o[k] = b.lo[k] * p.m[k];
+    }
+    return p;
+}
+
+template<class T, class K>
+__device__ __forceinline__ K sfc3D(T x, T y, T z, const KeyParams<T, K>& p, int kind)
+{
+    constexpr int mcoord = (1 << KeyTraits<K>::maxLevel) - 1;
+    int ix = RN<T>::toIntRz(RN<T>::sub(RN<T>::floor_(RN<T>::mul(x, p.m[0])), p.o[0]));
+    int iy = RN<T>::toIntRz(RN<T>::sub(RN<T>::floor_(RN<T>::mul(y, p.m[1])), p.o[1]));
+    int iz = RN<T>::toIntRz(RN<T>::sub(RN<T>::floor_(RN<T>::mul(z, p.m[2])), p.o[2]));
+    ix     = min(ix, mcoord);
+    iy     = min(iy, mcoord);
+    iz     = min(iz, mcoord);
+    return iSfc<K>(unsigned(ix), unsigned(iy), unsigned(iz), kind);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// status plumbing
+// ---------------------------------------------------------------------------------------------------------------
+void setLastError(const char* fmt, ...);
+
+#define CSG_CUDA_TRY(call)                                                                                             \
+    do                                                                                                                 \
+    {                                                                                                                  \
+        cudaError_t err_ = (call);                                                                                     \
+        if (err_ != cudaSuccess)                                                                                       \
+        {                                                                                                              \
+            ::csg::setLastError("%s:%d: %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(err_));                 \
+            return CS_ERR_CUDA;                                                                                        \
+        }                                                                                                              \
+    } while (0)
+
+#define CSG_CHECK_LAUNCH() CSG_CUDA_TRY(cudaGetLastError())
+
+inline unsigned iceil(size_t a, size_t b) { return unsigned((a + b - 1) / b); }
+
+// number of SMs of the current device (cached per device)
+int smCount();
+
+// bump allocator over a caller workspace; `size` only accumulates when base == nullptr (size query)
+struct Arena
+{
+    char* base   = nullptr;
+    size_t size  = 0;
+    size_t limit = 0;
+
+    template<class T>
+    T* take(size_t n, size_t align = 256)
+    {
+        size_t off = (size + align - 1) / align * align;
+        size       = off + n * sizeof(T);
+        return base ? reinterpret_cast<T*>(base + off) : nullptr;
+    }
+    bool ok() const { return base == nullptr || size <= limit; }
+};
+
+// workspace helper: uses the caller's buffer when given, else a stream-ordered allocation freed on release()
+struct Workspace
+{
+    void* ptr        = nullptr;
+    bool owned       = false;
+    cudaStream_t str = nullptr;
+
+    int acquire(void* userPtr, size_t userBytes, size_t needed, cudaStream_t s)
+    {
+        str = s;
+        if (needed == 0) return CS_OK;
+        if (userPtr)
+        {
+            if (userBytes < needed)
+            {
+                setLastError("workspace too small: %zu bytes given, %zu needed", userBytes, needed);
+                return CS_ERR_INVALID;
+            }
+            ptr = userPtr;
+            return CS_OK;
+        }
+        CSG_CUDA_TRY(cudaMallocAsync(&ptr, needed, s));
+        owned = true;
+        return CS_OK;
+    }
+    ~Workspace()
+    {
+        if (owned && ptr) cudaFreeAsync(ptr, str);
+    }
+};
+
+} // namespace csg

@@ -1,0 +1,253 @@
+// Halo discovery: per-leaf h-expanded search boxes (focus/source_center.hpp:28-43, focus/source_center_gpu.cu:23-92)
+// and the collision traversal that flags every node outside the focus key range that overlaps a focus leaf's search
+// box (traversal/collisions.hpp:25-94, traversal/collisions_gpu.cu:23-77, traversal/boxoverlap.hpp:127-291).
+//
+// Search boxes: 8 lanes per leaf stride over its particles; min/max are exact, so any reduction order gives the
+// reference's bits. Collisions: one thread per focus leaf, stackless traversal over childOffsets/parents exactly as
+// singleTraversal (traversal/traversal.hpp:26-69); floating-point expressions unfused, in the reference's order.
+#include "cs_common.cuh"
+#include "halos.cuh"
+
+namespace csg
+{
+
+template<class T>
+__global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z,
+                                  const T* __restrict__ h, const uint32_t* __restrict__ layout, int firstLeaf,
+                                  int lastLeaf, T scale, const int32_t* __restrict__ l2i,
+                                  const T* __restrict__ nodeCenters, T* __restrict__ sc, T* __restrict__ ss)
+{
+    constexpr int TPL = 8;
+    int gtid          = blockIdx.x * blockDim.x + threadIdx.x;
+    int leaf          = firstLeaf + gtid / TPL;
+    int sub           = gtid % TPL;
+    bool valid        = leaf < lastLeaf;
+    T mn[3], mx[3];
+    if (valid)
+    {
+        const T* init = nodeCenters + 3 * size_t(l2i[leaf]);
+        for (int k = 0; k < 3; ++k)
+            mn[k] = mx[k] = init[k];
+        uint32_t first = layout[leaf], last = layout[leaf + 1];
+        for (uint32_t i = first + sub; i < last; i += TPL)
+        {
+            T r    = RN<T>::mul(h[i], scale);
+            T p[3] = {x[i], y[i], z[i]};
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+            {
+                T lo  = RN<T>::sub(p[k], r);
+                T hi  = RN<T>::add(p[k], r);
+                mn[k] = lo < mn[k] ? lo : mn[k];
+                mx[k] = mx[k] < hi ? hi : mx[k];
+            }
+        }
+    }
+    else
+    {
+        for (int k = 0; k < 3; ++k)
+            mn[k] = mx[k] = T(0);
+    }
+#pragma unroll
+    for (int o = 1; o < TPL; o <<= 1)
+    {
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            T a   = __shfl_down_sync(0xffffffffu, mn[k], o, TPL);
+            T b   = __shfl_down_sync(0xffffffffu, mx[k], o, TPL);
+            mn[k] = a < mn[k] ? a : mn[k];
+            mx[k] = mx[k] < b ? b : mx[k];
+        }
+    }
+    if (valid && sub == 0)
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            sc[3 * size_t(leaf) + k] = RN<T>::mul(RN<T>::add(mx[k], mn[k]), T(0.5));
+            ss[3 * size_t(leaf) + k] = RN<T>::mul(RN<T>::sub(mx[k], mn[k]), T(0.5));
+        }
+    }
+}
+
+template<class T>
+int searchBoxes(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, const uint32_t* layout, int first,
+                int last, T scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss)
+{
+    if (last <= first) return CS_OK;
+    size_t threads = size_t(last - first) * 8;
+    searchBoxesKernel<T><<<iceil(threads, 256), 256, 0, s>>>(x, y, z, h, layout, first, last, scale, l2i, nodeCenters,
+                                                             sc, ss);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template<class T>
+__device__ __forceinline__ T pbcFold(T d, int pbc, T len, T ilen)
+{
+    // d - pbc * len * rint(d * ilen)   (applyPbc, sfc/box.hpp:178-190)
+    return RN<T>::sub(d, RN<T>::mul(RN<T>::mul(T(pbc), len), RN<T>::rint_(RN<T>::mul(d, ilen))));
+}
+
+template<class K, class T>
+__device__ bool boxContainedIn(K codeStart, K codeEnd, const T* center, const T* size, const BoxParams<T>& b,
+                               const KeyParams<T, K>& kp)
+{
+    T bmin[3], bmax[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        bmin[k] = RN<T>::sub(center[k], size[k]);
+        bmax[k] = RN<T>::add(center[k], size[k]);
+    }
+    T d0 = RN<T>::sub(bmin[0], b.lo[0]), d1 = RN<T>::sub(bmin[1], b.lo[1]), d2 = RN<T>::sub(bmin[2], b.lo[2]);
+    T dmin = d0;
+    dmin   = dmin < d1 ? dmin : d1;
+    dmin   = dmin < d2 ? dmin : d2;
+    T e0 = RN<T>::sub(bmax[0], b.hi[0]), e1 = RN<T>::sub(bmax[1], b.hi[1]), e2 = RN<T>::sub(bmax[2], b.hi[2]);
+    T dmax = e0;
+    dmax   = dmax > e1 ? dmax : e1;
+    dmax   = dmax > e2 ? dmax : e2;
+    if (dmin < T(0) || dmax > T(0)) return codeStart == 0 && codeEnd == nodeRange<K>(0);
+
+    const T unit = T(1) / T(1 << KeyTraits<K>::maxLevel);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        bmax[k] = RN<T>::add(bmax[k], RN<T>::mul(b.len[k], unit));
+    K lo       = sfc3D<T, K>(bmin[0], bmin[1], bmin[2], kp, CS_HILBERT);
+    K hi       = sfc3D<T, K>(bmax[0], bmax[1], bmax[2], kp, CS_HILBERT);
+    unsigned l = unsigned(commonPrefix<K>(lo, hi)) / 3u;
+    K s        = enclosingBoxCode<K>(lo, l);
+    K e        = s + nodeRange<K>(l);
+    return s >= codeStart && e <= codeEnd;
+}
+
+template<class K, class T>
+__global__ void findHalosKernel(const K* __restrict__ prefixes, const int32_t* __restrict__ childOffsets,
+                                const int32_t* __restrict__ parents, const T* __restrict__ nc,
+                                const T* __restrict__ ns, const K* __restrict__ leaves, const T* __restrict__ sc,
+                                const T* __restrict__ ss, BoxParams<T> b, KeyParams<T, K> kp, int firstNode,
+                                int lastNode, uint8_t* flags)
+{
+    int leaf = firstNode + blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= lastNode) return;
+    const K lowest  = leaves[firstNode];
+    const K highest = leaves[lastNode];
+    T tc[3], ts[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        tc[k] = sc[3 * size_t(leaf) + k];
+        ts[k] = ss[3 * size_t(leaf) + k];
+    }
+    if (boxContainedIn<K, T>(lowest, highest, tc, ts, b, kp)) return;
+
+    auto overlaps = [&](int idx) -> bool {
+        K pfx         = prefixes[idx];
+        K nk1         = decodePlaceholderBit<K>(pfx);
+        unsigned plen = decodePrefixLength<K>(pfx);
+        K nk2         = nk1 + (K(1) << (3u * KeyTraits<K>::maxLevel - plen));
+        bool inside   = !(nk1 < lowest || nk2 > highest);
+        if (inside) return false;
+        bool ov = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            T d = RN<T>::sub(tc[k], nc[3 * size_t(idx) + k]);
+            d   = RN<T>::abs_(pbcFold<T>(d, b.pbc[k], b.len[k], b.ilen[k]));
+            d   = RN<T>::sub(d, ns[3 * size_t(idx) + k]);
+            d   = RN<T>::sub(d, ts[k]);
+            ov  = ov && (d < T(0));
+        }
+        if (ov) flags[idx] = 1;
+        return ov;
+    };
+
+    if (!overlaps(0) || childOffsets[0] == 0) return;
+    int node       = childOffsets[0];
+    bool backtrack = false;
+    while (node != 0)
+    {
+        bool isLeaf  = childOffsets[node] == 0;
+        bool descend = !backtrack && overlaps(node);
+        int sib      = (node - 1) % 8;
+        if (!isLeaf && descend)
+        {
+            node      = childOffsets[node];
+            backtrack = false;
+        }
+        else if (sib < 7)
+        {
+            node++;
+            backtrack = false;
+        }
+        else
+        {
+            node      = parents[(node - 1) / 8];
+            backtrack = true;
+        }
+    }
+}
+
+template<class K, class T>
+int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, const int32_t* parents, const T* nc,
+              const T* ns, const K* leaves, const T* sc, const T* ss, const cs_box& box, int first, int last,
+              uint8_t* flags)
+{
+    if (last <= first) return CS_OK;
+    auto bp = makeBoxParams<T>(box);
+    auto kp = makeKeyParams<T, K>(bp);
+    findHalosKernel<K, T><<<iceil(size_t(last - first), 128), 128, 0, s>>>(prefixes, childOffsets, parents, nc, ns,
+                                                                          leaves, sc, ss, bp, kp, first, last, flags);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template int searchBoxes<float>(cudaStream_t, const float*, const float*, const float*, const float*, const uint32_t*,
+                                int, int, float, const int32_t*, const float*, float*, float*);
+template int searchBoxes<double>(cudaStream_t, const double*, const double*, const double*, const double*,
+                                 const uint32_t*, int, int, double, const int32_t*, const double*, double*, double*);
+template int findHalos<uint32_t, float>(cudaStream_t, const uint32_t*, const int32_t*, const int32_t*, const float*,
+                                        const float*, const uint32_t*, const float*, const float*, const cs_box&, int,
+                                        int, uint8_t*);
+template int findHalos<uint64_t, float>(cudaStream_t, const uint64_t*, const int32_t*, const int32_t*, const float*,
+                                        const float*, const uint64_t*, const float*, const float*, const cs_box&, int,
+                                        int, uint8_t*);
+template int findHalos<uint64_t, double>(cudaStream_t, const uint64_t*, const int32_t*, const int32_t*, const double*,
+                                         const double*, const uint64_t*, const double*, const double*, const cs_box&,
+                                         int, int, uint8_t*);
+
+} // namespace csg
+
+using namespace csg;
+
+extern "C" int cs_search_boxes_f32(cs_stream_t stream, const float* x, const float* y, const float* z, const float* h,
+                                   const uint32_t* layout, int32_t first, int32_t last, float scale,
+                                   const int32_t* l2i, const float* nc, float* sc, float* ss)
+{
+    return searchBoxes<float>(cudaStream_t(stream), x, y, z, h, layout, first, last, scale, l2i, nc, sc, ss);
+}
+extern "C" int cs_search_boxes_f64(cs_stream_t stream, const double* x, const double* y, const double* z,
+                                   const double* h, const uint32_t* layout, int32_t first, int32_t last, double scale,
+                                   const int32_t* l2i, const double* nc, double* sc, double* ss)
+{
+    return searchBoxes<double>(cudaStream_t(stream), x, y, z, h, layout, first, last, scale, l2i, nc, sc, ss);
+}
+
+#define CS_HALOS_ENTRY(kb, K, tb, T)                                                                                   \
+    extern "C" int cs_find_halos_##kb##_##tb(cs_stream_t stream, const K* prefixes, const int32_t* childOffsets,       \
+                                             const int32_t* parents, const T* nc, const T* ns, const K* leaves,         \
+                                             const T* sc, const T* ss, const cs_box* box, int32_t first,               \
+                                             int32_t last, uint8_t* flags)                                              \
+    {                                                                                                                  \
+        if (!box)                                                                                                      \
+        {                                                                                                              \
+            setLastError("find halos: null box");                                                                      \
+            return CS_ERR_INVALID;                                                                                     \
+        }                                                                                                              \
+        return findHalos<K, T>(cudaStream_t(stream), prefixes, childOffsets, parents, nc, ns, leaves, sc, ss, *box,    \
+                               first, last, flags);                                                                    \
+    }
+CS_HALOS_ENTRY(u32, uint32_t, f32, float)
+CS_HALOS_ENTRY(u64, uint64_t, f32, float)
+CS_HALOS_ENTRY(u64, uint64_t, f64, double)

@@ -1,0 +1,17 @@
+// Internal interface of halo discovery (halos.cu).
+#pragma once
+#include "cs_common.cuh"
+
+namespace csg
+{
+
+template<class T>
+int searchBoxes(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, const uint32_t* layout, int first,
+                int last, T scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss);
+
+template<class K, class T>
+int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, const int32_t* parents, const T* nc,
+              const T* ns, const K* leaves, const T* sc, const T* ss, const cs_box& box, int first, int last,
+              uint8_t* flags);
+
+} // namespace csg

@@ -1,0 +1,49 @@
+// Internal interface of the neighbour search (neighbors.cu).
+#pragma once
+#include "cs_common.cuh"
+
+namespace csg
+{
+
+template<class T>
+struct NbArgs
+{
+    const T *x, *y, *z, *h;
+    uint32_t first, last;
+    BoxParams<T> b;
+    int anyPbc;
+    const int32_t* childOffsets;
+    const int32_t* parents;
+    const int32_t* i2l;
+    const uint32_t* layout;
+    const T* centers;
+    const T* sizes;
+    float ext;
+    unsigned ngmax;
+    uint32_t* nb;
+    uint32_t* nc;
+};
+
+//! float shadows for the FP64 pre-filter: particles x = hi + lo (two floats), node centres hi + lo, node sizes
+struct NbPrep
+{
+    const float4* phi = nullptr;
+    const float4* plo = nullptr;
+    const float4* chi = nullptr;
+    const float4* clo = nullptr;
+    const float4* sz  = nullptr;
+    const float* cmax = nullptr; // bound on |coordinate| over particles and node boxes
+};
+
+size_t nbPrepBytes(size_t n, int numNodes);
+int nbPrepare(cudaStream_t s, const double* x, const double* y, const double* z, size_t n, const double* centers,
+              const double* sizes, int numNodes, void* ws, size_t wsBytes, NbPrep* prep);
+
+template<class T>
+NbArgs<T> makeNbArgs(const T* x, const T* y, const T* z, const T* h, uint32_t first, uint32_t last,
+                     const cs_box& box, const cs_ns_view& v, unsigned ngmax, uint32_t* nb, uint32_t* nc);
+
+template<class T>
+int findNeighbors(cudaStream_t s, const NbArgs<T>& a, const NbPrep& prep);
+
+} // namespace csg

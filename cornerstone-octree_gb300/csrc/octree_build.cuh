@@ -1,0 +1,47 @@
+// Internal interface of the cornerstone leaf-array build (octree_build.cu).
+#pragma once
+#include "cs_common.cuh"
+
+namespace csg
+{
+
+constexpr uint32_t ERRBIT_BARRIER_TIMEOUT = 2u;
+constexpr uint32_t ERRBIT_CAPACITY        = 4u;
+constexpr uint32_t ERRBIT_NO_CONVERGENCE  = 8u;
+
+struct BuildResult
+{
+    int numLeaves  = 0;
+    int iterations = 0;
+    int converged  = 0;
+    int needed     = 0;
+    int maxDepth   = 0; // deepest leaf level
+    int focusFirst = 0; // lower_bound(leaves, focus.start)
+    int focusLast  = 0; // lower_bound(leaves, focus.end)
+    int* stateDev  = nullptr; // device address of the state block (numLeaves, iterations, needed, err, converged)
+};
+
+//! optional: leaf range [lower_bound(start), lower_bound(end)) of a key range, computed by the build's last phase
+template<class K>
+struct FocusQuery
+{
+    K start     = 0;
+    K end       = 0;
+    bool enable = false;
+};
+
+template<class K>
+size_t octreeBuildWorkspaceBytes(int capacity, bool update);
+
+/*! Build (treeIn == nullptr: computeOctree from the root) or update (one updateOctree step from treeIn/countsIn).
+ *  With sync == false the call only enqueues work; the state block (see BuildResult::stateDev) holds the outcome. */
+template<class K>
+int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32_t maxCount, const K* treeIn,
+                const uint32_t* countsIn, int Lin, K* treeOut, uint32_t* countsOut, uint32_t* layoutOut, int capacity,
+                void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus = FocusQuery<K>{});
+
+template<class K>
+int nodeCounts(cudaStream_t s, const K* tree, uint32_t* counts, int numNodes, const K* keys, size_t n,
+               uint32_t maxCount, void* ws, size_t wsBytes);
+
+} // namespace csg

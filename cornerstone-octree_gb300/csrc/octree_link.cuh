@@ -1,0 +1,21 @@
+// Internal interface of the octree linkage and node geometry (octree_link.cu).
+#pragma once
+#include "cs_common.cuh"
+
+namespace csg
+{
+
+template<class K>
+size_t buildLinkWorkspaceBytes(int L);
+
+/*! Link the internal tree of leaves[0..L] into `v`. prefixBits (0 = full key width) limits the radix sort of the
+ *  placeholder prefixes to their significant bits (3 * deepest leaf level + 1). errWord: device word for sort
+ *  timeouts (nullptr = internal). */
+template<class K>
+int buildLink(cudaStream_t s, const K* leaves, int L, const cs_octree_view& v, int prefixBits, void* ws,
+              size_t wsBytes, uint32_t* errWord);
+
+template<class K, class T>
+int geoCenters(cudaStream_t s, const K* prefixes, int N, T* centers, T* sizes, const cs_box& box, int kind);
+
+} // namespace csg

@@ -1,0 +1,404 @@
+// The whole single-GPU path behind one C-ABI object: keys -> stable sort -> gather -> computeOctree -> link ->
+// node geometry -> search boxes + findHalos -> findNeighbors. The object owns its device buffers and only grows
+// them, so repeated runs (time steps, requests) allocate nothing once sized. The only host synchronisation per run
+// is the one that returns the leaf count of the build (the reference's updateOctreeGpu synchronises three times per
+// rebalance iteration; here the whole rebalance loop is one cooperative launch).
+#include "cs_common.cuh"
+#include "halos.cuh"
+#include "neighbors.cuh"
+#include "octree_build.cuh"
+#include "octree_link.cuh"
+#include "radix_sort.cuh"
+#include "sfc_keys.cuh"
+
+#include <algorithm>
+#include <memory>
+#include <type_traits>
+
+namespace csg
+{
+
+struct DevBuf
+{
+    void* p      = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need)
+    {
+        if (need <= bytes) return CS_OK;
+        if (p) cudaFree(p);
+        p     = nullptr;
+        bytes = 0;
+        size_t alloc = need + need / 8 + 256;
+        CSG_CUDA_TRY(cudaMalloc(&p, alloc));
+        bytes = alloc;
+        return CS_OK;
+    }
+    template<class T>
+    T* as() const
+    {
+        return static_cast<T*>(p);
+    }
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
+enum Stage
+{
+    ST_KEYS,
+    ST_SORT,
+    ST_GATHER,
+    ST_BUILD,
+    ST_LINK,
+    ST_GEO,
+    ST_HALOS,
+    ST_NBPREP,
+    ST_NEIGHBORS,
+    ST_COUNT
+};
+
+struct PipelineBase
+{
+    cs_pipeline_config cfg{};
+    virtual ~PipelineBase() = default;
+    virtual int run(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, size_t n,
+                    const cs_box& box, uint64_t f0, uint64_t f1, cs_pipeline_result* res, bool hostIn) = 0;
+    virtual int outputs(cs_pipeline_outputs* o) = 0;
+    virtual size_t deviceBytes() const          = 0;
+    virtual int copyBack(cudaStream_t s, uint32_t* nc, uint8_t* flags, size_t flagsCap) = 0;
+    cudaEvent_t ev[ST_COUNT + 1] = {};
+    float stageMs[ST_COUNT]      = {};
+    int lastN                    = 0;
+};
+
+template<class T, class K>
+struct Pipeline final : PipelineBase
+{
+    DevBuf inX, inY, inZ, inH;
+    DevBuf keys, keysAlt, order, orderAlt;
+    DevBuf xs, ys, zs, hs;
+    DevBuf sortWs, errWords;
+    DevBuf buildWs, leaves, counts, layout;
+    DevBuf prefixes, childOffsets, parents, levelRange, i2l, l2i, linkWs;
+    DevBuf centers, sizes, sc, ss, flags;
+    DevBuf nbPrepWs, nb, nc;
+    int capacity = 0;
+    size_t n     = 0;
+    cs_pipeline_result last{};
+    K* sortedKeys = nullptr;
+    uint32_t* sortedOrder = nullptr;
+
+    Pipeline()
+    {
+        for (auto& e : ev)
+            cudaEventCreate(&e);
+    }
+    ~Pipeline() override
+    {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+
+    size_t deviceBytes() const override
+    {
+        size_t t = 0;
+        for (const DevBuf* b : {&inX, &inY, &inZ, &inH, &keys, &keysAlt, &order, &orderAlt, &xs, &ys, &zs, &hs,
+                                &sortWs, &errWords, &buildWs, &leaves, &counts, &layout, &prefixes, &childOffsets,
+                                &parents, &levelRange, &i2l, &l2i, &linkWs, &centers, &sizes, &sc, &ss, &flags,
+                                &nbPrepWs, &nb, &nc})
+            t += b->bytes;
+        return t;
+    }
+
+    int run(cudaStream_t s, const void* xv, const void* yv, const void* zv, const void* hv, size_t nIn,
+            const cs_box& box, uint64_t f0, uint64_t f1, cs_pipeline_result* res, bool hostIn) override
+    {
+        n  = nIn;
+        int rc;
+        constexpr int KB = 8 * sizeof(K);
+        if (n == 0 || n >= (size_t(1) << 30))
+        {
+            setLastError("pipeline: n = %zu outside [1, 2^30)", n);
+            return CS_ERR_INVALID;
+        }
+        const T *x = static_cast<const T*>(xv), *y = static_cast<const T*>(yv), *z = static_cast<const T*>(zv),
+                *h = static_cast<const T*>(hv);
+        if (hostIn)
+        {
+            for (DevBuf* b : {&inX, &inY, &inZ, &inH})
+                if ((rc = b->ensure(n * sizeof(T)))) return rc;
+            CSG_CUDA_TRY(cudaMemcpyAsync(inX.p, x, n * sizeof(T), cudaMemcpyHostToDevice, s));
+            CSG_CUDA_TRY(cudaMemcpyAsync(inY.p, y, n * sizeof(T), cudaMemcpyHostToDevice, s));
+            CSG_CUDA_TRY(cudaMemcpyAsync(inZ.p, z, n * sizeof(T), cudaMemcpyHostToDevice, s));
+            CSG_CUDA_TRY(cudaMemcpyAsync(inH.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+            x = inX.as<T>();
+            y = inY.as<T>();
+            z = inZ.as<T>();
+            h = inH.as<T>();
+        }
+        for (DevBuf* b : {&keys, &keysAlt})
+            if ((rc = b->ensure(n * sizeof(K)))) return rc;
+        for (DevBuf* b : {&order, &orderAlt})
+            if ((rc = b->ensure(n * sizeof(uint32_t)))) return rc;
+        for (DevBuf* b : {&xs, &ys, &zs, &hs})
+            if ((rc = b->ensure(n * sizeof(T)))) return rc;
+        // keys have 3*maxLevel significant bits (no removeKey entries: they are computed here)
+        const int keyBits = 3 * KeyTraits<K>::maxLevel;
+        if ((rc = sortWs.ensure(radixSortWorkspaceBytes<K>(n, 0, keyBits)))) return rc;
+        if ((rc = errWords.ensure(64))) return rc;
+        uint32_t* err = errWords.as<uint32_t>();
+        CSG_CUDA_TRY(cudaMemsetAsync(err, 0, 64, s));
+
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_KEYS], s));
+        if ((rc = sfcKeys<T, K>(s, x, y, z, keys.as<K>(), n, box, cfg.sfc_kind, false))) return rc;
+
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_SORT], s));
+        bool inAlt = false;
+        rc = radixSortPairs<K>(s, keys.as<K>(), order.as<uint32_t>(), keysAlt.as<K>(), orderAlt.as<uint32_t>(), n, 0,
+                               keyBits, true, sortWs.p, sortWs.bytes, err, &inAlt);
+        if (rc) return rc;
+        sortedKeys  = inAlt ? keysAlt.as<K>() : keys.as<K>();
+        sortedOrder = inAlt ? orderAlt.as<uint32_t>() : order.as<uint32_t>();
+
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_GATHER], s));
+        GatherArgs<T, 4> ga{{x, y, z, h}, {xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>()}};
+        if ((rc = gatherN<T, 4>(s, sortedOrder, n, ga))) return rc;
+
+        // ---- cornerstone build: grow the capacity until the converged tree fits ----
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_BUILD], s));
+        if (capacity == 0) capacity = int(std::min<size_t>(size_t(1) << 30, n / std::max(1u, cfg.bucket_size) * 16 + 4096));
+        BuildResult br;
+        for (;;)
+        {
+            if ((rc = buildWs.ensure(octreeBuildWorkspaceBytes<K>(capacity, false)))) return rc;
+            if ((rc = leaves.ensure((size_t(capacity) + 1) * sizeof(K)))) return rc;
+            if ((rc = counts.ensure(size_t(capacity) * sizeof(uint32_t)))) return rc;
+            if ((rc = layout.ensure((size_t(capacity) + 1) * sizeof(uint32_t)))) return rc;
+            br = BuildResult{};
+            rc = octreeBuild<K>(s, sortedKeys, n, cfg.bucket_size, cfg.max_count, nullptr, nullptr, 0, leaves.as<K>(),
+                                counts.as<uint32_t>(), layout.as<uint32_t>(), capacity, buildWs.p, buildWs.bytes, &br,
+                                true, FocusQuery<K>{K(f0), K(f1), cfg.do_halos != 0});
+            if (rc == CS_ERR_CAPACITY)
+            {
+                capacity = std::max(2 * capacity, br.needed + br.needed / 4);
+                continue;
+            }
+            if (rc) return rc;
+            break;
+        }
+        const int L = br.numLeaves, I = (L - 1) / 7, N = L + I;
+
+        // ---- internal tree ----
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_LINK], s));
+        if ((rc = prefixes.ensure(size_t(N) * sizeof(K)))) return rc;
+        if ((rc = childOffsets.ensure((size_t(N) + 1) * sizeof(int32_t)))) return rc;
+        if ((rc = parents.ensure(size_t(std::max(1, (N - 1) / 8)) * sizeof(int32_t)))) return rc;
+        if ((rc = levelRange.ensure(size_t(KeyTraits<K>::maxLevel + 2) * sizeof(int32_t)))) return rc;
+        if ((rc = i2l.ensure(size_t(N) * sizeof(int32_t)))) return rc;
+        if ((rc = l2i.ensure(size_t(N) * sizeof(int32_t)))) return rc;
+        if ((rc = linkWs.ensure(buildLinkWorkspaceBytes<K>(L)))) return rc;
+        cs_octree_view v{L, I, N, prefixes.p, childOffsets.as<int32_t>(), parents.as<int32_t>(),
+                         levelRange.as<int32_t>(), i2l.as<int32_t>(), l2i.as<int32_t>()};
+        int prefixBits = std::min(KB, 3 * br.maxDepth + 1);
+        if ((rc = buildLink<K>(s, leaves.as<K>(), L, v, prefixBits, linkWs.p, linkWs.bytes, err + 1))) return rc;
+
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_GEO], s));
+        if ((rc = centers.ensure(3 * size_t(N) * sizeof(T)))) return rc;
+        if ((rc = sizes.ensure(3 * size_t(N) * sizeof(T)))) return rc;
+        if ((rc = geoCenters<K, T>(s, prefixes.as<K>(), N, centers.as<T>(), sizes.as<T>(), box, cfg.sfc_kind))) return rc;
+
+        // ---- halos for the focus leaves ----
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_HALOS], s));
+        if ((rc = flags.ensure(size_t(N)))) return rc;
+        CSG_CUDA_TRY(cudaMemsetAsync(flags.p, 0, size_t(N), s));
+        if (cfg.do_halos && br.focusLast > br.focusFirst)
+        {
+            if ((rc = sc.ensure(3 * size_t(L) * sizeof(T)))) return rc;
+            if ((rc = ss.ensure(3 * size_t(L) * sizeof(T)))) return rc;
+            T scale = T(2.0f * cfg.halo_search_ext);
+            if ((rc = searchBoxes<T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), layout.as<uint32_t>(),
+                                     br.focusFirst, br.focusLast, scale, l2i.as<int32_t>() + I, centers.as<T>(),
+                                     sc.as<T>(), ss.as<T>())))
+                return rc;
+            if constexpr (!(std::is_same_v<K, uint32_t> && std::is_same_v<T, double>))
+            {
+                if ((rc = findHalos<K, T>(s, prefixes.as<K>(), childOffsets.as<int32_t>(), parents.as<int32_t>(),
+                                          centers.as<T>(), sizes.as<T>(), leaves.as<K>(), sc.as<T>(), ss.as<T>(), box,
+                                          br.focusFirst, br.focusLast, flags.as<uint8_t>())))
+                    return rc;
+            }
+        }
+
+        // ---- neighbours ----
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_NBPREP], s));
+        if ((rc = nc.ensure(n * sizeof(uint32_t)))) return rc;
+        NbPrep prep{};
+        if (cfg.do_neighbors)
+        {
+            if ((rc = nb.ensure(std::max<size_t>(1, n * cfg.ngmax) * sizeof(uint32_t)))) return rc;
+            if constexpr (std::is_same_v<T, double>)
+            {
+                if ((rc = nbPrepWs.ensure(nbPrepBytes(n, N)))) return rc;
+                if ((rc = nbPrepare(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), n, centers.as<T>(), sizes.as<T>(), N,
+                                    nbPrepWs.p, nbPrepWs.bytes, &prep)))
+                    return rc;
+            }
+        }
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_NEIGHBORS], s));
+        if (cfg.do_neighbors)
+        {
+            cs_ns_view nv{L, N, childOffsets.as<int32_t>(), parents.as<int32_t>(), i2l.as<int32_t>(),
+                          layout.as<uint32_t>(), centers.p, sizes.p, cfg.search_ext};
+            NbArgs<T> a = makeNbArgs<T>(xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), 0, uint32_t(n), box, nv,
+                                        cfg.ngmax, nb.as<uint32_t>(), nc.as<uint32_t>());
+            if ((rc = findNeighbors<T>(s, a, prep))) return rc;
+        }
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_COUNT], s));
+
+        last             = cs_pipeline_result{L, N, br.iterations, br.focusFirst, br.focusLast, br.maxDepth};
+        lastN            = 1;
+        if (res) *res    = last;
+        return CS_OK;
+    }
+
+    int copyBack(cudaStream_t s, uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap) override
+    {
+        if (ncHost) CSG_CUDA_TRY(cudaMemcpyAsync(ncHost, nc.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        if (flagsHost)
+        {
+            if (flagsCap < size_t(last.num_nodes))
+            {
+                setLastError("pipeline: halo flag buffer holds %zu, %d needed", flagsCap, last.num_nodes);
+                return CS_ERR_CAPACITY;
+            }
+            CSG_CUDA_TRY(cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, s));
+        }
+        uint32_t herr[2] = {0, 0};
+        CSG_CUDA_TRY(cudaMemcpyAsync(herr, errWords.p, sizeof(herr), cudaMemcpyDeviceToHost, s));
+        CSG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (herr[0] | herr[1])
+        {
+            setLastError("pipeline: a bounded device wait timed out (sort look-back)");
+            return CS_ERR_TIMEOUT;
+        }
+        return CS_OK;
+    }
+
+    int outputs(cs_pipeline_outputs* o) override
+    {
+        if (!lastN)
+        {
+            setLastError("pipeline: no run yet");
+            return CS_ERR_INVALID;
+        }
+        int L = last.num_leaves, N = last.num_nodes, I = N - L;
+        o->sorted_keys     = sortedKeys;
+        o->order           = sortedOrder;
+        o->x               = xs.p;
+        o->y               = ys.p;
+        o->z               = zs.p;
+        o->h               = hs.p;
+        o->leaves          = leaves.p;
+        o->counts          = counts.as<uint32_t>();
+        o->layout          = layout.as<uint32_t>();
+        o->octree          = cs_octree_view{L, I, N, prefixes.p, childOffsets.as<int32_t>(), parents.as<int32_t>(),
+                                   levelRange.as<int32_t>(), i2l.as<int32_t>(), l2i.as<int32_t>()};
+        o->centers         = centers.p;
+        o->sizes           = sizes.p;
+        o->halo_flags      = flags.as<uint8_t>();
+        o->neighbors       = cfg.do_neighbors ? nb.as<uint32_t>() : nullptr;
+        o->neighbor_counts = nc.as<uint32_t>();
+        return CS_OK;
+    }
+};
+
+} // namespace csg
+
+using namespace csg;
+
+struct cs_pipeline_s
+{
+    std::unique_ptr<PipelineBase> impl;
+};
+
+extern "C" int cs_pipeline_create(cs_pipeline* out, int coord_bits, int key_bits, const cs_pipeline_config* cfg)
+{
+    if (!out || !cfg || (coord_bits != 32 && coord_bits != 64) || (key_bits != 32 && key_bits != 64) ||
+        cfg->bucket_size == 0)
+    {
+        setLastError("pipeline create: invalid arguments");
+        return CS_ERR_INVALID;
+    }
+    auto* p = new cs_pipeline_s;
+    if (coord_bits == 64 && key_bits == 64) p->impl = std::make_unique<Pipeline<double, uint64_t>>();
+    else if (coord_bits == 64) p->impl = std::make_unique<Pipeline<double, uint32_t>>();
+    else if (key_bits == 64) p->impl = std::make_unique<Pipeline<float, uint64_t>>();
+    else p->impl = std::make_unique<Pipeline<float, uint32_t>>();
+    p->impl->cfg = *cfg;
+    *out         = p;
+    return CS_OK;
+}
+
+extern "C" int cs_pipeline_destroy(cs_pipeline p)
+{
+    delete p;
+    return CS_OK;
+}
+
+extern "C" int cs_pipeline_run(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
+                               const void* h, size_t n, const cs_box* box, uint64_t f0, uint64_t f1,
+                               cs_pipeline_result* res)
+{
+    if (!p || !box || !x || !y || !z || !h)
+    {
+        setLastError("pipeline run: null argument");
+        return CS_ERR_INVALID;
+    }
+    return p->impl->run(cudaStream_t(stream), x, y, z, h, n, *box, f0, f1, res, false);
+}
+
+extern "C" int cs_pipeline_run_host(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
+                                    const void* h, size_t n, const cs_box* box, uint64_t f0, uint64_t f1,
+                                    uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap, cs_pipeline_result* res)
+{
+    if (!p || !box || !x || !y || !z || !h)
+    {
+        setLastError("pipeline run: null argument");
+        return CS_ERR_INVALID;
+    }
+    int rc = p->impl->run(cudaStream_t(stream), x, y, z, h, n, *box, f0, f1, res, true);
+    if (rc) return rc;
+    return p->impl->copyBack(cudaStream_t(stream), ncHost, flagsHost, flagsCap);
+}
+
+extern "C" int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out)
+{
+    if (!p || !out)
+    {
+        setLastError("pipeline outputs: null argument");
+        return CS_ERR_INVALID;
+    }
+    return p->impl->outputs(out);
+}
+
+extern "C" size_t cs_pipeline_device_bytes(cs_pipeline p) { return p ? p->impl->deviceBytes() : 0; }
+
+/* per-stage device time of the last run in ms (keys, sort, gather, build, link, geometry, halos, neighbour prep,
+ * neighbours); synchronises on the last run's events */
+extern "C" int cs_pipeline_stage_times(cs_pipeline p, float* ms, int count)
+{
+    if (!p || !ms)
+    {
+        setLastError("pipeline stage times: null argument");
+        return CS_ERR_INVALID;
+    }
+    CSG_CUDA_TRY(cudaEventSynchronize(p->impl->ev[ST_COUNT]));
+    for (int i = 0; i < count && i < ST_COUNT; ++i)
+    {
+        float t = 0;
+        CSG_CUDA_TRY(cudaEventElapsedTime(&t, p->impl->ev[i], p->impl->ev[i + 1]));
+        ms[i] = t;
+    }
+    return CS_OK;
+}

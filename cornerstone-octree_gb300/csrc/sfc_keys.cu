@@ -1,0 +1,179 @@
+// SFC key encoding and permutation gathers.
+//
+// Keys: one pass over x, y, z (SoA), 4 particles per thread with 16-byte vector loads where the arrays are aligned,
+// sfc3D quantisation with unfused arithmetic (sfc/sfc.hpp:142-179), Hilbert or Morton interleave, 16-byte stores.
+// HBM-bound: 3*sizeof(T) + sizeof(K) bytes per particle (+ sizeof(K) when removeKey entries are respected).
+#include "cs_common.cuh"
+#include "sfc_keys.cuh"
+
+namespace csg
+{
+
+template<class T, class K, int Kind, bool RespectRemove>
+__global__ void __launch_bounds__(256) sfcKeysKernel(const T* __restrict__ x, const T* __restrict__ y,
+                                                     const T* __restrict__ z, K* __restrict__ keys, size_t n,
+                                                     KeyParams<T, K> p)
+{
+    constexpr int V = 4;
+    size_t stride   = size_t(gridDim.x) * blockDim.x;
+    for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) * V; base < n; base += stride * V)
+    {
+        if (base + V <= n)
+        {
+            T xs[V], ys[V], zs[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+            {
+                xs[v] = __ldcs(x + base + v);
+                ys[v] = __ldcs(y + base + v);
+                zs[v] = __ldcs(z + base + v);
+            }
+            K out[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+            {
+                K k = sfc3D<T, K>(xs[v], ys[v], zs[v], p, Kind);
+                if constexpr (RespectRemove)
+                {
+                    K old = keys[base + v];
+                    if (old == removeKey<K>()) k = old;
+                }
+                out[v] = k;
+            }
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                keys[base + v] = out[v];
+        }
+        else
+        {
+            for (size_t i = base; i < n; ++i)
+            {
+                K k = sfc3D<T, K>(x[i], y[i], z[i], p, Kind);
+                if constexpr (RespectRemove)
+                {
+                    if (keys[i] == removeKey<K>()) continue;
+                }
+                keys[i] = k;
+            }
+        }
+    }
+}
+
+template<class T, class K>
+int sfcKeys(cudaStream_t s, const T* x, const T* y, const T* z, K* keys, size_t n, const cs_box& box, int kind,
+            bool respectRemove)
+{
+    if (n == 0) return CS_OK;
+    if (!x || !y || !z || !keys)
+    {
+        setLastError("sfc keys: null pointer");
+        return CS_ERR_INVALID;
+    }
+    auto bp        = makeBoxParams<T>(box);
+    auto kp        = makeKeyParams<T, K>(bp);
+    unsigned thr   = 256;
+    size_t blocksN = (n + 4 * thr - 1) / (4 * thr);
+    unsigned grid  = unsigned(blocksN < size_t(smCount()) * 16 ? blocksN : size_t(smCount()) * 16);
+    if (kind == CS_HILBERT)
+    {
+        if (respectRemove) sfcKeysKernel<T, K, CS_HILBERT, true><<<grid, thr, 0, s>>>(x, y, z, keys, n, kp);
+        else sfcKeysKernel<T, K, CS_HILBERT, false><<<grid, thr, 0, s>>>(x, y, z, keys, n, kp);
+    }
+    else
+    {
+        if (respectRemove) sfcKeysKernel<T, K, CS_MORTON, true><<<grid, thr, 0, s>>>(x, y, z, keys, n, kp);
+        else sfcKeysKernel<T, K, CS_MORTON, false><<<grid, thr, 0, s>>>(x, y, z, keys, n, kp);
+    }
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template int sfcKeys(cudaStream_t, const float*, const float*, const float*, uint32_t*, size_t, const cs_box&, int, bool);
+template int sfcKeys(cudaStream_t, const double*, const double*, const double*, uint32_t*, size_t, const cs_box&, int,
+                     bool);
+template int sfcKeys(cudaStream_t, const float*, const float*, const float*, uint64_t*, size_t, const cs_box&, int, bool);
+template int sfcKeys(cudaStream_t, const double*, const double*, const double*, uint64_t*, size_t, const cs_box&, int,
+                     bool);
+
+// ---------------------------------------------------------------------------------------------------------------
+// gathers: out[i] = in[perm[i]]. The permutation is read once for up to four arrays.
+// ---------------------------------------------------------------------------------------------------------------
+template<class T, int NA>
+__global__ void __launch_bounds__(256) gatherKernel(const uint32_t* __restrict__ perm, size_t n,
+                                                    GatherArgs<T, NA> a)
+{
+    size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        uint32_t j = __ldcs(perm + i);
+#pragma unroll
+        for (int k = 0; k < NA; ++k)
+            __stcs(a.out[k] + i, __ldg(a.in[k] + j));
+    }
+}
+
+template<class T, int NA>
+int gatherN(cudaStream_t s, const uint32_t* perm, size_t n, GatherArgs<T, NA> a)
+{
+    if (n == 0) return CS_OK;
+    unsigned thr  = 256;
+    size_t blocks = (n + thr - 1) / thr;
+    unsigned grid = unsigned(blocks < size_t(smCount()) * 32 ? blocks : size_t(smCount()) * 32);
+    gatherKernel<T, NA><<<grid, thr, 0, s>>>(perm, n, a);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template int gatherN(cudaStream_t, const uint32_t*, size_t, GatherArgs<float, 1>);
+template int gatherN(cudaStream_t, const uint32_t*, size_t, GatherArgs<double, 1>);
+template int gatherN(cudaStream_t, const uint32_t*, size_t, GatherArgs<float, 4>);
+template int gatherN(cudaStream_t, const uint32_t*, size_t, GatherArgs<double, 4>);
+
+} // namespace csg
+
+using namespace csg;
+
+#define CS_KEYS_ENTRY(kindname, KIND, kb, K, tb, T)                                                                    \
+    extern "C" int cs_sfc_keys_##kindname##_##kb##_##tb(cs_stream_t stream, const T* x, const T* y, const T* z,        \
+                                                         K* keys, size_t n, const cs_box* box, int respect)            \
+    {                                                                                                                  \
+        if (!box)                                                                                                      \
+        {                                                                                                              \
+            setLastError("sfc keys: null box");                                                                        \
+            return CS_ERR_INVALID;                                                                                     \
+        }                                                                                                              \
+        return sfcKeys<T, K>(cudaStream_t(stream), x, y, z, keys, n, *box, KIND, respect != 0);                       \
+    }
+
+CS_KEYS_ENTRY(hilbert, CS_HILBERT, u32, uint32_t, f32, float)
+CS_KEYS_ENTRY(hilbert, CS_HILBERT, u32, uint32_t, f64, double)
+CS_KEYS_ENTRY(hilbert, CS_HILBERT, u64, uint64_t, f32, float)
+CS_KEYS_ENTRY(hilbert, CS_HILBERT, u64, uint64_t, f64, double)
+CS_KEYS_ENTRY(morton, CS_MORTON, u32, uint32_t, f32, float)
+CS_KEYS_ENTRY(morton, CS_MORTON, u32, uint32_t, f64, double)
+CS_KEYS_ENTRY(morton, CS_MORTON, u64, uint64_t, f32, float)
+CS_KEYS_ENTRY(morton, CS_MORTON, u64, uint64_t, f64, double)
+
+extern "C" int cs_gather_f32(cs_stream_t stream, const uint32_t* perm, const float* in, float* out, size_t n)
+{
+    GatherArgs<float, 1> a{{in}, {out}};
+    return gatherN<float, 1>(cudaStream_t(stream), perm, n, a);
+}
+extern "C" int cs_gather_f64(cs_stream_t stream, const uint32_t* perm, const double* in, double* out, size_t n)
+{
+    GatherArgs<double, 1> a{{in}, {out}};
+    return gatherN<double, 1>(cudaStream_t(stream), perm, n, a);
+}
+extern "C" int cs_gather4_f64(cs_stream_t stream, const uint32_t* perm, size_t n, const double* in0, const double* in1,
+                              const double* in2, const double* in3, double* out0, double* out1, double* out2,
+                              double* out3)
+{
+    GatherArgs<double, 4> a{{in0, in1, in2, in3}, {out0, out1, out2, out3}};
+    return gatherN<double, 4>(cudaStream_t(stream), perm, n, a);
+}
+extern "C" int cs_gather4_f32(cs_stream_t stream, const uint32_t* perm, size_t n, const float* in0, const float* in1,
+                              const float* in2, const float* in3, float* out0, float* out1, float* out2, float* out3)
+{
+    GatherArgs<float, 4> a{{in0, in1, in2, in3}, {out0, out1, out2, out3}};
+    return gatherN<float, 4>(cudaStream_t(stream), perm, n, a);
+}

@@ -1,0 +1,399 @@
+"""Python binding of libcstone_gb300.so (the C ABI in include/cstone_gb300.h) over torch CUDA tensors.
+
+The binding is deliberately thin: every function passes device pointers, sizes and the current torch stream
+straight to one C-ABI entry point and raises CsError on a non-zero status. There is no CPU path: if the shared
+library is missing or fails to load, import raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcstone_gb300.so")
+
+MORTON, HILBERT = 0, 1
+OPEN, PERIODIC, FIXED, CUBIC_OPEN = 0, 1, 2, 3
+CS_OK, CS_ERR_INVALID, CS_ERR_CAPACITY, CS_ERR_CUDA, CS_ERR_TIMEOUT, CS_ERR_DEVICE = range(6)
+
+
+class CsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"cstone_gb300 status {code}: {msg}")
+        self.code = code
+
+
+class Box(C.Structure):
+    _fields_ = [("lo", C.c_double * 3), ("hi", C.c_double * 3), ("boundary", C.c_int * 3)]
+
+
+def make_box(lo, hi, boundary=OPEN):
+    lo = [float(v) for v in (lo if np.ndim(lo) else [lo] * 3)]
+    hi = [float(v) for v in (hi if np.ndim(hi) else [hi] * 3)]
+    b = list(boundary) if np.ndim(boundary) else [int(boundary)] * 3
+    return Box((C.c_double * 3)(*lo), (C.c_double * 3)(*hi), (C.c_int * 3)(*b))
+
+
+class OctreeView(C.Structure):
+    _fields_ = [("num_leaf_nodes", C.c_int32), ("num_internal_nodes", C.c_int32), ("num_nodes", C.c_int32),
+                ("prefixes", C.c_void_p), ("child_offsets", C.c_void_p), ("parents", C.c_void_p),
+                ("level_range", C.c_void_p), ("internal_to_leaf", C.c_void_p), ("leaf_to_internal", C.c_void_p)]
+
+
+class NsView(C.Structure):
+    _fields_ = [("num_leaf_nodes", C.c_int32), ("num_nodes", C.c_int32), ("child_offsets", C.c_void_p),
+                ("parents", C.c_void_p), ("internal_to_leaf", C.c_void_p), ("layout", C.c_void_p),
+                ("centers", C.c_void_p), ("sizes", C.c_void_p), ("search_ext_factor", C.c_float)]
+
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() (or cornerstone-octree_gb300/build.py)")
+lib = C.CDLL(LIB_PATH)
+lib.cs_last_error.restype = C.c_char_p
+for _name in ("cs_sort_pairs_workspace_bytes", "cs_node_counts_workspace_bytes", "cs_compute_octree_workspace_bytes",
+              "cs_update_octree_workspace_bytes", "cs_build_octree_workspace_bytes"):
+    getattr(lib, _name).restype = C.c_size_t
+lib.cs_sort_pairs_workspace_bytes.argtypes = [C.c_size_t, C.c_int]
+lib.cs_build_octree_workspace_bytes.argtypes = [C.c_int32, C.c_int]
+lib.cs_compute_octree_workspace_bytes.argtypes = [C.c_int32]
+lib.cs_update_octree_workspace_bytes.argtypes = [C.c_int32, C.c_int32]
+lib.cs_node_counts_workspace_bytes.argtypes = [C.c_int32]
+
+
+def _check(rc):
+    if rc != 0:
+        raise CsError(rc, lib.cs_last_error().decode())
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+_KB = {torch.int32: 32, torch.uint32: 32, torch.int64: 64, torch.uint64: 64}
+_TB = {torch.float32: "f32", torch.float64: "f64"}
+
+
+def key_bits(t):
+    return _KB[t.dtype]
+
+
+def key_dtype(bits):
+    return torch.int32 if bits == 32 else torch.int64
+
+
+def max_level(bits):
+    return 10 if bits == 32 else 21
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# keys, sort, gather
+# ---------------------------------------------------------------------------------------------------------------
+
+def sfc_keys(x, y, z, box, kind=HILBERT, bits=64, keys=None, respect_remove_key=False):
+    n = x.numel()
+    if keys is None:
+        keys = torch.empty(n, dtype=key_dtype(bits), device=x.device)
+    fn = getattr(lib, f"cs_sfc_keys_{'hilbert' if kind == HILBERT else 'morton'}_u{bits}_{_TB[x.dtype]}")
+    _check(fn(_stream(), _p(x), _p(y), _p(z), _p(keys), C.c_size_t(n), C.byref(box), int(respect_remove_key)))
+    return keys
+
+
+def sort_pairs(keys, values=None, begin_bit=0, end_bit=None, iota=True, workspace=None):
+    """Stable sort in place of keys (int32/int64 tensors holding u32/u64 keys); returns (keys, values)."""
+    n = keys.numel()
+    bits = key_bits(keys)
+    end_bit = bits if end_bit is None else end_bit
+    if values is None:
+        values = torch.empty(n, dtype=torch.int32, device=keys.device)
+        iota = True
+    kalt = torch.empty_like(keys)
+    valt = torch.empty_like(values)
+    ws_bytes = lib.cs_sort_pairs_workspace_bytes(n, bits)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=keys.device) if workspace is None else workspace
+    fn = lib.cs_sort_pairs_u32 if bits == 32 else lib.cs_sort_pairs_u64
+    _check(fn(_stream(), _p(keys), _p(values), C.c_size_t(n), _p(kalt), _p(valt), begin_bit, end_bit, int(iota),
+              _p(ws), C.c_size_t(ws.numel())))
+    return keys, values
+
+
+def gather(perm, src):
+    out = torch.empty_like(src)
+    fn = lib.cs_gather_f32 if src.dtype == torch.float32 else lib.cs_gather_f64
+    _check(fn(_stream(), _p(perm), _p(src), _p(out), C.c_size_t(src.numel())))
+    return out
+
+
+def gather4(perm, a, b, c, d):
+    outs = [torch.empty_like(t) for t in (a, b, c, d)]
+    fn = lib.cs_gather4_f32 if a.dtype == torch.float32 else lib.cs_gather4_f64
+    _check(fn(_stream(), _p(perm), C.c_size_t(a.numel()), _p(a), _p(b), _p(c), _p(d), *[_p(o) for o in outs]))
+    return outs
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# cornerstone leaf array
+# ---------------------------------------------------------------------------------------------------------------
+
+def node_counts(tree, keys, max_count=0xFFFFFFFF):
+    L = tree.numel() - 1
+    counts = torch.empty(L, dtype=torch.int32, device=tree.device)
+    bits = key_bits(tree)
+    fn = lib.cs_node_counts_u32 if bits == 32 else lib.cs_node_counts_u64
+    _check(fn(_stream(), _p(tree), _p(counts), L, _p(keys), C.c_size_t(keys.numel()), C.c_uint32(max_count), 0,
+              None, C.c_size_t(0)))
+    return counts
+
+
+def rebalance_decision(tree, counts, bucket):
+    L = tree.numel() - 1
+    ops = torch.empty(L + 1, dtype=torch.int32, device=tree.device)
+    conv = torch.empty(1, dtype=torch.int32, device=tree.device)
+    fn = lib.cs_rebalance_decision_u32 if key_bits(tree) == 32 else lib.cs_rebalance_decision_u64
+    _check(fn(_stream(), _p(tree), _p(counts), L, C.c_uint(bucket), _p(ops), _p(conv)))
+    return ops[:L], bool(conv.item())
+
+
+def compute_octree(keys, bucket, max_count=0xFFFFFFFF, capacity=None):
+    """computeOctree: returns (tree[L+1], counts[L], layout[L+1], iterations)."""
+    n = keys.numel()
+    bits = key_bits(keys)
+    cap = capacity or max(64, 16 * (n // max(bucket, 1)) + 4096)
+    fn = lib.cs_compute_octree_u32 if bits == 32 else lib.cs_compute_octree_u64
+    while True:
+        tree = torch.empty(cap + 1, dtype=keys.dtype, device=keys.device)
+        counts = torch.empty(cap, dtype=torch.int32, device=keys.device)
+        layout = torch.empty(cap + 1, dtype=torch.int32, device=keys.device)
+        L = C.c_int32()
+        it = C.c_int()
+        rc = fn(_stream(), _p(keys), C.c_size_t(n), C.c_uint(bucket), C.c_uint32(max_count), _p(tree), _p(counts),
+                _p(layout), cap, C.byref(L), C.byref(it), None, C.c_size_t(0))
+        if rc == CS_ERR_CAPACITY:
+            cap = 2 * max(cap, L.value)
+            continue
+        _check(rc)
+        return tree[: L.value + 1], counts[: L.value], layout[: L.value + 1], it.value
+
+
+def update_octree(keys, bucket, tree, counts, max_count=0xFFFFFFFF, capacity=None):
+    """one updateOctree step: returns (tree, counts, converged)."""
+    bits = key_bits(keys)
+    Lin = tree.numel() - 1
+    cap = capacity or (8 * Lin + 4096)
+    fn = lib.cs_update_octree_u32 if bits == 32 else lib.cs_update_octree_u64
+    while True:
+        tout = torch.empty(cap + 1, dtype=keys.dtype, device=keys.device)
+        cout = torch.empty(cap, dtype=torch.int32, device=keys.device)
+        L = C.c_int32()
+        conv = C.c_int()
+        rc = fn(_stream(), _p(keys), C.c_size_t(keys.numel()), C.c_uint(bucket), C.c_uint32(max_count), _p(tree),
+                _p(counts), Lin, _p(tout), _p(cout), cap, C.byref(L), C.byref(conv), None, C.c_size_t(0))
+        if rc == CS_ERR_CAPACITY:
+            cap = 2 * max(cap, L.value)
+            continue
+        _check(rc)
+        return tout[: L.value + 1], cout[: L.value], bool(conv.value)
+
+
+class Octree:
+    """Device arrays of a linked octree (cstone::OctreeData)."""
+
+    def __init__(self, leaves):
+        L = leaves.numel() - 1
+        bits = key_bits(leaves)
+        dev = leaves.device
+        self.bits = bits
+        self.leaves = leaves
+        self.num_leaves = L
+        self.num_internal = (L - 1) // 7
+        self.num_nodes = L + self.num_internal
+        N = self.num_nodes
+        self.prefixes = torch.empty(N, dtype=leaves.dtype, device=dev)
+        self.child_offsets = torch.empty(N + 1, dtype=torch.int32, device=dev)
+        self.parents = torch.empty(max(1, (N - 1) // 8), dtype=torch.int32, device=dev)
+        self.level_range = torch.empty(max_level(bits) + 2, dtype=torch.int32, device=dev)
+        self.internal_to_leaf = torch.empty(N, dtype=torch.int32, device=dev)
+        self.leaf_to_internal = torch.empty(N, dtype=torch.int32, device=dev)
+
+    def view(self):
+        return OctreeView(self.num_leaves, self.num_internal, self.num_nodes, self.prefixes.data_ptr(),
+                          self.child_offsets.data_ptr(), self.parents.data_ptr(), self.level_range.data_ptr(),
+                          self.internal_to_leaf.data_ptr(), self.leaf_to_internal.data_ptr())
+
+
+def build_octree(leaves):
+    o = Octree(leaves)
+    fn = lib.cs_build_octree_u32 if o.bits == 32 else lib.cs_build_octree_u64
+    v = o.view()
+    _check(fn(_stream(), _p(leaves), o.num_leaves, C.byref(v), None, None, C.c_size_t(0)))
+    return o
+
+
+def geo_centers(prefixes, box, dtype=torch.float64, kind=HILBERT):
+    N = prefixes.numel()
+    c = torch.empty((N, 3), dtype=dtype, device=prefixes.device)
+    s = torch.empty((N, 3), dtype=dtype, device=prefixes.device)
+    fn = getattr(lib, f"cs_geo_centers_u{key_bits(prefixes)}_{_TB[dtype]}")
+    _check(fn(_stream(), _p(prefixes), N, _p(c), _p(s), C.byref(box), kind))
+    return c, s
+
+
+def search_boxes(x, y, z, h, layout, first, last, scale, leaf_to_internal_leaves, node_centers):
+    L = layout.numel() - 1
+    sc = torch.zeros((L, 3), dtype=x.dtype, device=x.device)
+    ss = torch.zeros((L, 3), dtype=x.dtype, device=x.device)
+    if x.dtype == torch.float32:
+        _check(lib.cs_search_boxes_f32(_stream(), _p(x), _p(y), _p(z), _p(h), _p(layout), first, last,
+                                       C.c_float(scale), _p(leaf_to_internal_leaves), _p(node_centers), _p(sc),
+                                       _p(ss)))
+    else:
+        _check(lib.cs_search_boxes_f64(_stream(), _p(x), _p(y), _p(z), _p(h), _p(layout), first, last,
+                                       C.c_double(scale), _p(leaf_to_internal_leaves), _p(node_centers), _p(sc),
+                                       _p(ss)))
+    return sc, ss
+
+
+def find_halos(o, node_centers, node_sizes, search_centers, search_sizes, box, first, last, flags=None):
+    if flags is None:
+        flags = torch.zeros(o.num_nodes, dtype=torch.uint8, device=o.prefixes.device)
+    fn = getattr(lib, f"cs_find_halos_u{o.bits}_{_TB[node_centers.dtype]}")
+    _check(fn(_stream(), _p(o.prefixes), _p(o.child_offsets), _p(o.parents), _p(node_centers), _p(node_sizes),
+              _p(o.leaves), _p(search_centers), _p(search_sizes), C.byref(box), first, last, _p(flags)))
+    return flags
+
+
+def ns_view(o, layout, centers, sizes, search_ext=1.0):
+    return NsView(o.num_leaves, o.num_nodes, o.child_offsets.data_ptr(), o.parents.data_ptr(),
+                  o.internal_to_leaf.data_ptr(), layout.data_ptr(), centers.data_ptr(), sizes.data_ptr(),
+                  float(search_ext))
+
+
+def find_neighbors(x, y, z, h, first, last, box, o, layout, centers, sizes, ngmax, search_ext=1.0, out=None):
+    n = last - first
+    if out is None:
+        nb = torch.empty((n, ngmax), dtype=torch.int32, device=x.device)
+        nc = torch.empty(n, dtype=torch.int32, device=x.device)
+    else:
+        nb, nc = out
+    v = ns_view(o, layout, centers, sizes, search_ext)
+    fn = lib.cs_find_neighbors_f32 if x.dtype == torch.float32 else lib.cs_find_neighbors_f64
+    _check(fn(_stream(), _p(x), _p(y), _p(z), _p(h), C.c_uint32(first), C.c_uint32(last), C.byref(box),
+              C.byref(v), C.c_uint(ngmax), _p(nb), _p(nc)))
+    return nb, nc
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# whole path (cs_pipeline_*)
+# ---------------------------------------------------------------------------------------------------------------
+
+class PipelineConfig(C.Structure):
+    _fields_ = [("sfc_kind", C.c_int), ("bucket_size", C.c_uint), ("max_count", C.c_uint32), ("ngmax", C.c_uint),
+                ("search_ext", C.c_float), ("halo_search_ext", C.c_float), ("do_halos", C.c_int),
+                ("do_neighbors", C.c_int)]
+
+
+class PipelineResult(C.Structure):
+    _fields_ = [("num_leaves", C.c_int32), ("num_nodes", C.c_int32), ("iterations", C.c_int32),
+                ("focus_first", C.c_int32), ("focus_last", C.c_int32), ("max_depth", C.c_int32)]
+
+
+class PipelineOutputs(C.Structure):
+    _fields_ = [("sorted_keys", C.c_void_p), ("order", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p),
+                ("z", C.c_void_p), ("h", C.c_void_p), ("leaves", C.c_void_p), ("counts", C.c_void_p),
+                ("layout", C.c_void_p), ("octree", OctreeView), ("centers", C.c_void_p), ("sizes", C.c_void_p),
+                ("halo_flags", C.c_void_p), ("neighbors", C.c_void_p), ("neighbor_counts", C.c_void_p)]
+
+
+lib.cs_pipeline_device_bytes.restype = C.c_size_t
+lib.cs_pipeline_device_bytes.argtypes = [C.c_void_p]
+
+STAGES = ("keys", "sort", "gather", "build", "link", "geometry", "halos", "nbprep", "neighbors")
+
+
+class Pipeline:
+    """keys -> sort -> gather -> computeOctree -> link -> geometry -> findHalos -> findNeighbors, device resident."""
+
+    def __init__(self, coord_bits=64, key_bits=64, kind=HILBERT, bucket=64, ngmax=200, search_ext=1.0,
+                 halo_search_ext=1.0, do_halos=True, do_neighbors=True, max_count=0xFFFFFFFF):
+        self.cfg = PipelineConfig(kind, bucket, max_count, ngmax, search_ext, halo_search_ext, int(do_halos),
+                                  int(do_neighbors))
+        self.coord_bits, self.key_bits = coord_bits, key_bits
+        self.handle = C.c_void_p()
+        _check(lib.cs_pipeline_create(C.byref(self.handle), coord_bits, key_bits, C.byref(self.cfg)))
+        self.result = PipelineResult()
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            lib.cs_pipeline_destroy(self.handle)
+            self.handle = None
+
+    def run(self, x, y, z, h, box, focus=(0, 0)):
+        self._n = x.numel()
+        _check(lib.cs_pipeline_run(self.handle, _stream(), _p(x), _p(y), _p(z), _p(h), C.c_size_t(x.numel()),
+                                   C.byref(box), C.c_uint64(focus[0]), C.c_uint64(focus[1]), C.byref(self.result)))
+        return self.result
+
+    def run_host(self, x, y, z, h, box, focus=(0, 0), nc_out=None, flags_out=None):
+        """x..h: pinned (or pageable) host torch tensors; nc_out/flags_out host tensors or None."""
+        fcap = flags_out.numel() if flags_out is not None else 0
+        self._n = x.numel()
+        _check(lib.cs_pipeline_run_host(self.handle, _stream(), _p(x), _p(y), _p(z), _p(h), C.c_size_t(x.numel()),
+                                        C.byref(box), C.c_uint64(focus[0]), C.c_uint64(focus[1]), _p(nc_out),
+                                        _p(flags_out), C.c_size_t(fcap), C.byref(self.result)))
+        return self.result
+
+    def stage_times(self):
+        ms = (C.c_float * len(STAGES))()
+        _check(lib.cs_pipeline_stage_times(self.handle, ms, len(STAGES)))
+        return dict(zip(STAGES, list(ms)))
+
+    def device_bytes(self):
+        return lib.cs_pipeline_device_bytes(self.handle)
+
+    def outputs(self):
+        """torch views of the device results of the last run (no copies)."""
+        o = PipelineOutputs()
+        _check(lib.cs_pipeline_get_outputs(self.handle, C.byref(o)))
+        r = self.result
+        n = self._n
+        tdt = torch.float64 if self.coord_bits == 64 else torch.float32
+        kdt = key_dtype(self.key_bits)
+        L, N = r.num_leaves, r.num_nodes
+        out = dict(sorted_keys=_wrap(o.sorted_keys, n, kdt), order=_wrap(o.order, n, torch.int32),
+                   x=_wrap(o.x, n, tdt), y=_wrap(o.y, n, tdt), z=_wrap(o.z, n, tdt), h=_wrap(o.h, n, tdt),
+                   leaves=_wrap(o.leaves, L + 1, kdt), counts=_wrap(o.counts, L, torch.int32),
+                   layout=_wrap(o.layout, L + 1, torch.int32), prefixes=_wrap(o.octree.prefixes, N, kdt),
+                   child_offsets=_wrap(o.octree.child_offsets, N, torch.int32),
+                   parents=_wrap(o.octree.parents, max(1, (N - 1) // 8), torch.int32),
+                   level_range=_wrap(o.octree.level_range, max_level(self.key_bits) + 2, torch.int32),
+                   internal_to_leaf=_wrap(o.octree.internal_to_leaf, N, torch.int32),
+                   leaf_to_internal=_wrap(o.octree.leaf_to_internal, N, torch.int32),
+                   centers=_wrap(o.centers, 3 * N, tdt).view(N, 3), sizes=_wrap(o.sizes, 3 * N, tdt).view(N, 3),
+                   halo_flags=_wrap(o.halo_flags, N, torch.uint8),
+                   neighbor_counts=_wrap(o.neighbor_counts, n, torch.int32))
+        if o.neighbors:
+            out["neighbors"] = _wrap(o.neighbors, n * self.cfg.ngmax, torch.int32).view(n, self.cfg.ngmax)
+        return out
+
+
+def _wrap(ptr, count, dtype):
+    """non-owning torch view of device memory held by the library"""
+    if count == 0 or not ptr:
+        return torch.empty(0, dtype=dtype, device="cuda")
+    nbytes = count * torch.empty(0, dtype=dtype).element_size()
+    arr = _CudaArray(ptr, nbytes)
+    t = torch.as_tensor(arr, device="cuda").view(torch.uint8)[:nbytes]
+    return t.view(dtype)
+
+
+class _CudaArray:
+    """exposes a raw device pointer through __cuda_array_interface__ so torch can view it"""
+
+    def __init__(self, ptr, nbytes):
+        self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (int(ptr), False),
+                                         "version": 3}
+

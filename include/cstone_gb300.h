@@ -1,0 +1,329 @@
+/*
+ * cstone_gb300 — C ABI of the GB300 (sm_103a) implementation of cornerstone-octree's single-GPU octree path:
+ * SFC keys -> stable key sort -> cornerstone leaf build/update -> internal-tree link -> node geometry ->
+ * findHalos -> findNeighbors.
+ *
+ * Conventions
+ *  - Every entry point is stream-ordered on `stream` (a cudaStream_t passed as void*, NULL = legacy default stream)
+ *    and returns a status code (CS_OK = 0). cs_last_error() describes the last failure of the calling thread.
+ *  - All array arguments are device pointers owned by the caller, except where a name ends in `_host`.
+ *  - No entry point keeps global device state, so calls on different streams may run concurrently.
+ *  - Entry points that need temporary device memory take (workspace, workspace_bytes) and have a *_workspace_bytes
+ *    query; passing workspace == NULL makes the call allocate stream-ordered memory (cudaMallocAsync) itself.
+ *  - Key arrays hold 32-bit (u32) or 64-bit (u64) SFC keys, coordinates are float (f32) or double (f64).
+ *  - Node arrays follow cstone::OctreeView (tree/octree.hpp:233-283): level-sorted node order, placeholder-bit
+ *    prefixes, childOffsets (0 = leaf), parents per group of 8 siblings, levelRange of maxTreeLevel + 2 entries.
+ *
+ * Each declaration cites the reference interface it replaces (path:line within the reference project).
+ */
+#ifndef CSTONE_GB300_H
+#define CSTONE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void* cs_stream_t;
+
+enum cs_status
+{
+    CS_OK           = 0,
+    CS_ERR_INVALID  = 1, /* bad argument (size, pointer, bucket size ...) */
+    CS_ERR_CAPACITY = 2, /* an output buffer is too small; the required size is reported */
+    CS_ERR_CUDA     = 3, /* a CUDA runtime call failed */
+    CS_ERR_TIMEOUT  = 4, /* a bounded device-side wait gave up (look-back or grid barrier) */
+    CS_ERR_DEVICE   = 5  /* a device-side consistency check failed */
+};
+
+/* SFC kind: cstone::MortonKey / cstone::HilbertKey (sfc/sfc.hpp:31-40) */
+enum cs_sfc_kind
+{
+    CS_MORTON  = 0,
+    CS_HILBERT = 1
+};
+
+/* cstone::BoundaryType (sfc/box.hpp:77-83) */
+enum cs_boundary
+{
+    CS_OPEN       = 0,
+    CS_PERIODIC   = 1,
+    CS_FIXED      = 2,
+    CS_CUBIC_OPEN = 3
+};
+
+/* cstone::Box<T> (sfc/box.hpp:96-175). Limits are given in double; f32 entry points convert them to float and derive
+ * lengths and inverse lengths in float, as Box<float> does. */
+typedef struct
+{
+    double lo[3];
+    double hi[3];
+    int boundary[3];
+} cs_box;
+
+/* cstone::OctreeView<KeyType> (tree/octree.hpp:233-253), device pointers, sized as OctreeData::resize
+ * (tree/octree.hpp:293-308): num_internal_nodes = (L-1)/7, num_nodes = L + num_internal_nodes,
+ * prefixes/internal_to_leaf/leaf_to_internal: num_nodes, child_offsets: num_nodes + 1,
+ * parents: max(1, (num_nodes-1)/8), level_range: maxTreeLevel + 2 (12 for u32, 23 for u64). */
+typedef struct
+{
+    int32_t num_leaf_nodes;
+    int32_t num_internal_nodes;
+    int32_t num_nodes;
+    void* prefixes; /* uint32_t* or uint64_t* */
+    int32_t* child_offsets;
+    int32_t* parents;
+    int32_t* level_range;
+    int32_t* internal_to_leaf;
+    int32_t* leaf_to_internal;
+} cs_octree_view;
+
+/* cstone::OctreeNsView<T, KeyType> (tree/octree.hpp:255-283): what findNeighbors reads */
+typedef struct
+{
+    int32_t num_leaf_nodes;
+    int32_t num_nodes;
+    const int32_t* child_offsets;
+    const int32_t* parents;
+    const int32_t* internal_to_leaf;
+    const uint32_t* layout; /* first particle of each leaf, num_leaf_nodes + 1 entries */
+    const void* centers;    /* 3 * num_nodes of T (node geometric centres) */
+    const void* sizes;      /* 3 * num_nodes of T (node half sizes) */
+    float search_ext_factor;
+} cs_ns_view;
+
+const char* cs_last_error(void);
+int cs_version(void);
+
+/* ---- SFC keys ----------------------------------------------------------------------------------------------
+ * replaces computeSfcKeys(execution::Gpu, x, y, z, keys, n, box) (sfc/sfc_gpu.h:24-26, kernel sfc/sfc_gpu.cu:23-44).
+ * respect_remove_key = 1 keeps keys that equal removeKey (2^30 / 2^63) untouched, as the reference kernel does;
+ * 0 writes every key without reading the key array first. */
+int cs_sfc_keys_hilbert_u32_f32(cs_stream_t stream, const float* x, const float* y, const float* z, uint32_t* keys,
+                                size_t n, const cs_box* box, int respect_remove_key);
+int cs_sfc_keys_hilbert_u32_f64(cs_stream_t stream, const double* x, const double* y, const double* z, uint32_t* keys,
+                                size_t n, const cs_box* box, int respect_remove_key);
+int cs_sfc_keys_hilbert_u64_f32(cs_stream_t stream, const float* x, const float* y, const float* z, uint64_t* keys,
+                                size_t n, const cs_box* box, int respect_remove_key);
+int cs_sfc_keys_hilbert_u64_f64(cs_stream_t stream, const double* x, const double* y, const double* z, uint64_t* keys,
+                                size_t n, const cs_box* box, int respect_remove_key);
+int cs_sfc_keys_morton_u32_f32(cs_stream_t stream, const float* x, const float* y, const float* z, uint32_t* keys,
+                               size_t n, const cs_box* box, int respect_remove_key);
+int cs_sfc_keys_morton_u32_f64(cs_stream_t stream, const double* x, const double* y, const double* z, uint32_t* keys,
+                               size_t n, const cs_box* box, int respect_remove_key);
+int cs_sfc_keys_morton_u64_f32(cs_stream_t stream, const float* x, const float* y, const float* z, uint64_t* keys,
+                               size_t n, const cs_box* box, int respect_remove_key);
+int cs_sfc_keys_morton_u64_f64(cs_stream_t stream, const double* x, const double* y, const double* z, uint64_t* keys,
+                               size_t n, const cs_box* box, int respect_remove_key);
+
+/* ---- stable key sort ----------------------------------------------------------------------------------------
+ * replaces sortByKeyTempStorage / sortByKey(exec, keys, values, keyBuf, valueBuf) (primitives/primitives_gpu.h:118-155,
+ * CUB SortPairs in primitives/primitives_gpu.cu:310-356). Stable LSD radix sort (onesweep, decoupled look-back) of
+ * bits [begin_bit, end_bit); keys_alt/values_alt are ping-pong buffers of n elements. The sorted result is left in
+ * keys/values. values_are_iota = 1 ignores the input values and sorts the permutation 0..n-1 (the `sequence` +
+ * sortByKey idiom of the reference's callers). n must be below 2^30. */
+size_t cs_sort_pairs_workspace_bytes(size_t n, int key_bits);
+int cs_sort_pairs_u32(cs_stream_t stream, uint32_t* keys, uint32_t* values, size_t n, uint32_t* keys_alt,
+                      uint32_t* values_alt, int begin_bit, int end_bit, int values_are_iota, void* workspace,
+                      size_t workspace_bytes);
+int cs_sort_pairs_u64(cs_stream_t stream, uint64_t* keys, uint32_t* values, size_t n, uint64_t* keys_alt,
+                      uint32_t* values_alt, int begin_bit, int end_bit, int values_are_iota, void* workspace,
+                      size_t workspace_bytes);
+
+/* ---- permutation gather --------------------------------------------------------------------------------------
+ * replaces gather(exec, ordering, in, out) / gatherArrays (primitives/primitives_gpu.cu:74-90, domain/layout.hpp:231).
+ * out[i] = in[perm[i]] for i < n. The 4-array form gathers x, y, z, h in one pass. */
+int cs_gather_f32(cs_stream_t stream, const uint32_t* perm, const float* in, float* out, size_t n);
+int cs_gather_f64(cs_stream_t stream, const uint32_t* perm, const double* in, double* out, size_t n);
+int cs_gather4_f64(cs_stream_t stream, const uint32_t* perm, size_t n, const double* in0, const double* in1,
+                   const double* in2, const double* in3, double* out0, double* out1, double* out2, double* out3);
+int cs_gather4_f32(cs_stream_t stream, const uint32_t* perm, size_t n, const float* in0, const float* in1,
+                   const float* in2, const float* in3, float* out0, float* out1, float* out2, float* out3);
+
+/* ---- cornerstone leaf array -----------------------------------------------------------------------------------
+ * cs_node_counts replaces computeNodeCountsGpu(exec, tree, counts, numNodes, keys, maxCount, useCountsAsGuess)
+ * (tree/csarray_gpu.h:41-47, tree/csarray_gpu.cu:86-122): counts[i] = min(#keys in [tree[i], tree[i+1]), max_count).
+ * With use_counts_as_guess the input counts seed an exponential search, as updateNodeCount does. */
+size_t cs_node_counts_workspace_bytes(int32_t num_nodes);
+int cs_node_counts_u32(cs_stream_t stream, const uint32_t* tree, uint32_t* counts, int32_t num_nodes,
+                       const uint32_t* keys, size_t n, uint32_t max_count, int use_counts_as_guess, void* workspace,
+                       size_t workspace_bytes);
+int cs_node_counts_u64(cs_stream_t stream, const uint64_t* tree, uint32_t* counts, int32_t num_nodes,
+                       const uint64_t* keys, size_t n, uint32_t max_count, int use_counts_as_guess, void* workspace,
+                       size_t workspace_bytes);
+
+/* cs_rebalance_decision replaces computeNodeOpsGpu's decision half (rebalanceDecisionKernel,
+ * tree/csarray_gpu.cu:151-162): ops[i] in {0,1,8,64,512,4096} for i < num_nodes; *converged_dev (device int) is
+ * set to 1 if every op is 1, else 0. */
+int cs_rebalance_decision_u32(cs_stream_t stream, const uint32_t* tree, const uint32_t* counts, int32_t num_nodes,
+                              unsigned bucket_size, int32_t* ops, int* converged_dev);
+int cs_rebalance_decision_u64(cs_stream_t stream, const uint64_t* tree, const uint32_t* counts, int32_t num_nodes,
+                              unsigned bucket_size, int32_t* ops, int* converged_dev);
+
+/* cs_compute_octree replaces computeOctree / the `while(!updateOctreeGpu(...))` build loop (tree/csarray.hpp:429-440,
+ * tree/update_gpu.cuh:43-68). Builds the converged cornerstone leaf array of the sorted keys from the root in one
+ * cooperative launch (no host round trip per iteration). tree must hold capacity+1 keys, counts capacity entries,
+ * layout (optional, may be NULL) capacity+1 entries = first particle of each leaf. *num_leaves_host receives L; on
+ * CS_ERR_CAPACITY it receives the number of leaves that did not fit. *iterations_host (may be NULL) receives the
+ * number of updateOctree steps the reference loop would take. */
+size_t cs_compute_octree_workspace_bytes(int32_t capacity);
+int cs_compute_octree_u32(cs_stream_t stream, const uint32_t* keys, size_t n, unsigned bucket_size,
+                          uint32_t max_count, uint32_t* tree, uint32_t* counts, uint32_t* layout, int32_t capacity,
+                          int32_t* num_leaves_host, int* iterations_host, void* workspace, size_t workspace_bytes);
+int cs_compute_octree_u64(cs_stream_t stream, const uint64_t* keys, size_t n, unsigned bucket_size,
+                          uint32_t max_count, uint64_t* tree, uint32_t* counts, uint32_t* layout, int32_t capacity,
+                          int32_t* num_leaves_host, int* iterations_host, void* workspace, size_t workspace_bytes);
+
+/* cs_update_octree replaces one updateOctree / updateOctreeGpu step (tree/csarray.hpp:408-426,
+ * tree/update_gpu.cuh:43-68): decision on counts_in, rebalance, recount of tree_out against keys (guessed search).
+ * *num_leaves_out_host receives the new leaf count, *converged_host whether the decision changed nothing. */
+size_t cs_update_octree_workspace_bytes(int32_t num_leaves_in, int32_t capacity);
+int cs_update_octree_u32(cs_stream_t stream, const uint32_t* keys, size_t n, unsigned bucket_size, uint32_t max_count,
+                         const uint32_t* tree_in, const uint32_t* counts_in, int32_t num_leaves_in, uint32_t* tree_out,
+                         uint32_t* counts_out, int32_t capacity, int32_t* num_leaves_out_host, int* converged_host,
+                         void* workspace, size_t workspace_bytes);
+int cs_update_octree_u64(cs_stream_t stream, const uint64_t* keys, size_t n, unsigned bucket_size, uint32_t max_count,
+                         const uint64_t* tree_in, const uint32_t* counts_in, int32_t num_leaves_in, uint64_t* tree_out,
+                         uint32_t* counts_out, int32_t capacity, int32_t* num_leaves_out_host, int* converged_host,
+                         void* workspace, size_t workspace_bytes);
+
+/* ---- internal tree ------------------------------------------------------------------------------------------------
+ * replaces buildOctreeGpu(exec, leaves, OctreeView) (tree/octree_gpu.h:35-45, tree/octree_gpu.cu:138-203) and
+ * updateInternalTree (tree/octree.hpp:362-369): placeholder prefixes in (level, key) order, childOffsets, parents,
+ * levelRange (written to device memory), internalToLeaf, leafToInternal. level_range_host (may be NULL) receives a
+ * host copy of levelRange (the call then synchronises the stream). */
+size_t cs_build_octree_workspace_bytes(int32_t num_leaves, int key_bits);
+int cs_build_octree_u32(cs_stream_t stream, const uint32_t* leaves, int32_t num_leaves, const cs_octree_view* view,
+                        int32_t* level_range_host, void* workspace, size_t workspace_bytes);
+int cs_build_octree_u64(cs_stream_t stream, const uint64_t* leaves, int32_t num_leaves, const cs_octree_view* view,
+                        int32_t* level_range_host, void* workspace, size_t workspace_bytes);
+
+/* ---- node geometry ----------------------------------------------------------------------------------------------
+ * replaces computeGeoCentersGpu(exec, prefixes, numNodes, centers, sizes, box) (focus/source_center_gpu.cu:212-240,
+ * CPU nodeFpCenters focus/source_center.hpp:145-158). centers/sizes hold 3*num_nodes values (x,y,z per node).
+ * kind = CS_HILBERT decodes node boxes as the reference always does; CS_MORTON decodes them as Morton boxes, for
+ * trees built from Morton keys (an extension: the reference has no Morton geometry). */
+int cs_geo_centers_u32_f32(cs_stream_t stream, const uint32_t* prefixes, int32_t num_nodes, float* centers,
+                           float* sizes, const cs_box* box, int kind);
+int cs_geo_centers_u32_f64(cs_stream_t stream, const uint32_t* prefixes, int32_t num_nodes, double* centers,
+                           double* sizes, const cs_box* box, int kind);
+int cs_geo_centers_u64_f32(cs_stream_t stream, const uint64_t* prefixes, int32_t num_nodes, float* centers,
+                           float* sizes, const cs_box* box, int kind);
+int cs_geo_centers_u64_f64(cs_stream_t stream, const uint64_t* prefixes, int32_t num_nodes, double* centers,
+                           double* sizes, const cs_box* box, int kind);
+
+/* ---- halo discovery -----------------------------------------------------------------------------------------------
+ * cs_search_boxes replaces computeBoundingBoxGpu (focus/source_center_gpu.cu:23-92) as called by discoverHalos
+ * (focus/octree_focus_mpi.hpp:534-544): for leaves [first_leaf, last_leaf), the box around p -/+ h*scale of the
+ * leaf's particles, initialised with the leaf's geometric centre centers[leaf_to_internal[leaf]]
+ * (leaf_to_internal = OctreeView.leafToInternal + numInternalNodes). search_centers/sizes hold 3 values per leaf.
+ * cs_find_halos replaces findHalosGpu (traversal/collisions_gpu.h:46-59, traversal/collisions_gpu.cu:23-77): flags
+ * (num_nodes bytes, zeroed by the caller) are set to 1 for every node outside [leaves[first], leaves[last]) that
+ * overlaps a search box of a focus leaf. */
+int cs_search_boxes_f32(cs_stream_t stream, const float* x, const float* y, const float* z, const float* h,
+                        const uint32_t* layout, int32_t first_leaf, int32_t last_leaf, float scale,
+                        const int32_t* leaf_to_internal, const float* node_centers, float* search_centers,
+                        float* search_sizes);
+int cs_search_boxes_f64(cs_stream_t stream, const double* x, const double* y, const double* z, const double* h,
+                        const uint32_t* layout, int32_t first_leaf, int32_t last_leaf, double scale,
+                        const int32_t* leaf_to_internal, const double* node_centers, double* search_centers,
+                        double* search_sizes);
+int cs_find_halos_u32_f32(cs_stream_t stream, const uint32_t* prefixes, const int32_t* child_offsets,
+                          const int32_t* parents, const float* node_centers, const float* node_sizes,
+                          const uint32_t* leaves, const float* search_centers, const float* search_sizes,
+                          const cs_box* box, int32_t first_node, int32_t last_node, uint8_t* flags);
+int cs_find_halos_u64_f32(cs_stream_t stream, const uint64_t* prefixes, const int32_t* child_offsets,
+                          const int32_t* parents, const float* node_centers, const float* node_sizes,
+                          const uint64_t* leaves, const float* search_centers, const float* search_sizes,
+                          const cs_box* box, int32_t first_node, int32_t last_node, uint8_t* flags);
+int cs_find_halos_u64_f64(cs_stream_t stream, const uint64_t* prefixes, const int32_t* child_offsets,
+                          const int32_t* parents, const double* node_centers, const double* node_sizes,
+                          const uint64_t* leaves, const double* search_centers, const double* search_sizes,
+                          const cs_box* box, int32_t first_node, int32_t last_node, uint8_t* flags);
+
+/* ---- neighbour search ---------------------------------------------------------------------------------------------
+ * replaces findNeighbors(x, y, z, h, firstId, lastId, box, OctreeNsView, ngmax, neighbors, neighborsCount)
+ * (findneighbors.hpp:156-177) and the GPU builder GpuAlwaysTraverseNeighborhoodBuilder
+ * (traversal/ijloop/gpu_alwaystraverse.cuh:174-204). Particles are in SFC order; for each i in [first, last)
+ * counts[i-first] receives the uncapped number of j != i with |x_j - x_i|^2 < (2 h_i)^2 among the leaves whose
+ * boxes pass the reference's pruning test, and neighbors[(i-first)*ngmax + k] the k-th such j in ascending order
+ * for k < min(count, ngmax) — exactly the CPU reference's result. */
+int cs_find_neighbors_f32(cs_stream_t stream, const float* x, const float* y, const float* z, const float* h,
+                          uint32_t first, uint32_t last, const cs_box* box, const cs_ns_view* tree, unsigned ngmax,
+                          uint32_t* neighbors, uint32_t* counts);
+int cs_find_neighbors_f64(cs_stream_t stream, const double* x, const double* y, const double* z, const double* h,
+                          uint32_t first, uint32_t last, const cs_box* box, const cs_ns_view* tree, unsigned ngmax,
+                          uint32_t* neighbors, uint32_t* counts);
+
+/* ---- whole path: keys -> sort -> gather -> computeOctree -> link -> geometry -> findHalos -> findNeighbors ---------
+ * The single-rank inner part of the reference's Domain::sync + discoverHalos + neighbour search
+ * (domain/assignment.hpp:105-120, focus/octree_focus_mpi.hpp:512-568, findneighbors.hpp:156-177), as one object that
+ * keeps its device buffers between calls (no allocation once sized). Coordinates and h are f32 or f64 (coord_bits),
+ * keys u32 or u64 (key_bits). */
+typedef struct cs_pipeline_s* cs_pipeline;
+
+typedef struct
+{
+    int sfc_kind;           /* CS_HILBERT (the reference's SfcKind) or CS_MORTON */
+    unsigned bucket_size;   /* computeOctree bucketSize */
+    uint32_t max_count;     /* computeOctree maxCount (0xffffffff = uncapped) */
+    unsigned ngmax;         /* findNeighbors ngmax; 0 = counts only */
+    float search_ext;       /* OctreeNsView::searchExtFactor */
+    float halo_search_ext;  /* discoverHalos searchExtFact: search box = p +- 2 h halo_search_ext */
+    int do_halos;           /* run findHalos for the leaves in [focus_start, focus_end) of the key space */
+    int do_neighbors;       /* run findNeighbors for all particles */
+} cs_pipeline_config;
+
+typedef struct
+{
+    int32_t num_leaves;
+    int32_t num_nodes;
+    int32_t iterations; /* updateOctree steps of the build */
+    int32_t focus_first;
+    int32_t focus_last;
+    int32_t max_depth;  /* deepest leaf level */
+} cs_pipeline_result;
+
+/* device pointers to the results of the last cs_pipeline_run (valid until the next run or destroy) */
+typedef struct
+{
+    void* sorted_keys;      /* n keys, SFC order */
+    uint32_t* order;        /* n: sorted position -> input index (sort_by_key permutation) */
+    void *x, *y, *z, *h;    /* n each, SFC order */
+    void* leaves;           /* num_leaves + 1 */
+    uint32_t* counts;       /* num_leaves */
+    uint32_t* layout;       /* num_leaves + 1 */
+    cs_octree_view octree;  /* linked internal tree */
+    void* centers;          /* 3 * num_nodes */
+    void* sizes;            /* 3 * num_nodes */
+    uint8_t* halo_flags;    /* num_nodes */
+    uint32_t* neighbors;    /* n * ngmax */
+    uint32_t* neighbor_counts; /* n */
+} cs_pipeline_outputs;
+
+int cs_pipeline_create(cs_pipeline* out, int coord_bits, int key_bits, const cs_pipeline_config* config);
+int cs_pipeline_destroy(cs_pipeline p);
+/* inputs are device arrays of n particles (any order); box as for cs_sfc_keys */
+int cs_pipeline_run(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z, const void* h,
+                    size_t n, const cs_box* box, uint64_t focus_start, uint64_t focus_end, cs_pipeline_result* result);
+/* same from host arrays (pinned for full speed): copies the inputs in, runs, and copies the neighbour counts
+ * (n uint32, may be NULL) and halo flags (num_nodes bytes, may be NULL; call with NULL first to learn num_nodes)
+ * back; synchronises the stream. */
+int cs_pipeline_run_host(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
+                         const void* h, size_t n, const cs_box* box, uint64_t focus_start, uint64_t focus_end,
+                         uint32_t* neighbor_counts_host, uint8_t* halo_flags_host, size_t halo_flags_capacity,
+                         cs_pipeline_result* result);
+int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out);
+/* bytes of device memory the pipeline holds */
+size_t cs_pipeline_device_bytes(cs_pipeline p);
+/* device time in ms of each stage of the last run: keys, sort, gather, build, link, geometry, halos, neighbour
+ * preparation, neighbours (count <= 9 values); waits for the last run to finish */
+int cs_pipeline_stage_times(cs_pipeline p, float* ms, int count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CSTONE_GB300_H */

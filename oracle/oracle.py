@@ -458,3 +458,83 @@ def ref_find_neighbors(x, y, z, h, first, last, box, tree, layout, centers, size
        _p(np.ascontiguousarray(layout, np.uint32)), _p(centers), _p(sizes), C.c_float(search_ext), C.c_uint(ngmax),
        _p(nb), _p(nc))
     return nb.reshape(n, ngmax), nc
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# CPU baseline: the whole path on the host cores, stage by stage
+# ---------------------------------------------------------------------------------------------------------------
+
+def h_for_k_neighbors_cpu(x, y, z, box, k=100, tol=0.1, bucket=64, max_iter=40):
+    """h (input order) with |count(2h) - k| <= tol*k, by per-particle bisection with the oracle's counts."""
+    n = x.size
+    keys = sfc_keys(x, y, z, box)
+    skeys, perm = sort_by_key(keys)
+    xs, ys, zs = x[perm], y[perm], z[perm]
+    leaves, counts, _ = compute_octree(skeys, bucket)
+    tree = build_octree(leaves)
+    centers, sizes = node_fp_centers(tree.prefixes, box, x.dtype)
+    layout = layout_from_counts(counts)
+    idx = np.arange(n)
+    j = np.where(idx + k < n, idx + k, np.maximum(idx - k, 0))
+    h = 0.5 * np.sqrt((xs - xs[j]) ** 2 + (ys - ys[j]) ** 2 + (zs - zs[j]) ** 2)
+    h[h <= 0] = h[h > 0].min()
+    lo = np.zeros(n)
+    hi = np.full(n, np.inf)
+    for _ in range(max_iter):
+        _, nc = find_neighbors(xs, ys, zs, h, 0, n, box, tree, layout, centers, sizes, 0)
+        low = nc < k * (1 - tol)
+        high = nc > k * (1 + tol)
+        if not (low | high).any():
+            break
+        lo = np.where(low, h, lo)
+        hi = np.where(high, h, hi)
+        ratio = (k / np.maximum(nc, 1)) ** (1.0 / 3.0)
+        br = (lo > 0) & np.isfinite(hi)
+        hn = np.where(br, 0.5 * (lo + hi), np.where(low, h * np.clip(ratio, 1.02, 4), h * np.clip(ratio, 0.25, 0.98)))
+        h = np.where(low | high, hn, h)
+    out = np.empty(n)
+    out[perm] = h
+    return out
+
+
+def timed_pipeline(x, y, z, h, box, bucket, ngmax, focus=(0, 0), kind=HILBERT, key_bits=64, halo_ext=1.0):
+    """keys -> stable sort -> gather -> computeOctree -> link -> geometry -> search boxes + findHalos ->
+    findNeighbors on the CPU; returns (stage seconds dict, outputs dict)."""
+    import time
+
+    t = {}
+    n = x.size
+    c0 = time.perf_counter()
+    keys = sfc_keys(x, y, z, box, kind, key_bits)
+    c1 = time.perf_counter()
+    skeys, perm = sort_by_key(keys)
+    c2 = time.perf_counter()
+    outs = []
+    for a in (x, y, z, h):
+        o = np.empty_like(a)
+        fn = lib().cso_gather_f64 if a.dtype == np.float64 else lib().cso_gather_f32
+        fn(_p(perm), _p(a), _p(o), C.c_size_t(n))
+        outs.append(o)
+    xs, ys, zs, hs = outs
+    c3 = time.perf_counter()
+    leaves, counts, iters = compute_octree(skeys, bucket, key_bits)
+    c4 = time.perf_counter()
+    tree = build_octree(leaves, key_bits)
+    c5 = time.perf_counter()
+    centers, sizes = node_fp_centers(tree.prefixes, box, x.dtype, kind, key_bits)
+    layout = layout_from_counts(counts)
+    c6 = time.perf_counter()
+    flags = None
+    if focus[1] > focus[0]:
+        first = int(np.searchsorted(leaves, np.uint64(focus[0])))
+        last = int(np.searchsorted(leaves, np.uint64(focus[1])))
+        l2i = tree.leaf_to_internal[tree.num_internal:]
+        sc, ss = search_boxes(xs, ys, zs, hs, layout, first, last, 2.0 * halo_ext, l2i, centers)
+        flags = find_halos(tree, centers, sizes, sc, ss, box, first, last, key_bits)
+    c7 = time.perf_counter()
+    nb, nc = find_neighbors(xs, ys, zs, hs, 0, n, box, tree, layout, centers, sizes, ngmax)
+    c8 = time.perf_counter()
+    t = dict(keys=c1 - c0, sort=c2 - c1, gather=c3 - c2, build=c4 - c3, link=c5 - c4, geometry=c6 - c5,
+             halos=c7 - c6, neighbors=c8 - c7, total=c8 - c0)
+    return t, dict(sorted_keys=skeys, perm=perm, leaves=leaves, counts=counts, iterations=iters, tree=tree,
+                   centers=centers, sizes=sizes, flags=flags, nb=nb, nc=nc)

@@ -1,0 +1,122 @@
+"""GPU parity: halo search boxes + collision flags and neighbour search, bit-exact against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import dev, neighbor_lists_equal, to_dev, u32, uniform
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(O, cs, x, y, z, h, box_lo, box_hi, bnd, bucket, kind=1, bits=64):
+    obox = O.make_box(box_lo, box_hi, bnd)
+    ref = O.pipeline(x, y, z, h, obox, bucket, 1, kind, bits, with_neighbors=False)
+    tx, ty, tz, th = to_dev(ref["x"], ref["y"], ref["z"], ref["h"])
+    leaves = torch.from_numpy(ref["leaves"].view(np.int64)).to(dev())
+    o = cs.build_octree(leaves)
+    layout = torch.from_numpy(ref["layout"].view(np.int32)).to(dev())
+    box = cs.make_box(box_lo, box_hi, bnd)
+    c, s = cs.geo_centers(o.prefixes, box, tx.dtype, kind)
+    return ref, obox, box, o, layout, c, s, (tx, ty, tz, th)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("bnd", [0, 1])
+@pytest.mark.parametrize("focus", ["quarter", "middle", "all"])
+def test_halos(cs, O, dtype, bnd, focus):
+    n = 40000
+    x, y, z = uniform(O, 31, n, -1.0, 1.0, dtype)
+    h = (0.02 + 0.03 * O.philox_uniform(32, 0, n, 0, 1)).astype(dtype)
+    ref, obox, box, o, layout, c, s, (tx, ty, tz, th) = _setup(O, cs, x, y, z, h, -1.0, 1.0, bnd, 32)
+    L = o.num_leaves
+    leaves = ref["leaves"]
+    if focus == "quarter":
+        first, last = 0, int(np.searchsorted(leaves, np.uint64(1) << np.uint64(61)))
+    elif focus == "middle":
+        first, last = L // 3, 2 * L // 3
+    else:
+        first, last = 0, L
+    tree = ref["tree"]
+    l2i = tree.leaf_to_internal[tree.num_internal:]
+    rsc, rss = O.search_boxes(ref["x"], ref["y"], ref["z"], ref["h"], ref["layout"], first, last, 2.0, l2i,
+                              ref["centers"])
+    rflags = O.find_halos(tree, ref["centers"], ref["sizes"], rsc, rss, obox, first, last)
+    tl2i = o.leaf_to_internal[o.num_internal:]
+    sc, ss = cs.search_boxes(tx, ty, tz, th, layout, first, last, 2.0, tl2i, c)
+    flags = cs.find_halos(o, c, s, sc, ss, box, first, last)
+    torch.cuda.synchronize()
+    assert np.array_equal(sc[first:last].cpu().numpy(), rsc[first:last])
+    assert np.array_equal(ss[first:last].cpu().numpy(), rss[first:last])
+    assert np.array_equal(flags.cpu().numpy(), rflags)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("bnd", [0, 1])
+@pytest.mark.parametrize("hmode", ["const", "variable"])
+def test_neighbors_uniform(cs, O, dtype, bnd, hmode):
+    n = 60000
+    x, y, z = uniform(O, 41, n, -1.0, 1.0, dtype)
+    if hmode == "const":
+        h = np.full(n, 0.04, dtype)
+    else:
+        h = (0.01 + 0.11 * O.philox_uniform(42, 0, n, 0, 1)).astype(dtype)  # up to ~500 neighbours
+    ngmax = 100
+    ref, obox, box, o, layout, c, s, (tx, ty, tz, th) = _setup(O, cs, x, y, z, h, -1.0, 1.0, bnd, 32)
+    rnb, rnc = O.find_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], 0, n, obox, ref["tree"], ref["layout"],
+                                ref["centers"], ref["sizes"], ngmax)
+    nb, nc = cs.find_neighbors(tx, ty, tz, th, 0, n, box, o, layout, c, s, ngmax)
+    torch.cuda.synchronize()
+    neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)
+    assert (rnc > ngmax).any() or hmode == "const"  # truncation is exercised
+
+
+def test_neighbors_subrange_and_ext(cs, O):
+    n = 30000
+    x, y, z = uniform(O, 51, n, -0.5, 0.5)
+    h = np.full(n, 0.03)
+    ngmax = 64
+    ref, obox, box, o, layout, c, s, (tx, ty, tz, th) = _setup(O, cs, x, y, z, h, -0.5, 0.5, 0, 16)
+    first, last = 1234, 23456
+    rnb, rnc = O.find_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], first, last, obox, ref["tree"],
+                                ref["layout"], ref["centers"], ref["sizes"], ngmax, search_ext=1.25)
+    nb, nc = cs.find_neighbors(tx, ty, tz, th, first, last, box, o, layout, c, s, ngmax, search_ext=1.25)
+    torch.cuda.synchronize()
+    neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)
+
+
+def test_neighbors_plummer(cs, O):
+    n = 80000
+    x, y, z = O.plummer(17, n)
+    lo = (x.min(), y.min(), z.min())
+    hi = (x.max(), y.max(), z.max())
+    # adaptive h: from the distance to the 5th next particle in SFC order (as estimateH in the reference tests)
+    obox = O.make_box(lo, hi)
+    keys = O.sfc_keys(x, y, z, obox, 1, 64)
+    _, perm = O.sort_by_key(keys)
+    xs, ys, zs = x[perm], y[perm], z[perm]
+    j = np.minimum(np.arange(n) + 5, n - 1)
+    hs = 0.5001 * np.sqrt((xs - xs[j]) ** 2 + (ys - ys[j]) ** 2 + (zs - zs[j]) ** 2) + 1e-6
+    h = np.empty(n)
+    h[perm] = hs
+    ngmax = 200
+    ref, obox, box, o, layout, c, s, (tx, ty, tz, th) = _setup(O, cs, x, y, z, h, lo, hi, 0, 64)
+    rnb, rnc = O.find_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], 0, n, obox, ref["tree"], ref["layout"],
+                                ref["centers"], ref["sizes"], ngmax)
+    nb, nc = cs.find_neighbors(tx, ty, tz, th, 0, n, box, o, layout, c, s, ngmax)
+    torch.cuda.synchronize()
+    neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)
+
+
+def test_neighbors_duplicates(cs, O):
+    """coincident particles: j == i is excluded, coincident j != i are neighbours (CPU semantics)"""
+    n = 20000
+    x, y, z = uniform(O, 61, n // 2, -1.0, 1.0)
+    x, y, z = (np.concatenate([a, a]) for a in (x, y, z))
+    h = np.full(n, 0.05)
+    ngmax = 128
+    ref, obox, box, o, layout, c, s, (tx, ty, tz, th) = _setup(O, cs, x, y, z, h, -1.0, 1.0, 0, 8)
+    rnb, rnc = O.find_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], 0, n, obox, ref["tree"], ref["layout"],
+                                ref["centers"], ref["sizes"], ngmax)
+    nb, nc = cs.find_neighbors(tx, ty, tz, th, 0, n, box, o, layout, c, s, ngmax)
+    torch.cuda.synchronize()
+    neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)

@@ -1,0 +1,97 @@
+"""GPU parity of the whole path (cs_pipeline_*) against the CPU oracle run stage by stage on the same inputs."""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import keys_u, neighbor_lists_equal, to_dev, u32
+
+pytestmark = pytest.mark.gpu
+
+
+def _check_against_oracle(cs, O, x, y, z, h, lo, hi, bnd, bucket, ngmax, focus, coord_bits=64, key_bits=64):
+    obox = O.make_box(lo, hi, bnd)
+    t, ref = O.timed_pipeline(x, y, z, h, obox, bucket, ngmax, focus, key_bits=key_bits)
+    pipe = cs.Pipeline(coord_bits, key_bits, cs.HILBERT, bucket, ngmax, 1.0, 1.0, focus[1] > focus[0], True)
+    tx, ty, tz, th = to_dev(x, y, z, h)
+    res = pipe.run(tx, ty, tz, th, cs.make_box(lo, hi, bnd), focus)
+    out = pipe.outputs()
+    torch.cuda.synchronize()
+    assert np.array_equal(keys_u(out["sorted_keys"]), ref["sorted_keys"])
+    assert np.array_equal(u32(out["order"]), ref["perm"])
+    assert np.array_equal(keys_u(out["leaves"]), ref["leaves"])
+    assert np.array_equal(u32(out["counts"]), ref["counts"])
+    assert res.iterations == ref["iterations"]
+    tree = ref["tree"]
+    assert np.array_equal(keys_u(out["prefixes"]), tree.prefixes)
+    assert np.array_equal(out["child_offsets"].cpu().numpy(), tree.child_offsets)
+    assert np.array_equal(out["parents"].cpu().numpy(), tree.parents)
+    assert np.array_equal(out["internal_to_leaf"].cpu().numpy(), tree.internal_to_leaf)
+    assert np.array_equal(out["leaf_to_internal"].cpu().numpy(), tree.leaf_to_internal)
+    assert np.array_equal(out["centers"].cpu().numpy(), ref["centers"])
+    assert np.array_equal(out["sizes"].cpu().numpy(), ref["sizes"])
+    if ref["flags"] is not None:
+        assert np.array_equal(out["halo_flags"].cpu().numpy(), ref["flags"])
+    neighbor_lists_equal(u32(out["neighbors"]), u32(out["neighbor_counts"]), ref["nb"], ref["nc"], ngmax)
+    return res
+
+
+def test_pipeline_uniform_c1_like(cs, O):
+    """BASELINE config 1 shape at reduced size: U[-1,1]^3, constant h, Hilbert64, bucket 64, ngmax 150"""
+    n = 1 << 17
+    x, y, z = (O.philox_uniform(1, s, n, -1.0, 1.0) for s in range(3))
+    h = np.full(n, 0.028 * (2 ** 20 / n) ** (1 / 3))  # ~93 neighbours, as h = 0.028 at N = 2^20
+    res = _check_against_oracle(cs, O, x, y, z, h, -1.0, 1.0, 0, 64, 150, (0, 0))
+    assert res.num_leaves > 0
+
+
+def test_pipeline_plummer_c2_like(cs, O):
+    """BASELINE config 2 shape at reduced size: Plummer, tight box, adaptive h (~100 neighbours), halos in the first
+    quarter of the key space, ngmax 200"""
+    n = 1 << 17
+    x, y, z = O.plummer(5, n)
+    lo, hi = (x.min(), y.min(), z.min()), (x.max(), y.max(), z.max())
+    h = O.h_for_k_neighbors_cpu(x, y, z, O.make_box(lo, hi), 100)
+    res = _check_against_oracle(cs, O, x, y, z, h, lo, hi, 0, 64, 200, (0, 1 << 61))
+    assert res.focus_last > res.focus_first
+
+
+def test_pipeline_periodic_f64(cs, O):
+    n = 1 << 16
+    x, y, z = (O.philox_uniform(3, s, n, 0.0, 1.0) for s in range(3))
+    h = np.full(n, 1.2 * n ** (-1 / 3))
+    _check_against_oracle(cs, O, x, y, z, h, 0.0, 1.0, 1, 32, 150, (0, 1 << 61))
+
+
+def test_pipeline_host_call_matches_device_call(cs, O):
+    n = 1 << 16
+    x, y, z = O.plummer(8, n)
+    lo, hi = (x.min(), y.min(), z.min()), (x.max(), y.max(), z.max())
+    h = O.h_for_k_neighbors_cpu(x, y, z, O.make_box(lo, hi), 50)
+    box = cs.make_box(lo, hi)
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, 64, 100, 1.0, 1.0, True, True)
+    tx, ty, tz, th = to_dev(x, y, z, h)
+    pipe.run(tx, ty, tz, th, box, (0, 1 << 61))
+    nc_dev = pipe.outputs()["neighbor_counts"].clone()
+    flags_dev = pipe.outputs()["halo_flags"].clone()
+    hx, hy, hz, hh = (torch.from_numpy(a).pin_memory() for a in (x, y, z, h))
+    nc_host = torch.empty(n, dtype=torch.int32).pin_memory()
+    flags_host = torch.empty(flags_dev.numel(), dtype=torch.uint8).pin_memory()
+    pipe.run_host(hx, hy, hz, hh, box, (0, 1 << 61), nc_host, flags_host)
+    assert torch.equal(nc_host, nc_dev.cpu())
+    assert torch.equal(flags_host, flags_dev.cpu())
+
+
+def test_pipeline_repeated_runs_reuse_buffers(cs, O):
+    """a second run on different inputs (smaller, then larger) gives the same results as fresh objects"""
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, 32, 64, 1.0, 1.0, False, True)
+    for n, seed in ((40000, 1), (20000, 2), (70000, 3)):
+        x, y, z = (O.philox_uniform(seed, s, n, -1.0, 1.0) for s in range(3))
+        h = np.full(n, 0.05)
+        tx, ty, tz, th = to_dev(x, y, z, h)
+        pipe.run(tx, ty, tz, th, cs.make_box(-1.0, 1.0))
+        fresh = cs.Pipeline(64, 64, cs.HILBERT, 32, 64, 1.0, 1.0, False, True)
+        fresh.run(tx, ty, tz, th, cs.make_box(-1.0, 1.0))
+        a, b = pipe.outputs(), fresh.outputs()
+        torch.cuda.synchronize()
+        for k in ("sorted_keys", "leaves", "counts", "neighbor_counts"):
+            assert torch.equal(a[k], b[k]), (n, k)
