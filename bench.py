@@ -254,7 +254,9 @@ def main():
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(args.steps):
+            torch.cuda.nvtx.range_push("step")
             pipe.run(tx, ty, tz, th, box, FOCUS)
+            torch.cuda.nvtx.range_pop()
             st = pipe.stage_times()
             for k in st:
                 stage_acc[k] += st[k]
