@@ -132,6 +132,18 @@ int cs_sort_pairs_u64(cs_stream_t stream, uint64_t* keys, uint32_t* values, size
                       uint32_t* values_alt, int begin_bit, int end_bit, int values_are_iota, void* workspace,
                       size_t workspace_bytes);
 
+/* No counterpart in the reference. The same stable sort of u64 keys for callers that cannot allocate device memory
+ * when they sort (all device memory reserved up front by the host application's own pool, or a time-step loop that
+ * cannot afford cudaMalloc/cudaFree's implicit device synchronisation). Every temporary lives in one fixed
+ * file-scope device array, held by each device that loads the library until the process exits; the caller passes
+ * only keys and values, sorted in place. At most CS_SORT_NOALLOC_MAX_N keys (larger n: CS_ERR_INVALID). All calls
+ * share that array: calls that overlap on the GPU race, so serialise them. The first call on a device looks up the
+ * array's address with that device current; make it before any stream capture. Synchronises the stream on return,
+ * like cs_sort_pairs_u64. */
+#define CS_SORT_NOALLOC_MAX_N 262144
+int cs_sort_pairs_noalloc_u64(cs_stream_t stream, uint64_t* keys, uint32_t* values, size_t n, int begin_bit,
+                              int end_bit, int values_are_iota);
+
 /* ---- permutation gather --------------------------------------------------------------------------------------
  * replaces gather(exec, ordering, in, out) / gatherArrays (primitives/primitives_gpu.cu:74-90, domain/layout.hpp:231).
  * out[i] = in[perm[i]] for i < n. The 4-array form gathers x, y, z, h in one pass. */
