@@ -3,8 +3,9 @@
 // box (traversal/collisions.hpp:25-94, traversal/collisions_gpu.cu:23-77, traversal/boxoverlap.hpp:127-291).
 //
 // Search boxes: 8 lanes per leaf stride over its particles; min/max are exact, so any reduction order gives the
-// reference's bits. Collisions: one thread per focus leaf, stackless traversal over childOffsets/parents exactly as
-// singleTraversal (traversal/traversal.hpp:26-69); floating-point expressions unfused, in the reference's order.
+// reference's bits. Collisions: one warp per focus leaf tests 32 nodes at a time (see findHalosWarpKernel); the
+// flagged set equals that of the reference's per-leaf singleTraversal (traversal/traversal.hpp:26-69), and every
+// floating-point expression is unfused and in the reference's order.
 #include "cs_common.cuh"
 #include "halos.cuh"
 
@@ -122,14 +123,24 @@ __device__ bool boxContainedIn(K codeStart, K codeEnd, const T* center, const T*
     return s >= codeStart && e <= codeEnd;
 }
 
+// Warp-cooperative version of the same traversal: a node is tested iff its parent was tested and overlapped, and
+// it is flagged iff it overlaps, so the flagged set does not depend on the visiting order. One warp per focus leaf
+// pops up to four groups of eight siblings from a per-warp LIFO stack, tests the 32 nodes in parallel and pushes the
+// child group of every overlapping internal node. Popping the newest groups first bounds the stack by
+// 28 groups per level (< 21 * 28 + 32 entries).
+constexpr int HALO_WARPS = 4;
+constexpr int HALO_STACK = 1024;
+
 template<class K, class T>
-__global__ void findHalosKernel(const K* __restrict__ prefixes, const int32_t* __restrict__ childOffsets,
-                                const int32_t* __restrict__ parents, const T* __restrict__ nc,
-                                const T* __restrict__ ns, const K* __restrict__ leaves, const T* __restrict__ sc,
-                                const T* __restrict__ ss, BoxParams<T> b, KeyParams<T, K> kp, int firstNode,
-                                int lastNode, uint8_t* flags)
+__global__ void __launch_bounds__(32 * HALO_WARPS)
+    findHalosWarpKernel(const K* __restrict__ prefixes, const int32_t* __restrict__ childOffsets,
+                        const T* __restrict__ nc, const T* __restrict__ ns, const K* __restrict__ leaves,
+                        const T* __restrict__ sc, const T* __restrict__ ss, BoxParams<T> b, KeyParams<T, K> kp,
+                        int firstNode, int lastNode, uint8_t* flags, uint32_t* errWord)
 {
-    int leaf = firstNode + blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ int sStack[HALO_WARPS][HALO_STACK];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int leaf = firstNode + blockIdx.x * HALO_WARPS + warp;
     if (leaf >= lastNode) return;
     const K lowest  = leaves[firstNode];
     const K highest = leaves[lastNode];
@@ -163,42 +174,57 @@ __global__ void findHalosKernel(const K* __restrict__ prefixes, const int32_t* _
         return ov;
     };
 
-    if (!overlaps(0) || childOffsets[0] == 0) return;
-    int node       = childOffsets[0];
-    bool backtrack = false;
-    while (node != 0)
+    // the root is tested by lane 0 alone (a single node)
+    bool rootOv = false;
+    if (lane == 0) rootOv = overlaps(0);
+    rootOv = __shfl_sync(0xffffffffu, rootOv, 0);
+    if (!rootOv || childOffsets[0] == 0) return;
+
+    int* stack = sStack[warp];
+    int top    = 0;
+    if (lane == 0) stack[0] = childOffsets[0];
+    top = 1;
+    __syncwarp();
+    while (top > 0)
     {
-        bool isLeaf  = childOffsets[node] == 0;
-        bool descend = !backtrack && overlaps(node);
-        int sib      = (node - 1) % 8;
-        if (!isLeaf && descend)
+        int ng = min(4, top);
+        top -= ng;
+        int g = lane >> 3;
+        bool push = false;
+        int child = 0;
+        if (g < ng)
         {
-            node      = childOffsets[node];
-            backtrack = false;
+            int node = stack[top + g] + (lane & 7);
+            if (overlaps(node))
+            {
+                child = childOffsets[node];
+                push  = child != 0;
+            }
         }
-        else if (sib < 7)
+        __syncwarp();
+        unsigned pm = __ballot_sync(0xffffffffu, push);
+        if (top + __popc(pm) > HALO_STACK)
         {
-            node++;
-            backtrack = false;
+            if (lane == 0 && errWord) atomicOr(errWord, 1u);
+            return;
         }
-        else
-        {
-            node      = parents[(node - 1) / 8];
-            backtrack = true;
-        }
+        if (push) stack[top + __popc(pm & ((1u << lane) - 1u))] = child;
+        top += __popc(pm);
+        __syncwarp();
     }
 }
 
 template<class K, class T>
 int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, const int32_t* parents, const T* nc,
               const T* ns, const K* leaves, const T* sc, const T* ss, const cs_box& box, int first, int last,
-              uint8_t* flags)
+              uint8_t* flags, uint32_t* errWord)
 {
     if (last <= first) return CS_OK;
     auto bp = makeBoxParams<T>(box);
     auto kp = makeKeyParams<T, K>(bp);
-    findHalosKernel<K, T><<<iceil(size_t(last - first), 128), 128, 0, s>>>(prefixes, childOffsets, parents, nc, ns,
-                                                                          leaves, sc, ss, bp, kp, first, last, flags);
+    unsigned blocks = iceil(size_t(last - first), HALO_WARPS);
+    findHalosWarpKernel<K, T><<<blocks, 32 * HALO_WARPS, 0, s>>>(prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp,
+                                                                 first, last, flags, errWord);
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }
@@ -209,13 +235,13 @@ template int searchBoxes<double>(cudaStream_t, const double*, const double*, con
                                  const uint32_t*, int, int, double, const int32_t*, const double*, double*, double*);
 template int findHalos<uint32_t, float>(cudaStream_t, const uint32_t*, const int32_t*, const int32_t*, const float*,
                                         const float*, const uint32_t*, const float*, const float*, const cs_box&, int,
-                                        int, uint8_t*);
+                                        int, uint8_t*, uint32_t*);
 template int findHalos<uint64_t, float>(cudaStream_t, const uint64_t*, const int32_t*, const int32_t*, const float*,
                                         const float*, const uint64_t*, const float*, const float*, const cs_box&, int,
-                                        int, uint8_t*);
+                                        int, uint8_t*, uint32_t*);
 template int findHalos<uint64_t, double>(cudaStream_t, const uint64_t*, const int32_t*, const int32_t*, const double*,
                                          const double*, const uint64_t*, const double*, const double*, const cs_box&,
-                                         int, int, uint8_t*);
+                                         int, int, uint8_t*, uint32_t*);
 
 } // namespace csg
 
@@ -246,7 +272,7 @@ extern "C" int cs_search_boxes_f64(cs_stream_t stream, const double* x, const do
             return CS_ERR_INVALID;                                                                                     \
         }                                                                                                              \
         return findHalos<K, T>(cudaStream_t(stream), prefixes, childOffsets, parents, nc, ns, leaves, sc, ss, *box,    \
-                               first, last, flags);                                                                    \
+                               first, last, flags, nullptr);                                                           \
     }
 CS_HALOS_ENTRY(u32, uint32_t, f32, float)
 CS_HALOS_ENTRY(u64, uint64_t, f32, float)

@@ -12,6 +12,6 @@ int searchBoxes(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, 
 template<class K, class T>
 int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, const int32_t* parents, const T* nc,
               const T* ns, const K* leaves, const T* sc, const T* ss, const cs_box& box, int first, int last,
-              uint8_t* flags);
+              uint8_t* flags, uint32_t* errWord);
 
 } // namespace csg

@@ -123,16 +123,19 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
         bx = __double2float_rn(__dsub_rn(xi, double(Px)));
         by = __double2float_rn(__dsub_rn(yi, double(Py)));
         bz = __double2float_rn(__dsub_rn(zi, double(Pz)));
+        // thresholds in FP32 with directed rounding, so each is a true lower / upper bound of its real value:
+        // R >= max |x_i - P| over the warp, C >= max |x|, A = 4 eps R + 4 eps^2 C
         float rloc = active ? fmaxf(fabsf(bx), fmaxf(fabsf(by), fabsf(bz))) : 0.f;
-        double R   = double(warpMaxF(rloc)) * (1.0 + 8 * EPSD);
-        double C   = double(*prep.cmax) * (1.0 + 8 * EPSD);
-        double Ad  = 4 * EPSD * R + 4 * EPSD * EPSD * C;
-        double rr  = sqrt(r2) * (1.0 + 4 * EPSD);
-        double tin = r2 * (1 - 24 * EPSD) - 8 * Ad * rr - 32 * Ad * Ad;
-        double tou = r2 * (1 + 24 * EPSD) + 8 * Ad * rr + 32 * Ad * Ad;
-        Tin        = __double2float_rd(tin);
-        Tout       = __double2float_ru(tou);
-        A          = __double2float_ru(Ad * (1.0 + 8 * EPSD));
+        float R    = __fmul_ru(warpMaxF(rloc), 1.f + 4 * EPS32);
+        float C    = __fmul_ru(*prep.cmax, 1.f + 4 * EPS32);
+        A          = __fmaf_ru(4 * EPS32, R, __fmul_ru(4 * EPS32 * EPS32, C));
+        float r2lo = __double2float_rd(r2);
+        float r2hi = __double2float_ru(r2);
+        float rr   = __fsqrt_ru(r2hi);
+        float m    = __fmul_ru(__fmul_ru(8.f, A), rr);
+        float q    = __fmul_ru(__fmul_ru(32.f, A), A);
+        Tin        = __fadd_rd(__fadd_rd(__fmul_rd(r2lo, 1.f - 24 * EPS32), -m), -q);
+        Tout       = __fadd_ru(__fadd_ru(__fmul_ru(r2hi, 1.f + 24 * EPS32), m), q);
         cLo        = __double2float_rd(cellR2);
         cHi        = __double2float_ru(cellR2);
     }
@@ -153,18 +156,25 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
                 else
                 {
                     float4 ch = prep.chi[node], cl = prep.clo[node], sz = prep.sz[node];
-                    float Dx = __fsub_rn(__fadd_rn(__fsub_rn(ch.x, Px), cl.x), bx);
-                    float Dy = __fsub_rn(__fadd_rn(__fsub_rn(ch.y, Py), cl.y), by);
-                    float Dz = __fsub_rn(__fadd_rn(__fsub_rn(ch.z, Pz), cl.z), bz);
-                    float tx = fmaxf(fabsf(Dx) - sz.x, 0.f);
-                    float ty = fmaxf(fabsf(Dy) - sz.y, 0.f);
-                    float tz = fmaxf(fabsf(Dz) - sz.z, 0.f);
-                    float n2 = fmaf(tz, tz, fmaf(ty, ty, tx * tx));
-                    float gx = fmaf(fabsf(Dx) + sz.x, 1.001f, A);
-                    float gy = fmaf(fabsf(Dy) + sz.y, 1.001f, A);
-                    float gz = fmaf(fabsf(Dz) + sz.z, 1.001f, A);
-                    float g2 = fmaf(gz, gz, fmaf(gy, gy, gx * gx));
-                    float E  = fmaf(16.f * EPS32, g2, fmaf(3.f * A, gx + gy + gz, 4.f * A * A)) * 1.01f;
+                    float D[3] = {__fsub_rn(__fadd_rn(__fsub_rn(ch.x, Px), cl.x), bx),
+                                  __fsub_rn(__fadd_rn(__fsub_rn(ch.y, Py), cl.y), by),
+                                  __fsub_rn(__fadd_rn(__fsub_rn(ch.z, Pz), cl.z), bz)};
+                    float S[3] = {sz.x, sz.y, sz.z};
+                    float d[3], E = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                    {
+                        // t = |c - x| - s differs from its FP64 value by at most u (see the file header); an axis
+                        // with t + u < 0 is 0 in both precisions and adds no error, otherwise its square is off by
+                        // at most 2 u (max(t, 0) + u)
+                        float ad = fabsf(D[k]);
+                        float t  = ad - S[k];
+                        float u  = fmaf(4.5f * EPS32, ad + S[k], 1.05f * A);
+                        d[k]     = fmaxf(t, 0.f);
+                        if (t + u >= 0.f) E = fmaf(2.f * u, d[k] + u, E);
+                    }
+                    float n2 = fmaf(d[2], d[2], fmaf(d[1], d[1], d[0] * d[0]));
+                    E        = fmaf(1.02f, E, fmaf(6.f * EPS32, n2, 1e-37f));
                     if (n2 + E < cLo) ok = true;
                     else if (n2 - E >= cHi) ok = false;
                     else ok = cellOverlapsExact<T>(xi, yi, zi, false, cellR2, c, s, a.b);

@@ -225,7 +225,7 @@ struct Pipeline final : PipelineBase
             {
                 if ((rc = findHalos<K, T>(s, prefixes.as<K>(), childOffsets.as<int32_t>(), parents.as<int32_t>(),
                                           centers.as<T>(), sizes.as<T>(), leaves.as<K>(), sc.as<T>(), ss.as<T>(), box,
-                                          br.focusFirst, br.focusLast, flags.as<uint8_t>())))
+                                          br.focusFirst, br.focusLast, flags.as<uint8_t>(), err + 2)))
                     return rc;
             }
         }
@@ -274,13 +274,18 @@ struct Pipeline final : PipelineBase
             }
             CSG_CUDA_TRY(cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, s));
         }
-        uint32_t herr[2] = {0, 0};
+        uint32_t herr[3] = {0, 0, 0};
         CSG_CUDA_TRY(cudaMemcpyAsync(herr, errWords.p, sizeof(herr), cudaMemcpyDeviceToHost, s));
         CSG_CUDA_TRY(cudaStreamSynchronize(s));
         if (herr[0] | herr[1])
         {
             setLastError("pipeline: a bounded device wait timed out (sort look-back)");
             return CS_ERR_TIMEOUT;
+        }
+        if (herr[2])
+        {
+            setLastError("pipeline: halo traversal stack overflow (malformed tree)");
+            return CS_ERR_DEVICE;
         }
         return CS_OK;
     }
