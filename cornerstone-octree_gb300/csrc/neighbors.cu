@@ -76,6 +76,40 @@ __device__ __forceinline__ T pairDist2Exact(T xi, T yi, T zi, bool pbc, T xj, T 
     return RN<T>::add(RN<T>::add(RN<T>::mul(dx, dx), RN<T>::mul(dy, dy)), RN<T>::mul(dz, dz));
 }
 
+// Exact FP64 decisions of the pre-filter's rare ambiguous cases. They are kept out of line: inlined, the compiler
+// may hoist their FP64 multiplies into the FP32 fast path, and FP64 issues at a small fraction of the FP32 rate here.
+struct PbcArgs
+{
+    double len[3], ilen[3];
+    int pbc[3];
+};
+
+__device__ __noinline__ bool cellExactF64(double xi, double yi, double zi, bool pbc, double cellR2, const double* c,
+                                          const double* s, PbcArgs pa)
+{
+    BoxParams<double> b;
+    for (int k = 0; k < 3; ++k)
+    {
+        b.len[k]  = pa.len[k];
+        b.ilen[k] = pa.ilen[k];
+        b.pbc[k]  = pa.pbc[k];
+    }
+    return cellOverlapsExact<double>(xi, yi, zi, pbc, cellR2, c, s, b);
+}
+
+__device__ __noinline__ bool pairExactF64(double xi, double yi, double zi, bool pbc, double r2, const double* x,
+                                          const double* y, const double* z, uint32_t j, PbcArgs pa)
+{
+    BoxParams<double> b;
+    for (int k = 0; k < 3; ++k)
+    {
+        b.len[k]  = pa.len[k];
+        b.ilen[k] = pa.ilen[k];
+        b.pbc[k]  = pa.pbc[k];
+    }
+    return pairDist2Exact<double>(xi, yi, zi, pbc, x[j], y[j], z[j], b) < r2;
+}
+
 __device__ __forceinline__ float warpMaxF(float v)
 {
     for (int o = 16; o > 0; o >>= 1)
@@ -83,7 +117,7 @@ __device__ __forceinline__ float warpMaxF(float v)
     return v;
 }
 
-template<class T>
+template<class T, bool Stats>
 __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, NbPrep prep)
 {
     constexpr bool F64 = std::is_same_v<T, double>;
@@ -140,19 +174,30 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
         cHi        = __double2float_ru(cellR2);
     }
 
+    PbcArgs pa;
+    for (int k = 0; k < 3; ++k)
+    {
+        pa.len[k]  = double(a.b.len[k]);
+        pa.ilen[k] = double(a.b.ilen[k]);
+        pa.pbc[k]  = a.b.pbc[k];
+    }
     const unsigned ngmax = a.ngmax;
     uint32_t* myNb       = a.nb + size_t(i - a.first) * ngmax;
     unsigned nc          = 0;
+    // optional statistics, accumulated per lane and flushed once per warp
+    unsigned long long stCell = 0, stCellExact = 0, stPair = 0, stPairExact = 0, stLeaves = 0, stCand = 0, stNodes = 0;
 
     auto cellTest = [&](int node, unsigned parentMask) -> unsigned {
         bool ok = false;
+        if constexpr (Stats) stNodes++;
         if ((parentMask >> lane) & 1u)
         {
+            if constexpr (Stats) stCell++;
             const T* c = a.centers + 3 * size_t(node);
             const T* s = a.sizes + 3 * size_t(node);
             if constexpr (F64)
             {
-                if (pbc) { ok = cellOverlapsExact<T>(xi, yi, zi, true, cellR2, c, s, a.b); }
+                if (pbc) { ok = cellExactF64(xi, yi, zi, true, cellR2, c, s, pa); }
                 else
                 {
                     float4 ch = prep.chi[node], cl = prep.clo[node], sz = prep.sz[node];
@@ -177,7 +222,11 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
                     E        = fmaf(1.02f, E, fmaf(6.f * EPS32, n2, 1e-37f));
                     if (n2 + E < cLo) ok = true;
                     else if (n2 - E >= cHi) ok = false;
-                    else ok = cellOverlapsExact<T>(xi, yi, zi, false, cellR2, c, s, a.b);
+                    else
+                    {
+                        if constexpr (Stats) stCellExact++;
+                        ok = cellExactF64(xi, yi, zi, false, cellR2, c, s, pa);
+                    }
                 }
             }
             else { ok = cellOverlapsExact<T>(xi, yi, zi, pbc, cellR2, c, s, a.b); }
@@ -190,6 +239,11 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
         uint32_t first = a.layout[leafIdx];
         uint32_t last  = a.layout[leafIdx + 1];
         const bool mine = (mask >> lane) & 1u;
+        if constexpr (Stats)
+        {
+            stLeaves++;
+            stCand += last - first;
+        }
         for (uint32_t base = first; base < last; base += 32)
         {
             uint32_t j = base + lane;
@@ -218,14 +272,19 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
                     bool in;
                     if constexpr (F64)
                     {
-                        if (pbc) { in = pairDist2Exact<T>(xi, yi, zi, true, a.x[jj], a.y[jj], a.z[jj], a.b) < r2; }
+                        if (pbc) { in = pairExactF64(xi, yi, zi, true, r2, a.x, a.y, a.z, jj, pa); }
                         else
                         {
                             float dx = c.x - bx, dy = c.y - by, dz = c.z - bz;
                             float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                            if constexpr (Stats) stPair++;
                             if (d2 >= Tout) continue;
                             in = d2 < Tin;
-                            if (!in) in = pairDist2Exact<T>(xi, yi, zi, false, a.x[jj], a.y[jj], a.z[jj], a.b) < r2;
+                            if (!in)
+                            {
+                                if constexpr (Stats) stPairExact++;
+                                in = pairExactF64(xi, yi, zi, false, r2, a.x, a.y, a.z, jj, pa);
+                            }
                         }
                     }
                     else { in = pairDist2Exact<T>(xi, yi, zi, pbc, T(c.x), T(c.y), T(c.z), a.b) < r2; }
@@ -280,6 +339,20 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
         }
     }
     if (active) a.nc[i - a.first] = nc;
+    if constexpr (Stats)
+    {
+        unsigned long long v[7] = {stCell, stCellExact, stPair, stPairExact, stLeaves, stCand, stNodes};
+#pragma unroll
+        for (int k = 0; k < 7; ++k)
+        {
+            unsigned long long x = v[k];
+            if (k >= 4) x = lane == 0 ? x : 0; // per-warp quantities: count once
+            for (int o = 16; o > 0; o >>= 1)
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) atomicAdd(a.stats + k, x);
+        }
+        if (lane == 0) atomicAdd(a.stats + 7, 1ull);
+    }
 }
 
 // float shadows of the FP64 particle coordinates and node boxes, and the magnitude bound C
@@ -375,7 +448,8 @@ int findNeighbors(cudaStream_t s, const NbArgs<T>& a, const NbPrep& prep)
     if (a.last <= a.first) return CS_OK;
     size_t warps  = (size_t(a.last - a.first) + 31) / 32;
     size_t blocks = (warps + NB_WARPS - 1) / NB_WARPS;
-    findNeighborsKernel<T><<<unsigned(blocks), NB_THREADS, 0, s>>>(a, prep);
+    if (a.stats) findNeighborsKernel<T, true><<<unsigned(blocks), NB_THREADS, 0, s>>>(a, prep);
+    else findNeighborsKernel<T, false><<<unsigned(blocks), NB_THREADS, 0, s>>>(a, prep);
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }

@@ -22,6 +22,10 @@ struct NbArgs
     unsigned ngmax;
     uint32_t* nb;
     uint32_t* nc;
+    //! optional traversal statistics (null: off): [0] lane cell tests, [1] cell tests decided in FP64,
+    //! [2] lane pair tests, [3] pair tests decided in FP64, [4] leaves visited per warp, [5] candidates staged,
+    //! [6] nodes visited per warp, [7] warps
+    unsigned long long* stats = nullptr;
 };
 
 //! float shadows for the FP64 pre-filter: particles x = hi + lo (two floats), node centres hi + lo, node sizes

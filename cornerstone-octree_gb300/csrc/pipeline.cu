@@ -12,6 +12,8 @@
 #include "sfc_keys.cuh"
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <memory>
 #include <type_traits>
 
@@ -82,7 +84,9 @@ struct Pipeline final : PipelineBase
     DevBuf buildWs, leaves, counts, layout;
     DevBuf prefixes, childOffsets, parents, levelRange, i2l, l2i, linkWs;
     DevBuf centers, sizes, sc, ss, flags;
-    DevBuf nbPrepWs, nb, nc;
+    DevBuf nbPrepWs, nb, nc, nbStats;
+    // opt-in traversal statistics of the neighbour search, printed to stderr (CSTONE_GB300_NB_STATS=1)
+    bool statsOn = std::getenv("CSTONE_GB300_NB_STATS") != nullptr;
     int capacity = 0;
     size_t n     = 0;
     cs_pipeline_result last{};
@@ -252,7 +256,24 @@ struct Pipeline final : PipelineBase
                           layout.as<uint32_t>(), centers.p, sizes.p, cfg.search_ext};
             NbArgs<T> a = makeNbArgs<T>(xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), 0, uint32_t(n), box, nv,
                                         cfg.ngmax, nb.as<uint32_t>(), nc.as<uint32_t>());
+            if (statsOn)
+            {
+                if ((rc = nbStats.ensure(8 * sizeof(unsigned long long)))) return rc;
+                CSG_CUDA_TRY(cudaMemsetAsync(nbStats.p, 0, 8 * sizeof(unsigned long long), s));
+                a.stats = nbStats.as<unsigned long long>();
+            }
             if ((rc = findNeighbors<T>(s, a, prep))) return rc;
+            if (statsOn)
+            {
+                unsigned long long h[8];
+                CSG_CUDA_TRY(cudaMemcpyAsync(h, nbStats.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+                CSG_CUDA_TRY(cudaStreamSynchronize(s));
+                std::fprintf(stderr,
+                             "[cstone_gb300 neighbour stats] warps %llu | per warp: nodes %.1f leaves %.1f candidates "
+                             "%.1f | lane cell tests %llu (fp64 %llu) | lane pair tests %llu (fp64 %llu)\n",
+                             h[7], double(h[6]) / h[7], double(h[4]) / h[7], double(h[5]) / h[7], h[0], h[1], h[2],
+                             h[3]);
+            }
         }
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_COUNT], s));
 
