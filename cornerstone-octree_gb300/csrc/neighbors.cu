@@ -24,6 +24,7 @@
 #include "neighbors.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 
 namespace csg
@@ -146,6 +147,9 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
                       RN<T>::add(yi, twoh) <= a.b.hi[1] && RN<T>::add(zi, twoh) <= a.b.hi[2];
         pbc = !inside;
     }
+    // in the default mode this kernel only serves warps with a particle whose search sphere crosses a periodic
+    // boundary; findNeighborsGroupKernel serves all others
+    if (a.pathOnlyPbcWarps && !__any_sync(0xffffffffu, active && pbc)) return;
 
     // ---- FP32 pre-filter state (T = double) ----
     float Px = 0, Py = 0, Pz = 0, bx = 0, by = 0, bz = 0, A = 0, Tin = 0, Tout = 0, cLo = 0, cHi = 0;
@@ -355,6 +359,498 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
     }
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// Group traversal (all warps whose particles' search spheres stay inside the box, or open boxes).
+//
+// The reference visits a leaf for particle i only if every node on the root path passes i's pruning test. For a pair
+// (i, j) with d2(i, j) clearly below the pruning radius that condition always holds: j lies in every ancestor's box
+// up to the rounding slack delta of the key quantisation and of the node box arithmetic, so every ancestor is within
+// sqrt(d2) + sqrt(3) kappa of x_i (kappa = delta + the FP rounding of the cell test). Hence
+//   accept iff d2 < r2 and (d2 < Tsafe = cellR2 (1 - rho) - 4 kappa sqrt(cellR2) - 4 kappa^2
+//                           or every ancestor of j's leaf passes i's exact cell test)
+// gives exactly the reference's neighbour set; the explicit ancestor walk is needed only inside the thin band
+// [Tsafe, r2). The tree is therefore walked once per warp with a conservative group test (node box against the
+// bounding box of the warp's 32 search spheres, all boxes widened by their rounding margins), testing the 8
+// children of a node in parallel and keeping the reference's depth-first order with a per-warp stack, so leaves are
+// still met in SFC order and every lane sees its candidates in ascending j. Each reached leaf gets one conservative
+// per-lane test (lower bound of the distance from x_i to the leaf box) that decides which lanes scan it.
+// ---------------------------------------------------------------------------------------------------------------
+constexpr int NBG_STACK = 192;
+
+// exact decision of a pair in the ambiguous band (T = double): d2 < r2 and the reference's path condition
+__device__ __noinline__ bool pairDecideF64(double xi, double yi, double zi, double r2, double cellR2, double kappa,
+                                           const double* x, const double* y, const double* z, uint32_t j, int leafNode,
+                                           const int32_t* parents, const double* centers, const double* sizes)
+{
+    double dx = __dsub_rn(x[j], xi), dy = __dsub_rn(y[j], yi), dz = __dsub_rn(z[j], zi);
+    double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    if (!(d2 < r2)) return false;
+    double ts = cellR2 * (1.0 - 0x1p-46) - 4.0 * kappa * sqrt(cellR2) - 4.0 * kappa * kappa;
+    if (d2 < ts) return true;
+    BoxParams<double> nb{};
+    for (int n = leafNode;;)
+    {
+        if (!cellOverlapsExact<double>(xi, yi, zi, false, cellR2, centers + 3 * size_t(n), sizes + 3 * size_t(n), nb))
+            return false;
+        if (n == 0) return true;
+        n = parents[(n - 1) / 8];
+    }
+}
+
+// the reference's path condition for a float pair already known to be within r (T = float)
+__device__ __noinline__ bool pathCheckF32(float xi, float yi, float zi, float cellR2, int leafNode,
+                                          const int32_t* parents, const float* centers, const float* sizes)
+{
+    BoxParams<float> nb{};
+    for (int n = leafNode;;)
+    {
+        if (!cellOverlapsExact<float>(xi, yi, zi, false, cellR2, centers + 3 * size_t(n), sizes + 3 * size_t(n), nb))
+            return false;
+        if (n == 0) return true;
+        n = parents[(n - 1) / 8];
+    }
+}
+
+__device__ __forceinline__ float warpMinF(float v)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+template<class T, bool Stats, int G>
+__global__ void __launch_bounds__(NB_THREADS) findNeighborsGroupKernel(NbArgs<T> a, NbPrep prep)
+{
+    // G targets per warp; the 32 / G lanes of one target test consecutive candidates side by side
+    static_assert(G == 8 || G == 16 || G == 32, "targets per warp");
+    constexpr int S      = 32 / G;
+    constexpr bool F64   = std::is_same_v<T, double>;
+    constexpr float EPS  = EPS32;
+    // rounding slack of the key quantisation / node boxes, and of the cell test, in units of C
+    constexpr float KAPPA_REL = F64 ? 32.f * 2.220446e-16f : 32.f * 1.1920929e-7f;
+    constexpr float RHO       = F64 ? 9.5367432e-7f : 7.6293945e-6f; // 2^-20, 2^-17
+
+    __shared__ int sStack[NB_WARPS][NBG_STACK];
+    __shared__ unsigned sMaskStack[NB_WARPS][NBG_STACK];
+    __shared__ float4 sCand[NB_WARPS][32];
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int t = lane % G, s = lane / G;
+    const size_t wid   = size_t(blockIdx.x) * NB_WARPS + warp;
+    const size_t base0 = size_t(a.first) + wid * G;
+    if (base0 >= size_t(a.last)) return;
+    if (a.anyPbc)
+    {
+        // the path kernel serves whole blocks of 32 targets that contain a sphere crossing a periodic boundary
+        size_t b32 = size_t(a.first) + (base0 - size_t(a.first)) / 32 * 32;
+        size_t ip  = b32 + lane;
+        bool act   = ip < size_t(a.last);
+        uint32_t q = act ? uint32_t(ip) : uint32_t(b32);
+        T hq = a.h[q], xq = a.x[q], yq = a.y[q], zq = a.z[q];
+        T twoh      = RN<T>::mul(T(2), hq);
+        bool inside = RN<T>::sub(xq, twoh) >= a.b.lo[0] && RN<T>::sub(yq, twoh) >= a.b.lo[1] &&
+                      RN<T>::sub(zq, twoh) >= a.b.lo[2] && RN<T>::add(xq, twoh) <= a.b.hi[0] &&
+                      RN<T>::add(yq, twoh) <= a.b.hi[1] && RN<T>::add(zq, twoh) <= a.b.hi[2];
+        if (__any_sync(0xffffffffu, act && !inside)) return; // served by findNeighborsKernel
+    }
+    const size_t i64  = base0 + t;
+    const bool active = i64 < size_t(a.last);
+    const uint32_t i  = active ? uint32_t(i64) : uint32_t(base0);
+
+    T xi = a.x[i], yi = a.y[i], zi = a.z[i];
+    T hi     = a.h[i];
+    T r2     = RN<T>::mul(RN<T>::mul(T(4.0), hi), hi);
+    T cellR2 = RN<T>::mul(RN<T>::mul(r2, T(a.ext)), T(a.ext));
+
+    // ---- the warp's float frame: P = lane 0's position rounded to float, b = x_i - P ----
+    float P[3], b[3];
+    P[0] = __shfl_sync(0xffffffffu, float(xi), 0);
+    P[1] = __shfl_sync(0xffffffffu, float(yi), 0);
+    P[2] = __shfl_sync(0xffffffffu, float(zi), 0);
+    if constexpr (F64)
+    {
+        b[0] = __double2float_rn(__dsub_rn(xi, double(P[0])));
+        b[1] = __double2float_rn(__dsub_rn(yi, double(P[1])));
+        b[2] = __double2float_rn(__dsub_rn(zi, double(P[2])));
+    }
+    else
+    {
+        b[0] = __fsub_rn(xi, P[0]);
+        b[1] = __fsub_rn(yi, P[1]);
+        b[2] = __fsub_rn(zi, P[2]);
+    }
+    float rloc = active ? fmaxf(fabsf(b[0]), fmaxf(fabsf(b[1]), fabsf(b[2]))) : 0.f;
+    float R    = __fmul_ru(warpMaxF(rloc), 1.f + 4 * EPS);
+    float C    = __fmul_ru(*prep.cmax, 1.f + 64 * EPS);
+    float A    = __fmaf_ru(4 * EPS, R, __fmul_ru(4 * EPS * EPS, C));
+    float delta = __fmul_ru(KAPPA_REL * 0.5f, C); // particle outside its node's float box by at most delta
+    float kappa = __fmul_ru(KAPPA_REL, C);
+    float r2lo, r2hi, cLo, cHi;
+    if constexpr (F64)
+    {
+        r2lo = __double2float_rd(r2);
+        r2hi = __double2float_ru(r2);
+        cLo  = __double2float_rd(cellR2);
+        cHi  = __double2float_ru(cellR2);
+    }
+    else { r2lo = r2hi = r2; cLo = cHi = cellR2; }
+    float rr = __fsqrt_ru(r2hi);
+    // path-safe threshold (lower bound)
+    float tsafe = __fadd_rd(__fadd_rd(__fmul_rd(cLo, 1.f - RHO), -__fmul_ru(__fmul_ru(4.f, kappa), __fsqrt_ru(cHi))),
+                            -__fmul_ru(__fmul_ru(4.f, kappa), kappa));
+    // FP32 pre-filter thresholds (T = double): d2_f < Tacc proves d2_64 < min(r2, Tsafe); d2_f >= Tout proves >= r2
+    float Tacc = 0, Tout = 0;
+    if constexpr (F64)
+    {
+        float m  = __fmul_ru(__fmul_ru(8.f, A), rr);
+        float q  = __fmul_ru(__fmul_ru(32.f, A), A);
+        float lo = fminf(r2lo, tsafe);
+        Tacc     = __fadd_rd(__fadd_rd(__fmul_rd(lo, 1.f - 24 * EPS), -m), -q);
+        Tout     = __fadd_ru(__fadd_ru(__fmul_ru(r2hi, 1.f + 24 * EPS), m), q);
+    }
+
+    // ---- bounding box of the warp's search spheres, widened by the frame's rounding ----
+    float gc[3], gh[3];
+    {
+        float rad = __fmul_ru(rr, 1.f + 64 * EPS);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            float slack = __fmaf_ru(2 * EPS, fabsf(b[k]), delta);
+            float lo    = active ? __fsub_rd(__fsub_rd(b[k], rad), slack) : INFINITY;
+            float hi    = active ? __fadd_ru(__fadd_ru(b[k], rad), slack) : -INFINITY;
+            lo          = warpMinF(lo);
+            hi          = warpMaxF(hi);
+            gc[k]       = 0.5f * (lo + hi);
+            gh[k]       = __fmul_ru(__fsub_ru(hi, lo), 0.5f);
+        }
+    }
+
+    const unsigned ngmax = a.ngmax;
+    uint32_t* myNb       = a.nb + size_t(i - a.first) * ngmax;
+    unsigned nc          = 0;
+    // the lanes serving this lane's target: t, t + G, t + 2G, ...
+    unsigned tmask = 0;
+#pragma unroll
+    for (int q = 0; q < S; ++q)
+        tmask |= 1u << (t + q * G);
+    unsigned long long stLeaves = 0, stCand = 0, stNodes = 0, stPair = 0, stExact = 0;
+
+    // node box in the warp frame: center cc = (chi - P) + clo, half size sz
+    auto nodeFrame = [&](int node, float cc[3], float sz[3]) {
+        float4 ch = prep.chi[node], cl = prep.clo[node], s4 = prep.sz[node];
+        cc[0]     = __fadd_rn(__fsub_rn(ch.x, P[0]), cl.x);
+        cc[1]     = __fadd_rn(__fsub_rn(ch.y, P[1]), cl.y);
+        cc[2]     = __fadd_rn(__fsub_rn(ch.z, P[2]), cl.z);
+        sz[0]     = s4.x;
+        sz[1]     = s4.y;
+        sz[2]     = s4.z;
+    };
+
+    // conservative per-lane test: can a particle of this node lie within the search radius of x_i? (a lower
+    // bound of |x_i - node box|, the box widened by the particle slack delta)
+    auto mayHit = [&](int node) -> bool {
+        float cc[3], sz[3];
+        nodeFrame(node, cc, sz);
+        float n2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            float D = fabsf(__fsub_rn(cc[k], b[k]));
+            float u = __fmaf_ru(4.5f * EPS, D + sz[k], __fmaf_ru(1.05f, A, delta));
+            float d = fmaxf(__fsub_rd(__fsub_rd(D, sz[k]), u), 0.f);
+            n2      = __fmaf_rd(d, d, n2);
+        }
+        return n2 < r2hi;
+    };
+
+    // decision for one candidate of the lane's target that survived the first distance filter
+    auto decide = [&](uint32_t jj, float d2, int node) -> bool {
+        bool in;
+        if constexpr (F64)
+        {
+            in = d2 < Tacc;
+            if (!in)
+            {
+                if constexpr (Stats) stExact++;
+                in = pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
+                                   a.centers, a.sizes);
+            }
+        }
+        else
+        {
+            in = d2 < tsafe;
+            if (!in)
+            {
+                if constexpr (Stats) stExact++;
+                in = pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
+                                  reinterpret_cast<const float*>(a.centers),
+                                  reinterpret_cast<const float*>(a.sizes));
+            }
+        }
+        return in && jj != i;
+    };
+    // first filter: FP32 distance of the staged candidate; returns d2 and whether it can be a neighbour
+    auto filter = [&](float4 c, float& d2) -> bool {
+        if constexpr (F64)
+        {
+            float dx = c.x - b[0], dy = c.y - b[1], dz = c.z - b[2];
+            d2       = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            return d2 < Tout;
+        }
+        else
+        {
+            float dx = __fsub_rn(c.x, float(xi)), dy = __fsub_rn(c.y, float(yi)), dz = __fsub_rn(c.z, float(zi));
+            d2       = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            return d2 < float(r2);
+        }
+    };
+
+    auto processLeaf = [&](int node, unsigned pmask) {
+        bool need     = ((pmask >> lane) & 1u) && mayHit(node);
+        unsigned mask = __ballot_sync(0xffffffffu, need);
+        if (mask == 0) return;
+        int leafIdx    = a.i2l[node];
+        uint32_t first = a.layout[leafIdx];
+        uint32_t last  = a.layout[leafIdx + 1];
+        if constexpr (Stats)
+        {
+            stLeaves++;
+            stCand += last - first;
+        }
+        for (uint32_t base = first; base < last; base += 32)
+        {
+            uint32_t j = base + lane;
+            float4 q   = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j < last)
+            {
+                if constexpr (F64)
+                {
+                    float4 ph = prep.phi[j], pl = prep.plo[j];
+                    q.x = __fadd_rn(__fsub_rn(ph.x, P[0]), pl.x);
+                    q.y = __fadd_rn(__fsub_rn(ph.y, P[1]), pl.y);
+                    q.z = __fadd_rn(__fsub_rn(ph.z, P[2]), pl.z);
+                }
+                else { q = make_float4(a.x[j], a.y[j], a.z[j], 0.f); }
+            }
+            __syncwarp();
+            sCand[warp][lane] = q;
+            __syncwarp();
+            int cnt = int(min(32u, last - base));
+            if constexpr (S == 1)
+            {
+                if (need)
+                {
+                    int k = 0;
+                    // four independent distance chains per step; the rare hits are handled in candidate order
+                    for (; k + 4 <= cnt; k += 4)
+                    {
+                        float e0, e1, e2, e3;
+                        bool h0 = filter(sCand[warp][k], e0);
+                        bool h1 = filter(sCand[warp][k + 1], e1);
+                        bool h2 = filter(sCand[warp][k + 2], e2);
+                        bool h3 = filter(sCand[warp][k + 3], e3);
+                        if constexpr (Stats) stPair += 4;
+                        if (h0 | h1 | h2 | h3)
+                        {
+                            float ev[4] = {e0, e1, e2, e3};
+                            bool hv[4]  = {h0, h1, h2, h3};
+#pragma unroll
+                            for (int q4 = 0; q4 < 4; ++q4)
+                            {
+                                uint32_t jj = base + k + q4;
+                                if (hv[q4] && decide(jj, ev[q4], node))
+                                {
+                                    if (nc < ngmax) myNb[nc] = jj;
+                                    nc++;
+                                }
+                            }
+                        }
+                    }
+                    for (; k < cnt; ++k)
+                    {
+                        float e;
+                        if constexpr (Stats) stPair++;
+                        uint32_t jj = base + k;
+                        if (filter(sCand[warp][k], e) && decide(jj, e, node))
+                        {
+                            if (nc < ngmax) myNb[nc] = jj;
+                            nc++;
+                        }
+                    }
+                }
+            }
+            else
+            {
+                // lane (t, s) tests candidate k0 + s for target t; a ballot keeps each target's hits in order
+                for (int k0 = 0; k0 < cnt; k0 += S)
+                {
+                    int k       = k0 + s;
+                    uint32_t jj = base + k;
+                    bool in     = false;
+                    if (need && k < cnt)
+                    {
+                        float e;
+                        if constexpr (Stats) stPair++;
+                        in = filter(sCand[warp][k], e) && decide(jj, e, node);
+                    }
+                    unsigned hits = __ballot_sync(0xffffffffu, in);
+                    unsigned mine = hits & tmask;
+                    if (in)
+                    {
+                        unsigned pos = nc + __popc(mine & ((1u << lane) - 1u));
+                        if (pos < ngmax) myNb[pos] = jj;
+                    }
+                    nc += __popc(mine);
+                }
+            }
+        }
+    };
+
+    // A warp whose targets are spread far apart (sparse regions, jumps of the curve) has a bounding box much larger
+    // than its spheres; it then tests every child per lane against the lane's own sphere and carries the lanes that
+    // remain alive on the stack, as the per-particle traversal does, instead of using the box.
+    // group bounding sphere around the box centre gc: every point of every lane's sphere is within gR of gc, so it
+    // cuts the corners of the box (which matter where the density rises steeply, e.g. towards a Plummer core)
+    const unsigned activeMask = __ballot_sync(0xffffffffu, active);
+    float rmax                = warpMaxF(active ? rr : 0.f);
+    float gR2;
+    {
+        float e0 = b[0] - gc[0], e1 = b[1] - gc[1], e2 = b[2] - gc[2];
+        float dc = __fsqrt_ru(__fmaf_ru(e2, e2, __fmaf_ru(e1, e1, __fmul_ru(e0, e0))));
+        float sl = __fmaf_ru(2 * EPS, fmaxf(fabsf(b[0]), fmaxf(fabsf(b[1]), fabsf(b[2]))), delta);
+        float gr = active ? __fadd_ru(__fadd_ru(__fmul_ru(dc, 1.f + 8 * EPS), __fmul_ru(rr, 1.f + 64 * EPS)), sl) : 0.f;
+        gr       = warpMaxF(gr);
+        gR2      = __fmul_ru(gr, gr);
+    }
+    // a warp whose targets are spread over more than a few radii tests children per lane (see below); so does a
+    // warp whose group bounds turn out to enclose many more nodes than its spheres (it switches after
+    // LOOSE_AFTER expansions, several times what a compact warp needs)
+    bool loose                 = __fsqrt_ru(gR2) > 3.f * rmax;
+    constexpr int LOOSE_AFTER  = 96;
+    int expansions             = 0;
+    long long t0              = Stats ? clock64() : 0;
+    float rminW               = Stats ? warpMinF(active ? rr : INFINITY) : 0.f;
+
+    int* stack          = sStack[warp];
+    unsigned* maskStack = sMaskStack[warp];
+    int top             = 0;
+    if (a.childOffsets[0] == 0) { processLeaf(0, activeMask); }
+    else
+    {
+        if (lane == 0)
+        {
+            stack[0]     = 0;
+            maskStack[0] = activeMask;
+        }
+        top = 1;
+    }
+    __syncwarp();
+    while (top > 0)
+    {
+        int node       = stack[top - 1];
+        unsigned pmask = maskStack[top - 1];
+        --top;
+        int c0 = a.childOffsets[node];
+        if (c0 == 0)
+        {
+            processLeaf(node, pmask);
+            continue;
+        }
+        if constexpr (Stats) stNodes++;
+        if (++expansions > LOOSE_AFTER) loose = true;
+        bool ok         = false;
+        unsigned cmask  = pmask; // lanes alive in the accepted child (this lane's child when lane < 8)
+        if (!loose)
+        {
+            if (lane < 8)
+            {
+                float cc[3], sz[3];
+                nodeFrame(c0 + lane, cc, sz);
+                ok          = true;
+                float dist2 = 0.f;
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                {
+                    float ad     = fabsf(cc[k] - gc[k]);
+                    float margin = __fmaf_ru(4 * EPS, fabsf(cc[k]) + sz[k] + fabsf(gc[k]) + gh[k],
+                                             __fmaf_ru(4 * EPS * EPS, C, delta));
+                    ok           = ok && (ad - sz[k] - gh[k] < margin);
+                    float dk     = fmaxf(__fsub_rd(__fsub_rd(ad, sz[k]), margin), 0.f);
+                    dist2        = __fmaf_rd(dk, dk, dist2);
+                }
+                ok = ok && dist2 <= gR2;
+            }
+        }
+        else
+        {
+            bool alive = (pmask >> lane) & 1u;
+#pragma unroll 1
+            for (int c = 0; c < 8; ++c)
+            {
+                unsigned m = __ballot_sync(0xffffffffu, alive && mayHit(c0 + c));
+                if (lane == c)
+                {
+                    cmask = m;
+                    ok    = m != 0;
+                }
+            }
+        }
+        unsigned m = __ballot_sync(0xffffffffu, ok);
+        __syncwarp();
+        if (top + 8 > NBG_STACK)
+        {
+            if (lane == 0 && a.errWord) atomicOr(a.errWord, 4u);
+            break;
+        }
+        // accepted children, highest index deepest in the stack, so the lowest is popped first
+        if (ok)
+        {
+            int pos        = top + __popc(m >> (lane + 1));
+            stack[pos]     = c0 + lane;
+            maskStack[pos] = cmask;
+        }
+        top += __popc(m);
+        __syncwarp();
+    }
+    if (active && s == 0) a.nc[i - a.first] = nc;
+    if constexpr (Stats)
+    {
+        unsigned long long v[5] = {stPair, stExact, stLeaves, stCand, stNodes};
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+        {
+            unsigned long long x = v[k];
+            if (k >= 2) x = lane == 0 ? x : 0;
+            for (int o = 16; o > 0; o >>= 1)
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+            // same slots as findNeighborsKernel: [2] pair tests, [3] exact, [4] leaves, [5] candidates, [6] nodes
+            if (lane == 0) atomicAdd(a.stats + 2 + k, x);
+        }
+        if (lane == 0)
+        {
+            atomicAdd(a.stats + 7, 1ull);
+            // slowest warp: [8] cycles, [9] its expansions, [10] leaves, [11] candidates, [12] loose flag,
+            // [13] its first target; [14] number of loose warps
+            unsigned long long cyc = (unsigned long long)(clock64() - t0);
+            if (atomicMax(a.stats + 8, cyc) < cyc)
+            {
+                a.stats[9]  = stNodes;
+                a.stats[10] = stLeaves;
+                a.stats[11] = stCand;
+                a.stats[12] = loose;
+                a.stats[13] = base0;
+                a.stats[15] = __float_as_uint(rmax);
+                a.stats[16] = __float_as_uint(__fsqrt_ru(gR2));
+                a.stats[17] = __float_as_uint(fmaxf(gh[0], fmaxf(gh[1], gh[2])));
+                a.stats[18] = __float_as_uint(rminW);
+                a.stats[19] = __float_as_uint(C);
+            }
+            if (loose) atomicAdd(a.stats + 14, 1ull);
+        }
+    }
+}
+
 // float shadows of the FP64 particle coordinates and node boxes, and the magnitude bound C
 __global__ void prepParticlesKernel(const double* __restrict__ x, const double* __restrict__ y,
                                     const double* __restrict__ z, size_t n, float4* __restrict__ phi,
@@ -404,6 +900,30 @@ __global__ void prepNodesKernel(const double* __restrict__ centers, const double
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m));
 }
 
+// float node boxes of a float tree (centre, zero low part, size) and the magnitude bound C
+__global__ void prepNodesF32Kernel(const float* __restrict__ centers, const float* __restrict__ sizes, int N,
+                                   float4* __restrict__ chi, float4* __restrict__ clo, float4* __restrict__ sz,
+                                   float* cmax)
+{
+    float m = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    {
+        float c[3], s[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            c[k] = centers[3 * size_t(i) + k];
+            s[k] = sizes[3 * size_t(i) + k];
+            m    = fmaxf(m, fabsf(c[k]) + s[k]);
+        }
+        chi[i] = make_float4(c[0], c[1], c[2], 0.f);
+        clo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        sz[i]  = make_float4(s[0], s[1], s[2], 0.f);
+    }
+    m = warpMaxF(m);
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m));
+}
+
 size_t nbPrepBytes(size_t n, int numNodes)
 {
     Arena ar;
@@ -416,12 +936,14 @@ size_t nbPrepBytes(size_t n, int numNodes)
     return ar.size + 256;
 }
 
-int nbPrepare(cudaStream_t s, const double* x, const double* y, const double* z, size_t n, const double* centers,
-              const double* sizes, int numNodes, void* ws, size_t wsBytes, NbPrep* prep)
+template<class T>
+int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, const T* centers, const T* sizes,
+              int numNodes, void* ws, size_t wsBytes, NbPrep* prep)
 {
+    constexpr bool F64 = std::is_same_v<T, double>;
     Arena ar{static_cast<char*>(ws), 0, wsBytes};
-    float4* phi = ar.take<float4>(n);
-    float4* plo = ar.take<float4>(n);
+    float4* phi = ar.take<float4>(F64 ? n : 0);
+    float4* plo = ar.take<float4>(F64 ? n : 0);
     float4* chi = ar.take<float4>(size_t(numNodes));
     float4* clo = ar.take<float4>(size_t(numNodes));
     float4* sz  = ar.take<float4>(size_t(numNodes));
@@ -432,25 +954,64 @@ int nbPrepare(cudaStream_t s, const double* x, const double* y, const double* z,
         return CS_ERR_INVALID;
     }
     CSG_CUDA_TRY(cudaMemsetAsync(cmax, 0, sizeof(float), s));
-    unsigned g = unsigned(std::min<size_t>((n + 255) / 256, size_t(smCount()) * 16));
-    if (n) prepParticlesKernel<<<g, 256, 0, s>>>(x, y, z, n, phi, plo, cmax);
-    CSG_CHECK_LAUNCH();
     unsigned gn = unsigned(std::min<size_t>((size_t(numNodes) + 255) / 256, size_t(smCount()) * 16));
-    if (numNodes) prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+    if constexpr (F64)
+    {
+        unsigned g = unsigned(std::min<size_t>((n + 255) / 256, size_t(smCount()) * 16));
+        if (n) prepParticlesKernel<<<g, 256, 0, s>>>(x, y, z, n, phi, plo, cmax);
+        CSG_CHECK_LAUNCH();
+        if (numNodes) prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+    }
+    else
+    {
+        if (numNodes) prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+    }
     CSG_CHECK_LAUNCH();
     *prep = NbPrep{phi, plo, chi, clo, sz, cmax};
     return CS_OK;
 }
 
+template int nbPrepare<float>(cudaStream_t, const float*, const float*, const float*, size_t, const float*,
+                              const float*, int, void*, size_t, NbPrep*);
+template int nbPrepare<double>(cudaStream_t, const double*, const double*, const double*, size_t, const double*,
+                               const double*, int, void*, size_t, NbPrep*);
+
 template<class T>
-int findNeighbors(cudaStream_t s, const NbArgs<T>& a, const NbPrep& prep)
+int findNeighbors(cudaStream_t s, const NbArgs<T>& a0, const NbPrep& prep)
 {
-    if (a.last <= a.first) return CS_OK;
-    size_t warps  = (size_t(a.last - a.first) + 31) / 32;
+    if (a0.last <= a0.first) return CS_OK;
+    size_t warps  = (size_t(a0.last - a0.first) + 31) / 32;
     size_t blocks = (warps + NB_WARPS - 1) / NB_WARPS;
-    if (a.stats) findNeighborsKernel<T, true><<<unsigned(blocks), NB_THREADS, 0, s>>>(a, prep);
-    else findNeighborsKernel<T, false><<<unsigned(blocks), NB_THREADS, 0, s>>>(a, prep);
+    NbArgs<T> a   = a0;
+    a.pathOnlyPbcWarps = 0;
+    int G = a.groupSize == 8 || a.groupSize == 16 || a.groupSize == 32 ? a.groupSize : 32;
+    if (const char* env = std::getenv("CSTONE_GB300_NB_GROUP")) G = std::atoi(env) == 8 ? 8 : std::atoi(env) == 32 ? 32 : 16;
+    size_t gwarps  = (size_t(a.last - a.first) + G - 1) / G;
+    unsigned gblk  = unsigned((gwarps + NB_WARPS - 1) / NB_WARPS);
+    if (G == 8)
+    {
+        if (a.stats) findNeighborsGroupKernel<T, true, 8><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+        else findNeighborsGroupKernel<T, false, 8><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+    }
+    else if (G == 16)
+    {
+        if (a.stats) findNeighborsGroupKernel<T, true, 16><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+        else findNeighborsGroupKernel<T, false, 16><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+    }
+    else
+    {
+        if (a.stats) findNeighborsGroupKernel<T, true, 32><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+        else findNeighborsGroupKernel<T, false, 32><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+    }
     CSG_CHECK_LAUNCH();
+    if (a.anyPbc)
+    {
+        // warps with a particle whose search sphere crosses a periodic boundary: per-lane path traversal
+        a.pathOnlyPbcWarps = 1;
+        if (a.stats) findNeighborsKernel<T, true><<<unsigned(blocks), NB_THREADS, 0, s>>>(a, prep);
+        else findNeighborsKernel<T, false><<<unsigned(blocks), NB_THREADS, 0, s>>>(a, prep);
+        CSG_CHECK_LAUNCH();
+    }
     return CS_OK;
 }
 
@@ -492,22 +1053,21 @@ int findNeighborsEntry(cudaStream_t s, const T* x, const T* y, const T* z, const
     }
     if (last == first) return CS_OK;
     NbArgs<T> a = makeNbArgs<T>(x, y, z, h, first, last, box, v, ngmax, nb, nc);
+    // the float shadows cover every particle a leaf can reference: [0, layout[L])
+    uint32_t nAll = 0;
     if constexpr (std::is_same_v<T, double>)
     {
-        // the shadows cover every particle a leaf can reference: [0, layout[L])
-        uint32_t nAll = 0;
         CSG_CUDA_TRY(cudaMemcpyAsync(&nAll, v.layout + v.num_leaf_nodes, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         CSG_CUDA_TRY(cudaStreamSynchronize(s));
-        Workspace w;
-        size_t need = nbPrepBytes(nAll, v.num_nodes);
-        int rc      = w.acquire(nullptr, 0, need, s);
-        if (rc) return rc;
-        NbPrep prep;
-        rc = nbPrepare(s, x, y, z, nAll, a.centers, a.sizes, v.num_nodes, w.ptr, need, &prep);
-        if (rc) return rc;
-        return findNeighbors<T>(s, a, prep);
     }
-    else { return findNeighbors<T>(s, a, NbPrep{}); }
+    Workspace w;
+    size_t need = nbPrepBytes(nAll, v.num_nodes);
+    int rc      = w.acquire(nullptr, 0, need, s);
+    if (rc) return rc;
+    NbPrep prep;
+    rc = nbPrepare<T>(s, x, y, z, nAll, a.centers, a.sizes, v.num_nodes, w.ptr, need, &prep);
+    if (rc) return rc;
+    return findNeighbors<T>(s, a, prep);
 }
 
 template int findNeighbors<float>(cudaStream_t, const NbArgs<float>&, const NbPrep&);

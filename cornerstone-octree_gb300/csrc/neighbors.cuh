@@ -26,6 +26,12 @@ struct NbArgs
     //! [2] lane pair tests, [3] pair tests decided in FP64, [4] leaves visited per warp, [5] candidates staged,
     //! [6] nodes visited per warp, [7] warps
     unsigned long long* stats = nullptr;
+    //! path kernel: serve only warps that contain a particle whose search sphere crosses a periodic boundary
+    int pathOnlyPbcWarps = 0;
+    //! device error word (may be null): traversal stack overflow of the group kernel
+    uint32_t* errWord = nullptr;
+    //! targets per warp of the group traversal (8, 16 or 32)
+    int groupSize = 32;
 };
 
 //! float shadows for the FP64 pre-filter: particles x = hi + lo (two floats), node centres hi + lo, node sizes
@@ -40,8 +46,9 @@ struct NbPrep
 };
 
 size_t nbPrepBytes(size_t n, int numNodes);
-int nbPrepare(cudaStream_t s, const double* x, const double* y, const double* z, size_t n, const double* centers,
-              const double* sizes, int numNodes, void* ws, size_t wsBytes, NbPrep* prep);
+template<class T>
+int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, const T* centers, const T* sizes,
+              int numNodes, void* ws, size_t wsBytes, NbPrep* prep);
 
 template<class T>
 NbArgs<T> makeNbArgs(const T* x, const T* y, const T* z, const T* h, uint32_t first, uint32_t last,

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <memory>
 #include <type_traits>
 
@@ -241,13 +242,11 @@ struct Pipeline final : PipelineBase
         if (cfg.do_neighbors)
         {
             if ((rc = nb.ensure(std::max<size_t>(1, n * cfg.ngmax) * sizeof(uint32_t)))) return rc;
-            if constexpr (std::is_same_v<T, double>)
-            {
-                if ((rc = nbPrepWs.ensure(nbPrepBytes(n, N)))) return rc;
-                if ((rc = nbPrepare(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), n, centers.as<T>(), sizes.as<T>(), N,
-                                    nbPrepWs.p, nbPrepWs.bytes, &prep)))
-                    return rc;
-            }
+            size_t nShadow = std::is_same_v<T, double> ? n : 0;
+            if ((rc = nbPrepWs.ensure(nbPrepBytes(nShadow, N)))) return rc;
+            if ((rc = nbPrepare<T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), nShadow, centers.as<T>(), sizes.as<T>(), N,
+                                   nbPrepWs.p, nbPrepWs.bytes, &prep)))
+                return rc;
         }
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_NEIGHBORS], s));
         if (cfg.do_neighbors)
@@ -256,23 +255,39 @@ struct Pipeline final : PipelineBase
                           layout.as<uint32_t>(), centers.p, sizes.p, cfg.search_ext};
             NbArgs<T> a = makeNbArgs<T>(xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), 0, uint32_t(n), box, nv,
                                         cfg.ngmax, nb.as<uint32_t>(), nc.as<uint32_t>());
+            a.errWord   = err + 3;
             if (statsOn)
             {
-                if ((rc = nbStats.ensure(8 * sizeof(unsigned long long)))) return rc;
-                CSG_CUDA_TRY(cudaMemsetAsync(nbStats.p, 0, 8 * sizeof(unsigned long long), s));
+                if ((rc = nbStats.ensure(24 * sizeof(unsigned long long)))) return rc;
+                CSG_CUDA_TRY(cudaMemsetAsync(nbStats.p, 0, 24 * sizeof(unsigned long long), s));
                 a.stats = nbStats.as<unsigned long long>();
             }
             if ((rc = findNeighbors<T>(s, a, prep))) return rc;
             if (statsOn)
             {
-                unsigned long long h[8];
+                unsigned long long h[24];
                 CSG_CUDA_TRY(cudaMemcpyAsync(h, nbStats.p, sizeof(h), cudaMemcpyDeviceToHost, s));
                 CSG_CUDA_TRY(cudaStreamSynchronize(s));
                 std::fprintf(stderr,
-                             "[cstone_gb300 neighbour stats] warps %llu | per warp: nodes %.1f leaves %.1f candidates "
-                             "%.1f | lane cell tests %llu (fp64 %llu) | lane pair tests %llu (fp64 %llu)\n",
+                             "[cstone_gb300 neighbour stats] warps %llu | per warp: node expansions %.1f leaves %.1f "
+                             "candidates %.1f | lane cell tests %llu (fp64 %llu) | lane pair tests %llu "
+                             "(exact %llu)\n",
                              h[7], double(h[6]) / h[7], double(h[4]) / h[7], double(h[5]) / h[7], h[0], h[1], h[2],
                              h[3]);
+                std::fprintf(stderr,
+                             "[cstone_gb300 neighbour stats] slowest warp: %llu cycles, expansions %llu leaves %llu "
+                             "candidates %llu loose %llu first target %llu | loose warps %llu\n",
+                             h[8], h[9], h[10], h[11], h[12], h[13], h[14]);
+                auto asf = [](unsigned long long v) {
+                    unsigned u = unsigned(v);
+                    float f;
+                    std::memcpy(&f, &u, 4);
+                    return double(f);
+                };
+                std::fprintf(stderr,
+                             "[cstone_gb300 neighbour stats] slowest warp geometry: rmax %g rmin %g group radius %g "
+                             "box half %g C %g\n",
+                             asf(h[15]), asf(h[18]), asf(h[16]), asf(h[17]), asf(h[19]));
             }
         }
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_COUNT], s));
@@ -295,13 +310,18 @@ struct Pipeline final : PipelineBase
             }
             CSG_CUDA_TRY(cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, s));
         }
-        uint32_t herr[3] = {0, 0, 0};
+        uint32_t herr[4] = {0, 0, 0, 0};
         CSG_CUDA_TRY(cudaMemcpyAsync(herr, errWords.p, sizeof(herr), cudaMemcpyDeviceToHost, s));
         CSG_CUDA_TRY(cudaStreamSynchronize(s));
         if (herr[0] | herr[1])
         {
             setLastError("pipeline: a bounded device wait timed out (sort look-back)");
             return CS_ERR_TIMEOUT;
+        }
+        if (herr[3])
+        {
+            setLastError("pipeline: neighbour traversal stack overflow (malformed tree)");
+            return CS_ERR_DEVICE;
         }
         if (herr[2])
         {
