@@ -300,7 +300,7 @@ def main():
     nb_bytes = n * (4 * 8 + 4) + 4.0 * stored  # x,y,z,h read + count written + stored neighbour indices
     nb_ms = stages["neighbors"]
     achieved = nb_bytes / (nb_ms * 1e-3) / 1e9
-    roofline = {"kernel": "findNeighborsKernel<double>", "bound": "hbm", "achieved": round(achieved, 1),
+    roofline = {"kernel": "findNeighborsGroupKernel<double>", "bound": "hbm", "achieved": round(achieved, 1),
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": profiled_traffic(n), "algorithmic_bytes": nb_bytes, "ms": round(nb_ms, 4)}
 

@@ -1,7 +1,9 @@
 """Build the GB300 C-ABI library libcstone_gb300.so in-tree with nvcc (sm_103a only).
 
 Each translation unit under csrc/ is compiled in parallel to an object file under csrc/_build/ and linked with
-nvcc -shared. Rebuilds only what changed (source or header newer than its object).
+nvcc -shared. Rebuilds only what changed (source or header newer than its object, or other compiler flags).
+CSTONE_GB300_NVCC_FLAGS adds flags to every compile (e.g. "-DNBG_MIN_BLOCKS=8" to trade registers of the neighbour
+search for occupancy).
 """
 import concurrent.futures as cf
 import glob
@@ -18,7 +20,8 @@ LIB = os.path.join(HERE, "cstone_gb300", "libcstone_gb300.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC", "-I", INCLUDE,
-         "-Xptxas", "-warn-spills"]
+         "-Xptxas", "-warn-spills"] + os.environ.get("CSTONE_GB300_NVCC_FLAGS", "").split()
+STAMP = os.path.join(OBJ_DIR, "flags.txt")
 
 
 def _headers():
@@ -43,6 +46,12 @@ def build(verbose=False, jobs=None):
     os.makedirs(OBJ_DIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdr_time = _headers()
+    stamp = " ".join(ARCH + FLAGS)
+    if not os.path.exists(STAMP) or open(STAMP).read() != stamp:
+        for o in glob.glob(os.path.join(OBJ_DIR, "*.o")):
+            os.remove(o)
+        with open(STAMP, "w") as f:
+            f.write(stamp)
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         results = list(ex.map(lambda s: _compile(s, hdr_time, verbose), srcs))
     errs = [e for _, e in results if e]

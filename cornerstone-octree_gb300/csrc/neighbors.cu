@@ -1,25 +1,44 @@
 // Neighbour search with the CPU reference's exact semantics (findneighbors.hpp:33-177).
 //
-// One warp serves 32 consecutive (SFC-ordered) target particles. The warp walks the tree once, depth first in the
-// reference's stackless order (childOffsets/parents, traversal/traversal.hpp:26-69), and keeps one 32-bit mask per
-// depth: the lanes whose own root-to-node path passed the reference's pruning test
-// |minDistance(x_i, node)|^2 < (2 h_i)^2 ext^2. A node is entered when any lane's path is alive; a lane tests a
-// leaf's particles only if its path reached that leaf. Leaves are visited in SFC order, so each lane meets its
-// candidates in ascending j: the first ngmax stored neighbours are the reference's, and the count is uncapped.
+// Semantics to reproduce. For each target i the reference walks the tree from the root in its stackless order
+// (traversal/traversal.hpp:26-69), descends into a node only if norm2(minDistance(x_i, node box)) < cellR2 with
+// cellR2 = (2 h_i)^2 ext^2, and in each leaf it reaches counts the particles j != i with |x_j - x_i|^2 < (2 h_i)^2,
+// storing the first ngmax of them in visiting order; the count is not capped. Leaves are met in SFC order, so the
+// stored neighbours are the first ngmax in ascending j among those on leaves whose whole root path passed the test.
 //
-// Arithmetic. The reference decides every test in the coordinate precision T without FMA. For T = float this kernel
-// evaluates the same expressions with round-to-nearest intrinsics. For T = double (GB300 has little FP64 throughput)
-// each test is first evaluated in FP32 on coordinates relative to a per-warp reference point P, with a proven bound
-// on the difference to the FP64 result:
+// Main kernel (findNeighborsGroupKernel): one warp serves 32 consecutive targets and walks the tree ONCE for all of
+// them, depth first with an explicit stack of (node, lane mask) in shared memory, lowest child first. A child is
+// pushed when it can hold a neighbour of some lane: normally tested against the bounding box and bounding sphere of
+// the warp's 32 search spheres by lanes 0-7 (one child each); a warp whose targets are spread far apart, or that has
+// already expanded many nodes, tests each child per lane instead and carries the alive lanes on the stack. At a leaf,
+// each lane whose conservative test says the leaf may hold a neighbour stages the leaf's candidates 32 at a time in
+// shared memory and tests them in order. Visiting superset leaves is harmless as long as the final decision equals the
+// reference's, which depends on the whole root path (next paragraph).
+//
+// Path safety. A candidate at distance^2 d2 < r2 is counted by the reference only if each ancestor of its leaf passed
+// the cell test. Every ancestor contains the candidate's key cell, so minDistance(x_i, ancestor) <= |x_j - x_i| up to
+// the rounding of node boxes; with kappa = 32 u C (u the unit roundoff of T, C a bound on |coordinate|) and
+// rho = 2^-20 (f64) / 2^-17 (f32),
+//   Tsafe = cellR2 (1 - rho) - 4 kappa sqrt(cellR2) - 4 kappa^2
+// is a lower bound below which every ancestor test passes in the reference's own arithmetic. Candidates with
+// d2 < min(r2, Tsafe) are accepted outright; the rare ones in [Tsafe, r2) (only when ext < 1 + O(kappa)) walk the
+// ancestor chain explicitly through parents[] with the reference's cell test.
+//
+// Arithmetic. T = float evaluates the reference's expressions with round-to-nearest intrinsics (no contraction).
+// T = double (GB300 has little FP64 throughput) first evaluates each test in FP32 on coordinates relative to a
+// per-warp reference point P, with a proven bound on the difference to the FP64 result:
 //   candidate  a_j = fl((xhi_j - P) + xlo_j)  (x = xhi + xlo, two floats),  target b_i = fl(x_i - P)
 //   per axis   |fl(a_j - b_i) - fl64(x_j - x_i)| <= 3 eps |dx| + A,   A = 4 eps R + 4 eps^2 C,   eps = 2^-24
 //              (R bounds |x_i - P| over the warp's targets, C bounds |x| over all particles)
 //   distance   |d2_f - d2_64| <= 9.2 eps d2 + 3.5 A sqrt(d2) + 6 A^2
-// so d2_f < T_in proves d2_64 < r2 and d2_f >= T_out proves d2_64 >= r2 with
-//   T_in = r2 (1 - 24 eps) - 8 A r - 32 A^2,   T_out = r2 (1 + 24 eps) + 8 A r + 32 A^2.
-// The cell test uses the analogous bound E = 16 eps sum G_k^2 + 3 A sum G_k + 4 A^2 with G_k = |c_k - x_k| + s_k.
-// Only tests that fall inside [T_in, T_out) (or the cell band) are re-evaluated in exact FP64, as are all tests of a
-// particle whose search sphere crosses a periodic boundary.
+// so d2_f < T_acc proves d2_64 < min(r2, Tsafe) and d2_f >= T_out proves d2_64 >= r2 with
+//   T_acc = min(r2, Tsafe) (1 - 24 eps) - 8 A r - 32 A^2,   T_out = r2 (1 + 24 eps) + 8 A r + 32 A^2.
+// Only the tests that fall in [T_acc, T_out) are decided again in exact FP64, in out-of-line functions: inlined, the
+// compiler hoists their FP64 multiplies into the hot FP32 loop.
+//
+// Periodic boundaries. Warps that contain a target whose search sphere crosses a periodic boundary are served by the
+// per-lane path kernel (findNeighborsKernel): each lane keeps a mask per depth of its own root-to-node path and
+// decides every test in T exactly as the reference does, with minimum-image folding.
 #include "cs_common.cuh"
 #include "neighbors.cuh"
 
@@ -376,6 +395,9 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
 // per-lane test (lower bound of the distance from x_i to the leaf box) that decides which lanes scan it.
 // ---------------------------------------------------------------------------------------------------------------
 constexpr int NBG_STACK = 192;
+#ifndef NBG_MIN_BLOCKS
+#define NBG_MIN_BLOCKS 7
+#endif
 
 // exact decision of a pair in the ambiguous band (T = double): d2 < r2 and the reference's path condition
 __device__ __noinline__ bool pairDecideF64(double xi, double yi, double zi, double r2, double cellR2, double kappa,
@@ -419,7 +441,7 @@ __device__ __forceinline__ float warpMinF(float v)
 }
 
 template<class T, bool Stats, int G>
-__global__ void __launch_bounds__(NB_THREADS) findNeighborsGroupKernel(NbArgs<T> a, NbPrep prep)
+__global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroupKernel(NbArgs<T> a, NbPrep prep)
 {
     // G targets per warp; the 32 / G lanes of one target test consecutive candidates side by side
     static_assert(G == 8 || G == 16 || G == 32, "targets per warp");
@@ -590,6 +612,27 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsGroupKernel(NbArgs<T>
         }
         return in && jj != i;
     };
+    // batch thresholds of the S == 1 loop: d2 < Tin is a neighbour (self aside), d2 >= Tup is not, the rest is
+    // decided by decideSlow
+    float Tin, Tup;
+    if constexpr (F64)
+    {
+        Tin = Tacc;
+        Tup = Tout;
+    }
+    else
+    {
+        Tin = fminf(float(r2), tsafe);
+        Tup = float(r2);
+    }
+    auto decideSlow = [&](uint32_t jj, int node) -> bool {
+        if constexpr (F64)
+            return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
+                                 a.centers, a.sizes);
+        else
+            return pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
+                                reinterpret_cast<const float*>(a.centers), reinterpret_cast<const float*>(a.sizes));
+    };
     // first filter: FP32 distance of the staged candidate; returns d2 and whether it can be a neighbour
     auto filter = [&](float4 c, float& d2) -> bool {
         if constexpr (F64)
@@ -621,7 +664,8 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsGroupKernel(NbArgs<T>
         for (uint32_t base = first; base < last; base += 32)
         {
             uint32_t j = base + lane;
-            float4 q   = make_float4(0.f, 0.f, 0.f, 0.f);
+            // beyond the leaf: a point at infinity, which fails every distance test
+            float4 q   = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
             if (j < last)
             {
                 if constexpr (F64)
@@ -641,42 +685,43 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsGroupKernel(NbArgs<T>
             {
                 if (need)
                 {
-                    int k = 0;
-                    // four independent distance chains per step; the rare hits are handled in candidate order
-                    for (; k + 4 <= cnt; k += 4)
+                    // bit k of inM: candidate k passes the FP32 test outright; of ambM: its test is undecided in
+                    // FP32 (or, T = float, its root path must be checked); eight independent distance chains per
+                    // step, the staged points past the leaf's end never pass
+                    unsigned inM = 0, ambM = 0;
+                    for (int k0 = 0; k0 < cnt; k0 += 8)
                     {
-                        float e0, e1, e2, e3;
-                        bool h0 = filter(sCand[warp][k], e0);
-                        bool h1 = filter(sCand[warp][k + 1], e1);
-                        bool h2 = filter(sCand[warp][k + 2], e2);
-                        bool h3 = filter(sCand[warp][k + 3], e3);
-                        if constexpr (Stats) stPair += 4;
-                        if (h0 | h1 | h2 | h3)
-                        {
-                            float ev[4] = {e0, e1, e2, e3};
-                            bool hv[4]  = {h0, h1, h2, h3};
+                        unsigned mi = 0, ma = 0;
 #pragma unroll
-                            for (int q4 = 0; q4 < 4; ++q4)
-                            {
-                                uint32_t jj = base + k + q4;
-                                if (hv[q4] && decide(jj, ev[q4], node))
-                                {
-                                    if (nc < ngmax) myNb[nc] = jj;
-                                    nc++;
-                                }
-                            }
-                        }
-                    }
-                    for (; k < cnt; ++k)
-                    {
-                        float e;
-                        if constexpr (Stats) stPair++;
-                        uint32_t jj = base + k;
-                        if (filter(sCand[warp][k], e) && decide(jj, e, node))
+                        for (int q8 = 0; q8 < 8; ++q8)
                         {
-                            if (nc < ngmax) myNb[nc] = jj;
-                            nc++;
+                            float e;
+                            filter(sCand[warp][k0 + q8], e);
+                            mi |= unsigned(e < Tin) << q8;
+                            ma |= unsigned(e < Tup) << q8;
                         }
+                        inM |= mi << k0;
+                        ambM |= ma << k0;
+                    }
+                    ambM &= ~inM;
+                    if constexpr (Stats)
+                    {
+                        stPair += cnt;
+                        stExact += __popc(ambM);
+                    }
+                    while (ambM)
+                    {
+                        int k = __ffs(ambM) - 1;
+                        ambM &= ambM - 1;
+                        if (decideSlow(base + k, node)) inM |= 1u << k;
+                    }
+                    if (i >= base && i - base < 32u) inM &= ~(1u << (i - base));
+                    while (inM)
+                    {
+                        int k = __ffs(inM) - 1;
+                        inM &= inM - 1;
+                        if (nc < ngmax) myNb[nc] = base + k;
+                        nc++;
                     }
                 }
             }
