@@ -3,7 +3,8 @@
 // box (traversal/collisions.hpp:25-94, traversal/collisions_gpu.cu:23-77, traversal/boxoverlap.hpp:127-291).
 //
 // Search boxes: 8 lanes per leaf stride over its particles; min/max are exact, so any reduction order gives the
-// reference's bits. Collisions: one warp per focus leaf tests 32 nodes at a time (see findHalosWarpKernel); the
+// reference's bits. Collisions: one warp per 32 focus leaves, each lane deciding the containment test for its own
+// leaf, and one warp-wide traversal testing 32 nodes at a time for each leaf that needs it (findHalosWarpKernel); the
 // flagged set equals that of the reference's per-leaf singleTraversal (traversal/traversal.hpp:26-69), and every
 // floating-point expression is unfused and in the reference's order.
 #include "cs_common.cuh"
@@ -124,10 +125,12 @@ __device__ bool boxContainedIn(K codeStart, K codeEnd, const T* center, const T*
 }
 
 // Warp-cooperative version of the same traversal: a node is tested iff its parent was tested and overlapped, and
-// it is flagged iff it overlaps, so the flagged set does not depend on the visiting order. One warp per focus leaf
-// pops up to four groups of eight siblings from a per-warp LIFO stack, tests the 32 nodes in parallel and pushes the
-// child group of every overlapping internal node. Popping the newest groups first bounds the stack by
-// 28 groups per level (< 21 * 28 + 32 entries).
+// it is flagged iff it overlaps, so the flagged set does not depend on the visiting order. One warp serves 32
+// consecutive focus leaves: each lane decides the containment test (FP64 key arithmetic) for its own leaf, then the
+// warp traverses for each leaf whose search box leaves the focus, one after the other. Per traversal the warp pops up
+// to four groups of eight siblings from a per-warp LIFO stack, tests the 32 nodes in parallel and pushes the child
+// group of every overlapping internal node. Popping the newest groups first bounds the stack by 28 groups per level
+// (< 21 * 28 + 32 entries).
 constexpr int HALO_WARPS = 4;
 constexpr int HALO_STACK = 1024;
 
@@ -140,77 +143,104 @@ __global__ void __launch_bounds__(32 * HALO_WARPS)
 {
     __shared__ int sStack[HALO_WARPS][HALO_STACK];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int leaf = firstNode + blockIdx.x * HALO_WARPS + warp;
-    if (leaf >= lastNode) return;
+    const long long leaf0 = firstNode + (long long)(blockIdx.x * HALO_WARPS + warp) * 32;
+    if (leaf0 >= lastNode) return;
     const K lowest  = leaves[firstNode];
     const K highest = leaves[lastNode];
-    T tc[3], ts[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-    {
-        tc[k] = sc[3 * size_t(leaf) + k];
-        ts[k] = ss[3 * size_t(leaf) + k];
-    }
-    if (boxContainedIn<K, T>(lowest, highest, tc, ts, b, kp)) return;
 
-    auto overlaps = [&](int idx) -> bool {
-        K pfx         = prefixes[idx];
-        K nk1         = decodePlaceholderBit<K>(pfx);
-        unsigned plen = decodePrefixLength<K>(pfx);
-        K nk2         = nk1 + (K(1) << (3u * KeyTraits<K>::maxLevel - plen));
-        bool inside   = !(nk1 < lowest || nk2 > highest);
-        if (inside) return false;
-        bool ov = true;
+    T myc[3], mys[3];
+    const int myLeaf = int(leaf0) + lane;
+    bool need        = false;
+    if (myLeaf < lastNode)
+    {
 #pragma unroll
         for (int k = 0; k < 3; ++k)
         {
-            T d = RN<T>::sub(tc[k], nc[3 * size_t(idx) + k]);
-            d   = RN<T>::abs_(pbcFold<T>(d, b.pbc[k], b.len[k], b.ilen[k]));
-            d   = RN<T>::sub(d, ns[3 * size_t(idx) + k]);
-            d   = RN<T>::sub(d, ts[k]);
-            ov  = ov && (d < T(0));
+            myc[k] = sc[3 * size_t(myLeaf) + k];
+            mys[k] = ss[3 * size_t(myLeaf) + k];
         }
-        if (ov) flags[idx] = 1;
-        return ov;
-    };
-
-    // the root is tested by lane 0 alone (a single node)
-    bool rootOv = false;
-    if (lane == 0) rootOv = overlaps(0);
-    rootOv = __shfl_sync(0xffffffffu, rootOv, 0);
-    if (!rootOv || childOffsets[0] == 0) return;
-
-    int* stack = sStack[warp];
-    int top    = 0;
-    if (lane == 0) stack[0] = childOffsets[0];
-    top = 1;
-    __syncwarp();
-    while (top > 0)
+        need = !boxContainedIn<K, T>(lowest, highest, myc, mys, b, kp);
+    }
+    else
     {
-        int ng = min(4, top);
-        top -= ng;
-        int g = lane >> 3;
-        bool push = false;
-        int child = 0;
-        if (g < ng)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            myc[k] = mys[k] = T(0);
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, need);
+    int* stack    = sStack[warp];
+
+    while (todo)
+    {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        T tc[3], ts[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
         {
-            int node = stack[top + g] + (lane & 7);
-            if (overlaps(node))
+            tc[k] = __shfl_sync(0xffffffffu, myc[k], src);
+            ts[k] = __shfl_sync(0xffffffffu, mys[k], src);
+        }
+
+        auto overlaps = [&](int idx) -> bool {
+            K pfx         = prefixes[idx];
+            K nk1         = decodePlaceholderBit<K>(pfx);
+            unsigned plen = decodePrefixLength<K>(pfx);
+            K nk2         = nk1 + (K(1) << (3u * KeyTraits<K>::maxLevel - plen));
+            bool inside   = !(nk1 < lowest || nk2 > highest);
+            if (inside) return false;
+            bool ov = true;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
             {
-                child = childOffsets[node];
-                push  = child != 0;
+                T d = RN<T>::sub(tc[k], nc[3 * size_t(idx) + k]);
+                d   = RN<T>::abs_(pbcFold<T>(d, b.pbc[k], b.len[k], b.ilen[k]));
+                d   = RN<T>::sub(d, ns[3 * size_t(idx) + k]);
+                d   = RN<T>::sub(d, ts[k]);
+                ov  = ov && (d < T(0));
             }
-        }
+            if (ov) flags[idx] = 1;
+            return ov;
+        };
+
+        // the root is tested by lane 0 alone (a single node)
+        bool rootOv = false;
+        if (lane == 0) rootOv = overlaps(0);
+        rootOv = __shfl_sync(0xffffffffu, rootOv, 0);
+        if (!rootOv || childOffsets[0] == 0) continue;
+
+        int top = 0;
         __syncwarp();
-        unsigned pm = __ballot_sync(0xffffffffu, push);
-        if (top + __popc(pm) > HALO_STACK)
+        if (lane == 0) stack[0] = childOffsets[0];
+        top = 1;
+        __syncwarp();
+        while (top > 0)
         {
-            if (lane == 0 && errWord) atomicOr(errWord, 1u);
-            return;
+            int ng = min(4, top);
+            top -= ng;
+            int g      = lane >> 3;
+            bool push  = false;
+            int child  = 0;
+            if (g < ng)
+            {
+                int node = stack[top + g] + (lane & 7);
+                if (overlaps(node))
+                {
+                    child = childOffsets[node];
+                    push  = child != 0;
+                }
+            }
+            __syncwarp();
+            unsigned pm = __ballot_sync(0xffffffffu, push);
+            if (top + __popc(pm) > HALO_STACK)
+            {
+                if (lane == 0 && errWord) atomicOr(errWord, 1u);
+                return;
+            }
+            if (push) stack[top + __popc(pm & ((1u << lane) - 1u))] = child;
+            top += __popc(pm);
+            __syncwarp();
         }
-        if (push) stack[top + __popc(pm & ((1u << lane) - 1u))] = child;
-        top += __popc(pm);
-        __syncwarp();
     }
 }
 
@@ -222,7 +252,7 @@ int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, co
     if (last <= first) return CS_OK;
     auto bp = makeBoxParams<T>(box);
     auto kp = makeKeyParams<T, K>(bp);
-    unsigned blocks = iceil(size_t(last - first), HALO_WARPS);
+    unsigned blocks = iceil(size_t(last - first), 32 * HALO_WARPS);
     findHalosWarpKernel<K, T><<<blocks, 32 * HALO_WARPS, 0, s>>>(prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp,
                                                                  first, last, flags, errWord);
     CSG_CHECK_LAUNCH();

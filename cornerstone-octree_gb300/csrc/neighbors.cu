@@ -53,7 +53,6 @@ constexpr int NB_THREADS  = 128;
 constexpr int NB_WARPS    = NB_THREADS / 32;
 constexpr int NB_MAXDEPTH = 24;
 constexpr float EPS32     = 5.9604644775390625e-8f; // 2^-24
-constexpr double EPSD     = 5.9604644775390625e-8;
 
 template<class T>
 __device__ __forceinline__ T pbcFoldNb(T d, int pbc, T len, T ilen)
@@ -1015,6 +1014,38 @@ int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, cons
     *prep = NbPrep{phi, plo, chi, clo, sz, cmax};
     return CS_OK;
 }
+
+template<class T>
+int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, int numNodes, void* ws, size_t wsBytes,
+                   NbPrep* prep)
+{
+    Arena ar{static_cast<char*>(ws), 0, wsBytes};
+    float4* chi = ar.take<float4>(size_t(numNodes));
+    float4* clo = ar.take<float4>(size_t(numNodes));
+    float4* sz  = ar.take<float4>(size_t(numNodes));
+    if (!ar.ok() || !prep->cmax)
+    {
+        setLastError("find neighbors: node workspace too small or no bound");
+        return CS_ERR_INVALID;
+    }
+    float* cmax = const_cast<float*>(prep->cmax);
+    unsigned gn = unsigned(std::min<size_t>((size_t(numNodes) + 255) / 256, size_t(smCount()) * 16));
+    if (numNodes)
+    {
+        if constexpr (std::is_same_v<T, double>)
+            prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+        else
+            prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+        CSG_CHECK_LAUNCH();
+    }
+    prep->chi = chi;
+    prep->clo = clo;
+    prep->sz  = sz;
+    return CS_OK;
+}
+
+template int nbPrepareNodes<float>(cudaStream_t, const float*, const float*, int, void*, size_t, NbPrep*);
+template int nbPrepareNodes<double>(cudaStream_t, const double*, const double*, int, void*, size_t, NbPrep*);
 
 template int nbPrepare<float>(cudaStream_t, const float*, const float*, const float*, size_t, const float*,
                               const float*, int, void*, size_t, NbPrep*);

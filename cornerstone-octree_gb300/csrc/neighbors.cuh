@@ -50,6 +50,12 @@ template<class T>
 int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, const T* centers, const T* sizes,
               int numNodes, void* ws, size_t wsBytes, NbPrep* prep);
 
+//! node part of nbPrepare only: the particle shadows (T = double) and cmax are set by the caller, cmax already holding
+//! the particles' bound (the node boxes are folded in with an atomic max)
+template<class T>
+int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, int numNodes, void* ws, size_t wsBytes,
+                   NbPrep* prep);
+
 template<class T>
 NbArgs<T> makeNbArgs(const T* x, const T* y, const T* z, const T* h, uint32_t first, uint32_t last,
                      const cs_box& box, const cs_ns_view& v, unsigned ngmax, uint32_t* nb, uint32_t* nc);

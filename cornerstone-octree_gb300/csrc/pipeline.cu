@@ -81,6 +81,7 @@ struct Pipeline final : PipelineBase
     DevBuf inX, inY, inZ, inH;
     DevBuf keys, keysAlt, order, orderAlt;
     DevBuf xs, ys, zs, hs;
+    DevBuf packed, shadowHi, shadowLo; // x,y,z,h records of the keys pass; float shadows made by the gather
     DevBuf sortWs, errWords;
     DevBuf buildWs, leaves, counts, layout;
     DevBuf prefixes, childOffsets, parents, levelRange, i2l, l2i, linkWs;
@@ -109,7 +110,8 @@ struct Pipeline final : PipelineBase
     {
         size_t t = 0;
         for (const DevBuf* b : {&inX, &inY, &inZ, &inH, &keys, &keysAlt, &order, &orderAlt, &xs, &ys, &zs, &hs,
-                                &sortWs, &errWords, &buildWs, &leaves, &counts, &layout, &prefixes, &childOffsets,
+                                &packed, &shadowHi, &shadowLo, &sortWs, &errWords, &buildWs, &leaves, &counts,
+                                &layout, &prefixes, &childOffsets,
                                 &parents, &levelRange, &i2l, &l2i, &linkWs, &centers, &sizes, &sc, &ss, &flags,
                                 &nbPrepWs, &nb, &nc})
             t += b->bytes;
@@ -148,15 +150,25 @@ struct Pipeline final : PipelineBase
             if ((rc = b->ensure(n * sizeof(uint32_t)))) return rc;
         for (DevBuf* b : {&xs, &ys, &zs, &hs})
             if ((rc = b->ensure(n * sizeof(T)))) return rc;
+        if ((rc = packed.ensure(n * sizeof(PackedT<T>)))) return rc;
+        constexpr bool F64 = std::is_same_v<T, double>;
+        const bool shadows = F64 && cfg.do_neighbors;
+        if (shadows)
+            for (DevBuf* b : {&shadowHi, &shadowLo})
+                if ((rc = b->ensure(n * sizeof(float4)))) return rc;
         // keys have 3*maxLevel significant bits (no removeKey entries: they are computed here)
         const int keyBits = 3 * KeyTraits<K>::maxLevel;
         if ((rc = sortWs.ensure(radixSortWorkspaceBytes<K>(n, 0, keyBits)))) return rc;
         if ((rc = errWords.ensure(64))) return rc;
+        // error words [0] sort, [1] link sort, [2] halo stack, [3] neighbour stack; [8] the neighbour search's
+        // coordinate bound (float, atomic max from 0)
         uint32_t* err = errWords.as<uint32_t>();
+        float* cmax   = reinterpret_cast<float*>(err + 8);
         CSG_CUDA_TRY(cudaMemsetAsync(err, 0, 64, s));
 
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_KEYS], s));
-        if ((rc = sfcKeys<T, K>(s, x, y, z, keys.as<K>(), n, box, cfg.sfc_kind, false))) return rc;
+        if ((rc = sfcKeysPacked<T, K>(s, x, y, z, h, keys.as<K>(), packed.as<PackedT<T>>(), n, box, cfg.sfc_kind)))
+            return rc;
 
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_SORT], s));
         bool inAlt = false;
@@ -167,8 +179,10 @@ struct Pipeline final : PipelineBase
         sortedOrder = inAlt ? orderAlt.as<uint32_t>() : order.as<uint32_t>();
 
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_GATHER], s));
-        GatherArgs<T, 4> ga{{x, y, z, h}, {xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>()}};
-        if ((rc = gatherN<T, 4>(s, sortedOrder, n, ga))) return rc;
+        if ((rc = gatherPacked<T>(s, sortedOrder, n, packed.as<PackedT<T>>(), xs.as<T>(), ys.as<T>(), zs.as<T>(),
+                                  hs.as<T>(), shadows ? shadowHi.as<float4>() : nullptr,
+                                  shadows ? shadowLo.as<float4>() : nullptr, cmax)))
+            return rc;
 
         // ---- cornerstone build: grow the capacity until the converged tree fits ----
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_BUILD], s));
@@ -242,10 +256,11 @@ struct Pipeline final : PipelineBase
         if (cfg.do_neighbors)
         {
             if ((rc = nb.ensure(std::max<size_t>(1, n * cfg.ngmax) * sizeof(uint32_t)))) return rc;
-            size_t nShadow = std::is_same_v<T, double> ? n : 0;
-            if ((rc = nbPrepWs.ensure(nbPrepBytes(nShadow, N)))) return rc;
-            if ((rc = nbPrepare<T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), nShadow, centers.as<T>(), sizes.as<T>(), N,
-                                   nbPrepWs.p, nbPrepWs.bytes, &prep)))
+            if ((rc = nbPrepWs.ensure(nbPrepBytes(0, N)))) return rc;
+            prep.phi  = shadows ? shadowHi.as<float4>() : nullptr;
+            prep.plo  = shadows ? shadowLo.as<float4>() : nullptr;
+            prep.cmax = cmax;
+            if ((rc = nbPrepareNodes<T>(s, centers.as<T>(), sizes.as<T>(), N, nbPrepWs.p, nbPrepWs.bytes, &prep)))
                 return rc;
         }
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_NEIGHBORS], s));

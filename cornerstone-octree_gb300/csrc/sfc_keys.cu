@@ -6,6 +6,8 @@
 #include "cs_common.cuh"
 #include "sfc_keys.cuh"
 
+#include <type_traits>
+
 namespace csg
 {
 
@@ -94,6 +96,138 @@ template int sfcKeys(cudaStream_t, const double*, const double*, const double*, 
 template int sfcKeys(cudaStream_t, const float*, const float*, const float*, uint64_t*, size_t, const cs_box&, int, bool);
 template int sfcKeys(cudaStream_t, const double*, const double*, const double*, uint64_t*, size_t, const cs_box&, int,
                      bool);
+
+// keys of the pipeline: as sfcKeysKernel, and x, y, z, h written as one record per particle, so that the gather after
+// the sort reads one sector per particle instead of four
+template<class T, class K, int Kind>
+__global__ void __launch_bounds__(256) sfcKeysPackKernel(const T* __restrict__ x, const T* __restrict__ y,
+                                                         const T* __restrict__ z, const T* __restrict__ h,
+                                                         K* __restrict__ keys, PackedT<T>* __restrict__ packed,
+                                                         size_t n, KeyParams<T, K> p)
+{
+    constexpr int V = 4;
+    size_t stride   = size_t(gridDim.x) * blockDim.x;
+    for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) * V; base < n; base += stride * V)
+    {
+        int m = int(n - base < V ? n - base : V);
+        T xs[V], ys[V], zs[V], hs[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+        {
+            if (v < m)
+            {
+                xs[v] = __ldcs(x + base + v);
+                ys[v] = __ldcs(y + base + v);
+                zs[v] = __ldcs(z + base + v);
+                hs[v] = __ldcs(h + base + v);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+        {
+            if (v < m)
+            {
+                keys[base + v]   = sfc3D<T, K>(xs[v], ys[v], zs[v], p, Kind);
+                PackedT<T> r;
+                r.x              = xs[v];
+                r.y              = ys[v];
+                r.z              = zs[v];
+                r.w              = hs[v];
+                packed[base + v] = r;
+            }
+        }
+    }
+}
+
+template<class T, class K>
+int sfcKeysPacked(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, K* keys, PackedT<T>* packed,
+                  size_t n, const cs_box& box, int kind)
+{
+    if (n == 0) return CS_OK;
+    auto bp        = makeBoxParams<T>(box);
+    auto kp        = makeKeyParams<T, K>(bp);
+    unsigned thr   = 256;
+    size_t blocksN = (n + 4 * thr - 1) / (4 * thr);
+    unsigned grid  = unsigned(blocksN < size_t(smCount()) * 16 ? blocksN : size_t(smCount()) * 16);
+    if (kind == CS_HILBERT)
+        sfcKeysPackKernel<T, K, CS_HILBERT><<<grid, thr, 0, s>>>(x, y, z, h, keys, packed, n, kp);
+    else
+        sfcKeysPackKernel<T, K, CS_MORTON><<<grid, thr, 0, s>>>(x, y, z, h, keys, packed, n, kp);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template int sfcKeysPacked(cudaStream_t, const float*, const float*, const float*, const float*, uint32_t*, float4*,
+                           size_t, const cs_box&, int);
+template int sfcKeysPacked(cudaStream_t, const double*, const double*, const double*, const double*, uint32_t*,
+                           double4_32a*, size_t, const cs_box&, int);
+template int sfcKeysPacked(cudaStream_t, const float*, const float*, const float*, const float*, uint64_t*, float4*,
+                           size_t, const cs_box&, int);
+template int sfcKeysPacked(cudaStream_t, const double*, const double*, const double*, const double*, uint64_t*,
+                           double4_32a*, size_t, const cs_box&, int);
+
+template<class T, bool Shadow>
+__global__ void __launch_bounds__(256) gatherPackedKernel(const uint32_t* __restrict__ perm, size_t n,
+                                                          const PackedT<T>* __restrict__ packed, T* __restrict__ xs,
+                                                          T* __restrict__ ys, T* __restrict__ zs, T* __restrict__ hs,
+                                                          float4* __restrict__ phi, float4* __restrict__ plo,
+                                                          float* cmax)
+{
+    size_t stride = size_t(gridDim.x) * blockDim.x;
+    float m       = 0.f;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        PackedT<T> r = packed[__ldcs(perm + i)];
+        __stcs(xs + i, r.x);
+        __stcs(ys + i, r.y);
+        __stcs(zs + i, r.z);
+        __stcs(hs + i, r.w);
+        if constexpr (Shadow)
+        {
+            // x = hi + lo to about 2^-48 relative; hi is x rounded to float
+            float h0 = __double2float_rn(r.x), h1 = __double2float_rn(r.y), h2 = __double2float_rn(r.z);
+            float l0 = __double2float_rn(__dsub_rn(r.x, double(h0)));
+            float l1 = __double2float_rn(__dsub_rn(r.y, double(h1)));
+            float l2 = __double2float_rn(__dsub_rn(r.z, double(h2)));
+            phi[i]   = make_float4(h0, h1, h2, 0.f);
+            plo[i]   = make_float4(l0, l1, l2, 0.f);
+            m        = fmaxf(m, fmaxf(fabsf(h0), fmaxf(fabsf(h1), fabsf(h2))));
+        }
+    }
+    if constexpr (Shadow)
+    {
+        for (int o = 16; o > 0; o >>= 1)
+            m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m));
+    }
+}
+
+template<class T>
+int gatherPacked(cudaStream_t s, const uint32_t* perm, size_t n, const PackedT<T>* packed, T* xs, T* ys, T* zs,
+                 T* hs, float4* phi, float4* plo, float* cmax)
+{
+    if (n == 0) return CS_OK;
+    unsigned thr  = 256;
+    size_t blocks = (n + thr - 1) / thr;
+    unsigned grid = unsigned(blocks < size_t(smCount()) * 32 ? blocks : size_t(smCount()) * 32);
+    if constexpr (std::is_same_v<T, double>)
+    {
+        if (phi)
+        {
+            gatherPackedKernel<T, true><<<grid, thr, 0, s>>>(perm, n, packed, xs, ys, zs, hs, phi, plo, cmax);
+            CSG_CHECK_LAUNCH();
+            return CS_OK;
+        }
+    }
+    gatherPackedKernel<T, false><<<grid, thr, 0, s>>>(perm, n, packed, xs, ys, zs, hs, phi, plo, cmax);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template int gatherPacked<float>(cudaStream_t, const uint32_t*, size_t, const float4*, float*, float*, float*, float*,
+                                 float4*, float4*, float*);
+template int gatherPacked<double>(cudaStream_t, const uint32_t*, size_t, const double4_32a*, double*, double*,
+                                  double*, double*, float4*, float4*, float*);
 
 // ---------------------------------------------------------------------------------------------------------------
 // gathers: out[i] = in[perm[i]]. The permutation is read once for up to four arrays.

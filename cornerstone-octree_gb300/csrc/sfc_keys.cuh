@@ -19,4 +19,31 @@ struct GatherArgs
 template<class T, int NA>
 int gatherN(cudaStream_t s, const uint32_t* perm, size_t n, GatherArgs<T, NA> a);
 
+//! x, y, z, h of one particle in one aligned record (one 32-byte sector for double)
+template<class T>
+struct Packed;
+template<>
+struct Packed<float>
+{
+    using type = float4;
+};
+template<>
+struct Packed<double>
+{
+    using type = double4_32a;
+};
+template<class T>
+using PackedT = typename Packed<T>::type;
+
+//! keys as sfcKeys (no removeKey entries), and the particles packed into one record each
+template<class T, class K>
+int sfcKeysPacked(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, K* keys, PackedT<T>* packed,
+                  size_t n, const cs_box& box, int kind);
+
+//! out[i] = packed[perm[i]] split into x, y, z, h; for T = double also the float shadows x = hi + lo of the
+//! neighbour search and the running bound cmax (an atomic max over |hi|, not reset here)
+template<class T>
+int gatherPacked(cudaStream_t s, const uint32_t* perm, size_t n, const PackedT<T>* packed, T* xs, T* ys, T* zs,
+                 T* hs, float4* phi, float4* plo, float* cmax);
+
 } // namespace csg
