@@ -2,16 +2,34 @@
 // and the collision traversal that flags every node outside the focus key range that overlaps a focus leaf's search
 // box (traversal/collisions.hpp:25-94, traversal/collisions_gpu.cu:23-77, traversal/boxoverlap.hpp:127-291).
 //
-// Search boxes: 8 lanes per leaf stride over its particles; min/max are exact, so any reduction order gives the
-// reference's bits. Collisions: one warp per 32 focus leaves, each lane deciding the containment test for its own
-// leaf, and one warp-wide traversal testing 32 nodes at a time for each leaf that needs it (findHalosWarpKernel); the
-// flagged set equals that of the reference's per-leaf singleTraversal (traversal/traversal.hpp:26-69), and every
-// floating-point expression is unfused and in the reference's order.
+// Search boxes: 8 lanes per leaf stride over its particles; min/max are exact (taken on order-preserving integer
+// images of the values), so any reduction order gives the reference's bits (up to the sign of a zero extremum that
+// ties with the other zero). Collisions: one warp per 32 focus leaves, each lane deciding the containment test for
+// its own leaf, and one warp-wide traversal testing 32 nodes at a time for each leaf that needs it
+// (findHalosWarpKernel); the flagged set equals that of the reference's per-leaf singleTraversal
+// (traversal/traversal.hpp:26-69), and every floating-point expression is unfused and in the reference's order.
 #include "cs_common.cuh"
 #include "halos.cuh"
 
+#include <type_traits>
+
 namespace csg
 {
+
+// order-preserving integer image of a float / double (sign-magnitude to two's complement): min and max of the images
+// are those of the values for all non-NaN inputs, with -0 ordered before +0, and they run on the integer pipes
+__device__ __forceinline__ long long ordKey(double v)
+{
+    long long b = __double_as_longlong(v);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double ordVal(long long k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL)); }
+__device__ __forceinline__ int ordKey(float v)
+{
+    int b = __float_as_int(v);
+    return b ^ ((b >> 31) & 0x7fffffff);
+}
+__device__ __forceinline__ float ordVal(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
 
 template<class T>
 __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z,
@@ -19,17 +37,18 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
                                   int lastLeaf, T scale, const int32_t* __restrict__ l2i,
                                   const T* __restrict__ nodeCenters, T* __restrict__ sc, T* __restrict__ ss)
 {
+    using I           = std::conditional_t<std::is_same_v<T, double>, long long, int>;
     constexpr int TPL = 8;
     int gtid          = blockIdx.x * blockDim.x + threadIdx.x;
     int leaf          = firstLeaf + gtid / TPL;
     int sub           = gtid % TPL;
     bool valid        = leaf < lastLeaf;
-    T mn[3], mx[3];
+    I mn[3], mx[3];
     if (valid)
     {
         const T* init = nodeCenters + 3 * size_t(l2i[leaf]);
         for (int k = 0; k < 3; ++k)
-            mn[k] = mx[k] = init[k];
+            mn[k] = mx[k] = ordKey(init[k]);
         uint32_t first = layout[leaf], last = layout[leaf + 1];
         for (uint32_t i = first + sub; i < last; i += TPL)
         {
@@ -38,8 +57,8 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
 #pragma unroll
             for (int k = 0; k < 3; ++k)
             {
-                T lo  = RN<T>::sub(p[k], r);
-                T hi  = RN<T>::add(p[k], r);
+                I lo  = ordKey(RN<T>::sub(p[k], r));
+                I hi  = ordKey(RN<T>::add(p[k], r));
                 mn[k] = lo < mn[k] ? lo : mn[k];
                 mx[k] = mx[k] < hi ? hi : mx[k];
             }
@@ -48,7 +67,7 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
     else
     {
         for (int k = 0; k < 3; ++k)
-            mn[k] = mx[k] = T(0);
+            mn[k] = mx[k] = 0;
     }
 #pragma unroll
     for (int o = 1; o < TPL; o <<= 1)
@@ -56,8 +75,8 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
 #pragma unroll
         for (int k = 0; k < 3; ++k)
         {
-            T a   = __shfl_down_sync(0xffffffffu, mn[k], o, TPL);
-            T b   = __shfl_down_sync(0xffffffffu, mx[k], o, TPL);
+            I a   = __shfl_down_sync(0xffffffffu, mn[k], o, TPL);
+            I b   = __shfl_down_sync(0xffffffffu, mx[k], o, TPL);
             mn[k] = a < mn[k] ? a : mn[k];
             mx[k] = mx[k] < b ? b : mx[k];
         }
@@ -66,8 +85,9 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
     {
         for (int k = 0; k < 3; ++k)
         {
-            sc[3 * size_t(leaf) + k] = RN<T>::mul(RN<T>::add(mx[k], mn[k]), T(0.5));
-            ss[3 * size_t(leaf) + k] = RN<T>::mul(RN<T>::sub(mx[k], mn[k]), T(0.5));
+            T lo = ordVal(mn[k]), hi = ordVal(mx[k]);
+            sc[3 * size_t(leaf) + k] = RN<T>::mul(RN<T>::add(hi, lo), T(0.5));
+            ss[3 * size_t(leaf) + k] = RN<T>::mul(RN<T>::sub(hi, lo), T(0.5));
         }
     }
 }
@@ -134,13 +154,36 @@ __device__ bool boxContainedIn(K codeStart, K codeEnd, const T* center, const T*
 constexpr int HALO_WARPS = 4;
 constexpr int HALO_STACK = 1024;
 
-template<class K, class T>
+// The reference's FP64 overlap test |tc - nc| - ns - ts < 0 on every axis (no periodic axis), out of line so that its
+// FP64 arithmetic stays off the float pre-filter's path.
+__device__ __noinline__ bool haloOverlapF64(double tc0, double tc1, double tc2, double ts0, double ts1, double ts2,
+                                            const double* __restrict__ nc, const double* __restrict__ ns, int idx)
+{
+    double tc[3] = {tc0, tc1, tc2}, ts[3] = {ts0, ts1, ts2};
+    bool ov      = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        double d = __dsub_rn(fabs(__dsub_rn(tc[k], nc[3 * size_t(idx) + k])), ns[3 * size_t(idx) + k]);
+        ov       = ov && (__dsub_rn(d, ts[k]) < 0.0);
+    }
+    return ov;
+}
+
+// FloatFilter (T = double, no periodic axis): each node test is first evaluated in FP32 on the float node boxes
+// (centre rounded to nearest, half size rounded to nearest) and the float-rounded search box. With S = |tc| + |nc| +
+// ns + ts and u = 2^-24 the FP32 value of |tc - nc| - ns - ts is within 4.01 u S of the exact one, and the FP64 value
+// within 4 * 2^-53 S, so D_f < -8 u S proves the reference's test passes on that axis and D_f >= 8 u S proves it
+// fails; anything in between is decided by haloOverlapF64.
+template<class K, class T, bool FloatFilter>
 __global__ void __launch_bounds__(32 * HALO_WARPS)
     findHalosWarpKernel(const K* __restrict__ prefixes, const int32_t* __restrict__ childOffsets,
                         const T* __restrict__ nc, const T* __restrict__ ns, const K* __restrict__ leaves,
                         const T* __restrict__ sc, const T* __restrict__ ss, BoxParams<T> b, KeyParams<T, K> kp,
-                        int firstNode, int lastNode, uint8_t* flags, uint32_t* errWord)
+                        int firstNode, int lastNode, uint8_t* flags, uint32_t* errWord,
+                        const float4* __restrict__ nchi, const float4* __restrict__ nsz)
 {
+    constexpr float U8 = 8.f * 5.9604644775390625e-8f;
     __shared__ int sStack[HALO_WARPS][HALO_STACK];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long leaf0 = firstNode + (long long)(blockIdx.x * HALO_WARPS + warp) * 32;
@@ -175,11 +218,14 @@ __global__ void __launch_bounds__(32 * HALO_WARPS)
         const int src = __ffs(todo) - 1;
         todo &= todo - 1;
         T tc[3], ts[3];
+        float tcf[3], tsf[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k)
         {
-            tc[k] = __shfl_sync(0xffffffffu, myc[k], src);
-            ts[k] = __shfl_sync(0xffffffffu, mys[k], src);
+            tc[k]  = __shfl_sync(0xffffffffu, myc[k], src);
+            ts[k]  = __shfl_sync(0xffffffffu, mys[k], src);
+            tcf[k] = float(tc[k]);
+            tsf[k] = float(ts[k]);
         }
 
         auto overlaps = [&](int idx) -> bool {
@@ -190,14 +236,33 @@ __global__ void __launch_bounds__(32 * HALO_WARPS)
             bool inside   = !(nk1 < lowest || nk2 > highest);
             if (inside) return false;
             bool ov = true;
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
+            if constexpr (FloatFilter)
             {
-                T d = RN<T>::sub(tc[k], nc[3 * size_t(idx) + k]);
-                d   = RN<T>::abs_(pbcFold<T>(d, b.pbc[k], b.len[k], b.ilen[k]));
-                d   = RN<T>::sub(d, ns[3 * size_t(idx) + k]);
-                d   = RN<T>::sub(d, ts[k]);
-                ov  = ov && (d < T(0));
+                float4 c4    = nchi[idx], s4 = nsz[idx];
+                float cc[3]  = {c4.x, c4.y, c4.z}, sz[3] = {s4.x, s4.y, s4.z};
+                bool sureIn  = true, sureOut = false;
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                {
+                    float d = __fsub_rn(__fsub_rn(fabsf(__fsub_rn(tcf[k], cc[k])), sz[k]), tsf[k]);
+                    float S = __fadd_ru(__fadd_ru(__fadd_ru(fabsf(tcf[k]), fabsf(cc[k])), sz[k]), tsf[k]);
+                    float E = __fmul_ru(U8, S);
+                    sureIn  = sureIn && d < -E;
+                    sureOut = sureOut || d >= E;
+                }
+                ov = !sureOut && (sureIn || haloOverlapF64(tc[0], tc[1], tc[2], ts[0], ts[1], ts[2], nc, ns, idx));
+            }
+            else
+            {
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                {
+                    T d = RN<T>::sub(tc[k], nc[3 * size_t(idx) + k]);
+                    d   = RN<T>::abs_(pbcFold<T>(d, b.pbc[k], b.len[k], b.ilen[k]));
+                    d   = RN<T>::sub(d, ns[3 * size_t(idx) + k]);
+                    d   = RN<T>::sub(d, ts[k]);
+                    ov  = ov && (d < T(0));
+                }
             }
             if (ov) flags[idx] = 1;
             return ov;
@@ -247,14 +312,25 @@ __global__ void __launch_bounds__(32 * HALO_WARPS)
 template<class K, class T>
 int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, const int32_t* parents, const T* nc,
               const T* ns, const K* leaves, const T* sc, const T* ss, const cs_box& box, int first, int last,
-              uint8_t* flags, uint32_t* errWord)
+              uint8_t* flags, uint32_t* errWord, const float4* nchi, const float4* nsz)
 {
     if (last <= first) return CS_OK;
     auto bp = makeBoxParams<T>(box);
     auto kp = makeKeyParams<T, K>(bp);
     unsigned blocks = iceil(size_t(last - first), 32 * HALO_WARPS);
-    findHalosWarpKernel<K, T><<<blocks, 32 * HALO_WARPS, 0, s>>>(prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp,
-                                                                 first, last, flags, errWord);
+    bool anyPbc     = bp.pbc[0] || bp.pbc[1] || bp.pbc[2];
+    if constexpr (std::is_same_v<T, double>)
+    {
+        if (nchi && nsz && !anyPbc)
+        {
+            findHalosWarpKernel<K, T, true><<<blocks, 32 * HALO_WARPS, 0, s>>>(
+                prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp, first, last, flags, errWord, nchi, nsz);
+            CSG_CHECK_LAUNCH();
+            return CS_OK;
+        }
+    }
+    findHalosWarpKernel<K, T, false><<<blocks, 32 * HALO_WARPS, 0, s>>>(
+        prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp, first, last, flags, errWord, nullptr, nullptr);
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }
@@ -265,13 +341,13 @@ template int searchBoxes<double>(cudaStream_t, const double*, const double*, con
                                  const uint32_t*, int, int, double, const int32_t*, const double*, double*, double*);
 template int findHalos<uint32_t, float>(cudaStream_t, const uint32_t*, const int32_t*, const int32_t*, const float*,
                                         const float*, const uint32_t*, const float*, const float*, const cs_box&, int,
-                                        int, uint8_t*, uint32_t*);
+                                        int, uint8_t*, uint32_t*, const float4*, const float4*);
 template int findHalos<uint64_t, float>(cudaStream_t, const uint64_t*, const int32_t*, const int32_t*, const float*,
                                         const float*, const uint64_t*, const float*, const float*, const cs_box&, int,
-                                        int, uint8_t*, uint32_t*);
+                                        int, uint8_t*, uint32_t*, const float4*, const float4*);
 template int findHalos<uint64_t, double>(cudaStream_t, const uint64_t*, const int32_t*, const int32_t*, const double*,
                                          const double*, const uint64_t*, const double*, const double*, const cs_box&,
-                                         int, int, uint8_t*, uint32_t*);
+                                         int, int, uint8_t*, uint32_t*, const float4*, const float4*);
 
 } // namespace csg
 
@@ -302,7 +378,7 @@ extern "C" int cs_search_boxes_f64(cs_stream_t stream, const double* x, const do
             return CS_ERR_INVALID;                                                                                     \
         }                                                                                                              \
         return findHalos<K, T>(cudaStream_t(stream), prefixes, childOffsets, parents, nc, ns, leaves, sc, ss, *box,    \
-                               first, last, flags, nullptr);                                                           \
+                               first, last, flags, nullptr, nullptr, nullptr);                                         \
     }
 CS_HALOS_ENTRY(u32, uint32_t, f32, float)
 CS_HALOS_ENTRY(u64, uint64_t, f32, float)

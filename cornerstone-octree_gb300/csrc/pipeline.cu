@@ -55,8 +55,8 @@ enum Stage
     ST_BUILD,
     ST_LINK,
     ST_GEO,
-    ST_HALOS,
     ST_NBPREP,
+    ST_HALOS,
     ST_NEIGHBORS,
     ST_COUNT
 };
@@ -227,6 +227,23 @@ struct Pipeline final : PipelineBase
         if ((rc = sizes.ensure(3 * size_t(N) * sizeof(T)))) return rc;
         if ((rc = geoCenters<K, T>(s, prefixes.as<K>(), N, centers.as<T>(), sizes.as<T>(), box, cfg.sfc_kind))) return rc;
 
+        // ---- float node boxes for the halo pre-filter and the neighbour search ----
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_NBPREP], s));
+        if ((rc = nc.ensure(n * sizeof(uint32_t)))) return rc;
+        NbPrep prep{};
+        const bool nodeShadows = cfg.do_neighbors || (F64 && cfg.do_halos);
+        if (nodeShadows)
+        {
+            if ((rc = nbPrepWs.ensure(nbPrepBytes(0, N)))) return rc;
+            prep.phi  = shadows ? shadowHi.as<float4>() : nullptr;
+            prep.plo  = shadows ? shadowLo.as<float4>() : nullptr;
+            prep.cmax = cmax;
+            if ((rc = nbPrepareNodes<T>(s, centers.as<T>(), sizes.as<T>(), N, nbPrepWs.p, nbPrepWs.bytes, &prep)))
+                return rc;
+        }
+        if (cfg.do_neighbors)
+            if ((rc = nb.ensure(std::max<size_t>(1, n * cfg.ngmax) * sizeof(uint32_t)))) return rc;
+
         // ---- halos for the focus leaves ----
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_HALOS], s));
         if ((rc = flags.ensure(size_t(N)))) return rc;
@@ -244,25 +261,12 @@ struct Pipeline final : PipelineBase
             {
                 if ((rc = findHalos<K, T>(s, prefixes.as<K>(), childOffsets.as<int32_t>(), parents.as<int32_t>(),
                                           centers.as<T>(), sizes.as<T>(), leaves.as<K>(), sc.as<T>(), ss.as<T>(), box,
-                                          br.focusFirst, br.focusLast, flags.as<uint8_t>(), err + 2)))
+                                          br.focusFirst, br.focusLast, flags.as<uint8_t>(), err + 2, prep.chi,
+                                          prep.sz)))
                     return rc;
             }
         }
 
-        // ---- neighbours ----
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_NBPREP], s));
-        if ((rc = nc.ensure(n * sizeof(uint32_t)))) return rc;
-        NbPrep prep{};
-        if (cfg.do_neighbors)
-        {
-            if ((rc = nb.ensure(std::max<size_t>(1, n * cfg.ngmax) * sizeof(uint32_t)))) return rc;
-            if ((rc = nbPrepWs.ensure(nbPrepBytes(0, N)))) return rc;
-            prep.phi  = shadows ? shadowHi.as<float4>() : nullptr;
-            prep.plo  = shadows ? shadowLo.as<float4>() : nullptr;
-            prep.cmax = cmax;
-            if ((rc = nbPrepareNodes<T>(s, centers.as<T>(), sizes.as<T>(), N, nbPrepWs.p, nbPrepWs.bytes, &prep)))
-                return rc;
-        }
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_NEIGHBORS], s));
         if (cfg.do_neighbors)
         {
@@ -445,8 +449,8 @@ extern "C" int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out)
 
 extern "C" size_t cs_pipeline_device_bytes(cs_pipeline p) { return p ? p->impl->deviceBytes() : 0; }
 
-/* per-stage device time of the last run in ms (keys, sort, gather, build, link, geometry, halos, neighbour prep,
- * neighbours); synchronises on the last run's events */
+/* per-stage device time of the last run in ms (keys, sort, gather, build, link, geometry, node prep, halos,
+ * neighbours) */
 extern "C" int cs_pipeline_stage_times(cs_pipeline p, float* ms, int count)
 {
     if (!p || !ms)

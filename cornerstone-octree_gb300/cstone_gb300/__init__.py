@@ -311,7 +311,7 @@ class PipelineOutputs(C.Structure):
 lib.cs_pipeline_device_bytes.restype = C.c_size_t
 lib.cs_pipeline_device_bytes.argtypes = [C.c_void_p]
 
-STAGES = ("keys", "sort", "gather", "build", "link", "geometry", "halos", "nbprep", "neighbors")
+STAGES = ("keys", "sort", "gather", "build", "link", "geometry", "nbprep", "halos", "neighbors")
 
 
 class Pipeline:

@@ -330,8 +330,9 @@ int cs_pipeline_run_host(cs_pipeline p, cs_stream_t stream, const void* x, const
 int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out);
 /* bytes of device memory the pipeline holds */
 size_t cs_pipeline_device_bytes(cs_pipeline p);
-/* device time in ms of each stage of the last run: keys, sort, gather, build, link, geometry, halos, neighbour
- * preparation, neighbours (count <= 9 values); waits for the last run to finish */
+/* device time in ms of each stage of the last run: keys, sort, gather, build, link, geometry, float node boxes
+ * (node preparation of the halo and neighbour searches), halos, neighbours (count <= 9 values); waits for the last
+ * run to finish */
 int cs_pipeline_stage_times(cs_pipeline p, float* ms, int count);
 
 #ifdef __cplusplus

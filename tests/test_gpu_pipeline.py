@@ -35,8 +35,8 @@ def _check_against_oracle(cs, O, x, y, z, h, lo, hi, bnd, bucket, ngmax, focus, 
     return res
 
 
-def test_pipeline_uniform_c1_like(cs, O):
-    """BASELINE config 1 shape at reduced size: U[-1,1]^3, constant h, Hilbert64, bucket 64, ngmax 150"""
+def test_pipeline_uniform_cube(cs, O):
+    """the uniform-cube workload at reduced size: U[-1,1]^3, constant h, Hilbert64, bucket 64, ngmax 150"""
     n = 1 << 17
     x, y, z = (O.philox_uniform(1, s, n, -1.0, 1.0) for s in range(3))
     h = np.full(n, 0.028 * (2 ** 20 / n) ** (1 / 3))  # ~93 neighbours, as h = 0.028 at N = 2^20
@@ -44,8 +44,8 @@ def test_pipeline_uniform_c1_like(cs, O):
     assert res.num_leaves > 0
 
 
-def test_pipeline_plummer_c2_like(cs, O):
-    """BASELINE config 2 shape at reduced size: Plummer, tight box, adaptive h (~100 neighbours), halos in the first
+def test_pipeline_plummer(cs, O):
+    """the 16M Plummer workload at reduced size: Plummer, tight box, adaptive h (~100 neighbours), halos in the first
     quarter of the key space, ngmax 200"""
     n = 1 << 17
     x, y, z = O.plummer(5, n)
