@@ -170,8 +170,8 @@ __device__ __noinline__ bool haloOverlapF64(double tc0, double tc1, double tc2, 
     return ov;
 }
 
-// FloatFilter (T = double, no periodic axis): each node test is first evaluated in FP32 on the float node boxes
-// (centre rounded to nearest, half size rounded to nearest) and the float-rounded search box. With S = |tc| + |nc| +
+// FloatFilter (T = double, no periodic axis): each node test is first evaluated in FP32 on the float node records
+// of the neighbour search (centre rounded to nearest, half size rounded to nearest) and the float-rounded search box. With S = |tc| + |nc| +
 // ns + ts and u = 2^-24 the FP32 value of |tc - nc| - ns - ts is within 4.01 u S of the exact one, and the FP64 value
 // within 4 * 2^-53 S, so D_f < -8 u S proves the reference's test passes on that axis and D_f >= 8 u S proves it
 // fails; anything in between is decided by haloOverlapF64.
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(32 * HALO_WARPS)
                         const T* __restrict__ nc, const T* __restrict__ ns, const K* __restrict__ leaves,
                         const T* __restrict__ sc, const T* __restrict__ ss, BoxParams<T> b, KeyParams<T, K> kp,
                         int firstNode, int lastNode, uint8_t* flags, uint32_t* errWord,
-                        const float4* __restrict__ nchi, const float4* __restrict__ nsz)
+                        const float4* __restrict__ nrec)
 {
     constexpr float U8 = 8.f * 5.9604644775390625e-8f;
     __shared__ int sStack[HALO_WARPS][HALO_STACK];
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(32 * HALO_WARPS)
             bool ov = true;
             if constexpr (FloatFilter)
             {
-                float4 c4    = nchi[idx], s4 = nsz[idx];
+                float4 c4    = nrec[3 * size_t(idx)], s4 = nrec[3 * size_t(idx) + 2];
                 float cc[3]  = {c4.x, c4.y, c4.z}, sz[3] = {s4.x, s4.y, s4.z};
                 bool sureIn  = true, sureOut = false;
 #pragma unroll
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(32 * HALO_WARPS)
 template<class K, class T>
 int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, const int32_t* parents, const T* nc,
               const T* ns, const K* leaves, const T* sc, const T* ss, const cs_box& box, int first, int last,
-              uint8_t* flags, uint32_t* errWord, const float4* nchi, const float4* nsz)
+              uint8_t* flags, uint32_t* errWord, const float4* nrec)
 {
     if (last <= first) return CS_OK;
     auto bp = makeBoxParams<T>(box);
@@ -321,16 +321,16 @@ int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, co
     bool anyPbc     = bp.pbc[0] || bp.pbc[1] || bp.pbc[2];
     if constexpr (std::is_same_v<T, double>)
     {
-        if (nchi && nsz && !anyPbc)
+        if (nrec && !anyPbc)
         {
             findHalosWarpKernel<K, T, true><<<blocks, 32 * HALO_WARPS, 0, s>>>(
-                prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp, first, last, flags, errWord, nchi, nsz);
+                prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp, first, last, flags, errWord, nrec);
             CSG_CHECK_LAUNCH();
             return CS_OK;
         }
     }
     findHalosWarpKernel<K, T, false><<<blocks, 32 * HALO_WARPS, 0, s>>>(
-        prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp, first, last, flags, errWord, nullptr, nullptr);
+        prefixes, childOffsets, nc, ns, leaves, sc, ss, bp, kp, first, last, flags, errWord, nullptr);
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }
@@ -341,13 +341,13 @@ template int searchBoxes<double>(cudaStream_t, const double*, const double*, con
                                  const uint32_t*, int, int, double, const int32_t*, const double*, double*, double*);
 template int findHalos<uint32_t, float>(cudaStream_t, const uint32_t*, const int32_t*, const int32_t*, const float*,
                                         const float*, const uint32_t*, const float*, const float*, const cs_box&, int,
-                                        int, uint8_t*, uint32_t*, const float4*, const float4*);
+                                        int, uint8_t*, uint32_t*, const float4*);
 template int findHalos<uint64_t, float>(cudaStream_t, const uint64_t*, const int32_t*, const int32_t*, const float*,
                                         const float*, const uint64_t*, const float*, const float*, const cs_box&, int,
-                                        int, uint8_t*, uint32_t*, const float4*, const float4*);
+                                        int, uint8_t*, uint32_t*, const float4*);
 template int findHalos<uint64_t, double>(cudaStream_t, const uint64_t*, const int32_t*, const int32_t*, const double*,
                                          const double*, const uint64_t*, const double*, const double*, const cs_box&,
-                                         int, int, uint8_t*, uint32_t*, const float4*, const float4*);
+                                         int, int, uint8_t*, uint32_t*, const float4*);
 
 } // namespace csg
 
@@ -378,7 +378,7 @@ extern "C" int cs_search_boxes_f64(cs_stream_t stream, const double* x, const do
             return CS_ERR_INVALID;                                                                                     \
         }                                                                                                              \
         return findHalos<K, T>(cudaStream_t(stream), prefixes, childOffsets, parents, nc, ns, leaves, sc, ss, *box,    \
-                               first, last, flags, nullptr, nullptr, nullptr);                                         \
+                               first, last, flags, nullptr, nullptr);                                                  \
     }
 CS_HALOS_ENTRY(u32, uint32_t, f32, float)
 CS_HALOS_ENTRY(u64, uint64_t, f32, float)

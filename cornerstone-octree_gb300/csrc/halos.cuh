@@ -9,11 +9,12 @@ template<class T>
 int searchBoxes(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, const uint32_t* layout, int first,
                 int last, T scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss);
 
-//! nchi / nsz (may be null): float node centres and half sizes rounded to nearest (the neighbour search's node
-//! shadows); with T = double and no periodic axis they enable the float pre-filter of the node test
+//! nrec (may be null): the neighbour search's float node records (NbPrep::nrec: centre and half size rounded to
+//! nearest at [3i] and [3i + 2]); with T = double and no periodic axis they enable the float pre-filter of the node
+//! test
 template<class K, class T>
 int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, const int32_t* parents, const T* nc,
               const T* ns, const K* leaves, const T* sc, const T* ss, const cs_box& box, int first, int last,
-              uint8_t* flags, uint32_t* errWord, const float4* nchi, const float4* nsz);
+              uint8_t* flags, uint32_t* errWord, const float4* nrec);
 
 } // namespace csg

@@ -222,7 +222,8 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
                 if (pbc) { ok = cellExactF64(xi, yi, zi, true, cellR2, c, s, pa); }
                 else
                 {
-                    float4 ch = prep.chi[node], cl = prep.clo[node], sz = prep.sz[node];
+                    float4 ch = prep.nrec[3 * size_t(node)], cl = prep.nrec[3 * size_t(node) + 1],
+                           sz = prep.nrec[3 * size_t(node) + 2];
                     float D[3] = {__fsub_rn(__fadd_rn(__fsub_rn(ch.x, Px), cl.x), bx),
                                   __fsub_rn(__fadd_rn(__fsub_rn(ch.y, Py), cl.y), by),
                                   __fsub_rn(__fadd_rn(__fsub_rn(ch.z, Pz), cl.z), bz)};
@@ -556,23 +557,27 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     for (int q = 0; q < S; ++q)
         tmask |= 1u << (t + q * G);
     unsigned long long stLeaves = 0, stCand = 0, stNodes = 0, stPair = 0, stExact = 0;
+    // cost model of the candidate batches (lane 0): steps of the lane-per-target loop, needing lanes, the cheaper of
+    // 11 instructions per step and 20 per needing lane, batches, cycles spent in the batches
+    unsigned long long stSteps = 0, stNeed = 0, stMinCost = 0, stBatches = 0, stCandCyc = 0;
 
     // node box in the warp frame: center cc = (chi - P) + clo, half size sz
+    auto frameOf = [&](float4 ch, float4 cl, float4 s4, float cc[3], float sz[3]) {
+        cc[0] = __fadd_rn(__fsub_rn(ch.x, P[0]), cl.x);
+        cc[1] = __fadd_rn(__fsub_rn(ch.y, P[1]), cl.y);
+        cc[2] = __fadd_rn(__fsub_rn(ch.z, P[2]), cl.z);
+        sz[0] = s4.x;
+        sz[1] = s4.y;
+        sz[2] = s4.z;
+    };
     auto nodeFrame = [&](int node, float cc[3], float sz[3]) {
-        float4 ch = prep.chi[node], cl = prep.clo[node], s4 = prep.sz[node];
-        cc[0]     = __fadd_rn(__fsub_rn(ch.x, P[0]), cl.x);
-        cc[1]     = __fadd_rn(__fsub_rn(ch.y, P[1]), cl.y);
-        cc[2]     = __fadd_rn(__fsub_rn(ch.z, P[2]), cl.z);
-        sz[0]     = s4.x;
-        sz[1]     = s4.y;
-        sz[2]     = s4.z;
+        const float4* r = prep.nrec + 3 * size_t(node);
+        frameOf(r[0], r[1], r[2], cc, sz);
     };
 
     // conservative per-lane test: can a particle of this node lie within the search radius of x_i? (a lower
     // bound of |x_i - node box|, the box widened by the particle slack delta)
-    auto mayHit = [&](int node) -> bool {
-        float cc[3], sz[3];
-        nodeFrame(node, cc, sz);
+    auto mayHitBox = [&](const float cc[3], const float sz[3]) -> bool {
         float n2 = 0.f;
 #pragma unroll
         for (int k = 0; k < 3; ++k)
@@ -583,6 +588,11 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             n2      = __fmaf_rd(d, d, n2);
         }
         return n2 < r2hi;
+    };
+    auto mayHit = [&](int node) -> bool {
+        float cc[3], sz[3];
+        nodeFrame(node, cc, sz);
+        return mayHitBox(cc, sz);
     };
 
     // decision for one candidate of the lane's target that survived the first distance filter
@@ -648,13 +658,33 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         }
     };
 
-    auto processLeaf = [&](int node, unsigned pmask) {
-        bool need     = ((pmask >> lane) & 1u) && mayHit(node);
+    // candidate j in the warp frame; beyond the leaf a point at infinity, which fails every distance test
+    auto stage = [&](uint32_t j, uint32_t last) -> float4 {
+        float4 q = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+        if (j < last)
+        {
+            if constexpr (F64)
+            {
+                float4 ph = prep.phi[j], pl = prep.plo[j];
+                q.x       = __fadd_rn(__fsub_rn(ph.x, P[0]), pl.x);
+                q.y       = __fadd_rn(__fsub_rn(ph.y, P[1]), pl.y);
+                q.z       = __fadd_rn(__fsub_rn(ph.z, P[2]), pl.z);
+            }
+            else { q = make_float4(a.x[j], a.y[j], a.z[j], 0.f); }
+        }
+        return q;
+    };
+
+    // a leaf with its record r0..r2: the lanes whose sphere may reach it test its particles, 32 per batch
+    auto processLeaf = [&](int node, unsigned pmask, float4 r0, float4 r1, float4 r2) {
+        const uint32_t first = __float_as_uint(r1.w), last = __float_as_uint(r2.w);
+        // the first batch is loaded before the lanes' box test, so that the two latencies overlap
+        float4 q0 = stage(first + lane, last);
+        float cc[3], sz[3];
+        frameOf(r0, r1, r2, cc, sz);
+        bool need     = ((pmask >> lane) & 1u) && mayHitBox(cc, sz);
         unsigned mask = __ballot_sync(0xffffffffu, need);
         if (mask == 0) return;
-        int leafIdx    = a.i2l[node];
-        uint32_t first = a.layout[leafIdx];
-        uint32_t last  = a.layout[leafIdx + 1];
         if constexpr (Stats)
         {
             stLeaves++;
@@ -662,24 +692,22 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         }
         for (uint32_t base = first; base < last; base += 32)
         {
-            uint32_t j = base + lane;
-            // beyond the leaf: a point at infinity, which fails every distance test
-            float4 q   = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
-            if (j < last)
-            {
-                if constexpr (F64)
-                {
-                    float4 ph = prep.phi[j], pl = prep.plo[j];
-                    q.x = __fadd_rn(__fsub_rn(ph.x, P[0]), pl.x);
-                    q.y = __fadd_rn(__fsub_rn(ph.y, P[1]), pl.y);
-                    q.z = __fadd_rn(__fsub_rn(ph.z, P[2]), pl.z);
-                }
-                else { q = make_float4(a.x[j], a.y[j], a.z[j], 0.f); }
-            }
+            float4 q = base == first ? q0 : stage(base + lane, last);
             __syncwarp();
             sCand[warp][lane] = q;
             __syncwarp();
             int cnt = int(min(32u, last - base));
+            long long tc0 = 0;
+            if constexpr (Stats)
+            {
+                unsigned steps = (unsigned(cnt) + 7u) & ~7u;
+                unsigned m     = __popc(mask);
+                stSteps += steps;
+                stNeed += m;
+                stMinCost += min(11u * steps, 20u * m);
+                stBatches++;
+                tc0 = clock64();
+            }
             if constexpr (S == 1)
             {
                 if (need)
@@ -748,6 +776,11 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     nc += __popc(mine);
                 }
             }
+            if constexpr (Stats)
+            {
+                __syncwarp();
+                stCandCyc += (unsigned long long)(clock64() - tc0);
+            }
         }
     };
 
@@ -779,26 +812,24 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     int* stack          = sStack[warp];
     unsigned* maskStack = sMaskStack[warp];
     int top             = 0;
-    if (a.childOffsets[0] == 0) { processLeaf(0, activeMask); }
-    else
+    if (lane == 0)
     {
-        if (lane == 0)
-        {
-            stack[0]     = 0;
-            maskStack[0] = activeMask;
-        }
-        top = 1;
+        stack[0]     = 0;
+        maskStack[0] = activeMask;
     }
+    top = 1;
     __syncwarp();
     while (top > 0)
     {
         int node       = stack[top - 1];
         unsigned pmask = maskStack[top - 1];
         --top;
-        int c0 = a.childOffsets[node];
+        const float4* rec = prep.nrec + 3 * size_t(node);
+        float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
+        int c0    = __float_as_int(r0.w);
         if (c0 == 0)
         {
-            processLeaf(node, pmask);
+            processLeaf(node, pmask, r0, r1, r2);
             continue;
         }
         if constexpr (Stats) stNodes++;
@@ -873,6 +904,12 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         }
         if (lane == 0)
         {
+            atomicAdd(a.stats + 20, stSteps);
+            atomicAdd(a.stats + 21, stNeed);
+            atomicAdd(a.stats + 22, stMinCost);
+            atomicAdd(a.stats + 23, stBatches);
+            atomicAdd(a.stats + 24, stCandCyc);
+            atomicAdd(a.stats + 25, (unsigned long long)(clock64() - t0));
             atomicAdd(a.stats + 7, 1ull);
             // slowest warp: [8] cycles, [9] its expansions, [10] leaves, [11] candidates, [12] loose flag,
             // [13] its first target; [14] number of loose warps
@@ -919,9 +956,26 @@ __global__ void prepParticlesKernel(const double* __restrict__ x, const double* 
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m));
 }
 
-__global__ void prepNodesKernel(const double* __restrict__ centers, const double* __restrict__ sizes, int N,
-                                float4* __restrict__ chi, float4* __restrict__ clo, float4* __restrict__ sz,
-                                float* cmax)
+// the child offset and particle range of node i, stored in the w components of its record
+__device__ __forceinline__ void nodeLinks(int i, const int32_t* childOffsets, const int32_t* i2l, const uint32_t* layout,
+                                          float& w0, float& w1, float& w2)
+{
+    int c0     = childOffsets[i];
+    uint32_t f = 0, e = 0;
+    if (c0 == 0)
+    {
+        int leaf = i2l[i];
+        f        = layout[leaf];
+        e        = layout[leaf + 1];
+    }
+    w0 = __int_as_float(c0);
+    w1 = __uint_as_float(f);
+    w2 = __uint_as_float(e);
+}
+
+__global__ void prepNodesKernel(const double* __restrict__ centers, const double* __restrict__ sizes,
+                                const int32_t* __restrict__ childOffsets, const int32_t* __restrict__ i2l,
+                                const uint32_t* __restrict__ layout, int N, float4* __restrict__ nrec, float* cmax)
 {
     float m = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
@@ -936,18 +990,20 @@ __global__ void prepNodesKernel(const double* __restrict__ centers, const double
             s[k]     = __double2float_rn(sizes[3 * size_t(i) + k]);
             m        = fmaxf(m, fabsf(h[k]) + s[k]);
         }
-        chi[i] = make_float4(h[0], h[1], h[2], 0.f);
-        clo[i] = make_float4(l[0], l[1], l[2], 0.f);
-        sz[i]  = make_float4(s[0], s[1], s[2], 0.f);
+        float w0, w1, w2;
+        nodeLinks(i, childOffsets, i2l, layout, w0, w1, w2);
+        nrec[3 * size_t(i)]     = make_float4(h[0], h[1], h[2], w0);
+        nrec[3 * size_t(i) + 1] = make_float4(l[0], l[1], l[2], w1);
+        nrec[3 * size_t(i) + 2] = make_float4(s[0], s[1], s[2], w2);
     }
     m = warpMaxF(m);
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m));
 }
 
-// float node boxes of a float tree (centre, zero low part, size) and the magnitude bound C
-__global__ void prepNodesF32Kernel(const float* __restrict__ centers, const float* __restrict__ sizes, int N,
-                                   float4* __restrict__ chi, float4* __restrict__ clo, float4* __restrict__ sz,
-                                   float* cmax)
+// records of a float tree (centre, zero low part, size) and the magnitude bound C
+__global__ void prepNodesF32Kernel(const float* __restrict__ centers, const float* __restrict__ sizes,
+                                   const int32_t* __restrict__ childOffsets, const int32_t* __restrict__ i2l,
+                                   const uint32_t* __restrict__ layout, int N, float4* __restrict__ nrec, float* cmax)
 {
     float m = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
@@ -960,9 +1016,11 @@ __global__ void prepNodesF32Kernel(const float* __restrict__ centers, const floa
             s[k] = sizes[3 * size_t(i) + k];
             m    = fmaxf(m, fabsf(c[k]) + s[k]);
         }
-        chi[i] = make_float4(c[0], c[1], c[2], 0.f);
-        clo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        sz[i]  = make_float4(s[0], s[1], s[2], 0.f);
+        float w0, w1, w2;
+        nodeLinks(i, childOffsets, i2l, layout, w0, w1, w2);
+        nrec[3 * size_t(i)]     = make_float4(c[0], c[1], c[2], w0);
+        nrec[3 * size_t(i) + 1] = make_float4(0.f, 0.f, 0.f, w1);
+        nrec[3 * size_t(i) + 2] = make_float4(s[0], s[1], s[2], w2);
     }
     m = warpMaxF(m);
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m));
@@ -973,25 +1031,22 @@ size_t nbPrepBytes(size_t n, int numNodes)
     Arena ar;
     ar.take<float4>(n);
     ar.take<float4>(n);
-    ar.take<float4>(size_t(numNodes));
-    ar.take<float4>(size_t(numNodes));
-    ar.take<float4>(size_t(numNodes));
+    ar.take<float4>(3 * size_t(numNodes));
     ar.take<float>(1);
     return ar.size + 256;
 }
 
 template<class T>
 int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, const T* centers, const T* sizes,
-              int numNodes, void* ws, size_t wsBytes, NbPrep* prep)
+              const int32_t* childOffsets, const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws,
+              size_t wsBytes, NbPrep* prep)
 {
     constexpr bool F64 = std::is_same_v<T, double>;
     Arena ar{static_cast<char*>(ws), 0, wsBytes};
-    float4* phi = ar.take<float4>(F64 ? n : 0);
-    float4* plo = ar.take<float4>(F64 ? n : 0);
-    float4* chi = ar.take<float4>(size_t(numNodes));
-    float4* clo = ar.take<float4>(size_t(numNodes));
-    float4* sz  = ar.take<float4>(size_t(numNodes));
-    float* cmax = ar.take<float>(1);
+    float4* phi  = ar.take<float4>(F64 ? n : 0);
+    float4* plo  = ar.take<float4>(F64 ? n : 0);
+    float4* nrec = ar.take<float4>(3 * size_t(numNodes));
+    float* cmax  = ar.take<float>(1);
     if (!ar.ok())
     {
         setLastError("find neighbors: workspace too small");
@@ -1004,25 +1059,27 @@ int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, cons
         unsigned g = unsigned(std::min<size_t>((n + 255) / 256, size_t(smCount()) * 16));
         if (n) prepParticlesKernel<<<g, 256, 0, s>>>(x, y, z, n, phi, plo, cmax);
         CSG_CHECK_LAUNCH();
-        if (numNodes) prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+        if (numNodes)
+            prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nrec, cmax);
     }
     else
     {
-        if (numNodes) prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+        if (numNodes)
+            prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nrec, cmax);
     }
     CSG_CHECK_LAUNCH();
-    *prep = NbPrep{phi, plo, chi, clo, sz, cmax};
+    *prep = NbPrep{phi, plo, nrec, cmax};
     return CS_OK;
 }
 
 template<class T>
-int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, int numNodes, void* ws, size_t wsBytes,
-                   NbPrep* prep)
+int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, const int32_t* childOffsets,
+                   const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws, size_t wsBytes, NbPrep* prep)
 {
     Arena ar{static_cast<char*>(ws), 0, wsBytes};
-    float4* chi = ar.take<float4>(size_t(numNodes));
-    float4* clo = ar.take<float4>(size_t(numNodes));
-    float4* sz  = ar.take<float4>(size_t(numNodes));
+    ar.take<float4>(0);
+    ar.take<float4>(0);
+    float4* nrec = ar.take<float4>(3 * size_t(numNodes));
     if (!ar.ok() || !prep->cmax)
     {
         setLastError("find neighbors: node workspace too small or no bound");
@@ -1033,24 +1090,26 @@ int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, int numNode
     if (numNodes)
     {
         if constexpr (std::is_same_v<T, double>)
-            prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+            prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nrec, cmax);
         else
-            prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, numNodes, chi, clo, sz, cmax);
+            prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nrec, cmax);
         CSG_CHECK_LAUNCH();
     }
-    prep->chi = chi;
-    prep->clo = clo;
-    prep->sz  = sz;
+    prep->nrec = nrec;
     return CS_OK;
 }
 
-template int nbPrepareNodes<float>(cudaStream_t, const float*, const float*, int, void*, size_t, NbPrep*);
-template int nbPrepareNodes<double>(cudaStream_t, const double*, const double*, int, void*, size_t, NbPrep*);
+template int nbPrepareNodes<float>(cudaStream_t, const float*, const float*, const int32_t*, const int32_t*,
+                                   const uint32_t*, int, void*, size_t, NbPrep*);
+template int nbPrepareNodes<double>(cudaStream_t, const double*, const double*, const int32_t*, const int32_t*,
+                                    const uint32_t*, int, void*, size_t, NbPrep*);
 
 template int nbPrepare<float>(cudaStream_t, const float*, const float*, const float*, size_t, const float*,
-                              const float*, int, void*, size_t, NbPrep*);
+                              const float*, const int32_t*, const int32_t*, const uint32_t*, int, void*, size_t,
+                              NbPrep*);
 template int nbPrepare<double>(cudaStream_t, const double*, const double*, const double*, size_t, const double*,
-                               const double*, int, void*, size_t, NbPrep*);
+                               const double*, const int32_t*, const int32_t*, const uint32_t*, int, void*, size_t,
+                               NbPrep*);
 
 template<class T>
 int findNeighbors(cudaStream_t s, const NbArgs<T>& a0, const NbPrep& prep)
@@ -1141,7 +1200,8 @@ int findNeighborsEntry(cudaStream_t s, const T* x, const T* y, const T* z, const
     int rc      = w.acquire(nullptr, 0, need, s);
     if (rc) return rc;
     NbPrep prep;
-    rc = nbPrepare<T>(s, x, y, z, nAll, a.centers, a.sizes, v.num_nodes, w.ptr, need, &prep);
+    rc = nbPrepare<T>(s, x, y, z, nAll, a.centers, a.sizes, v.child_offsets, v.internal_to_leaf, v.layout, v.num_nodes,
+                      w.ptr, need, &prep);
     if (rc) return rc;
     return findNeighbors<T>(s, a, prep);
 }

@@ -34,27 +34,30 @@ struct NbArgs
     int groupSize = 32;
 };
 
-//! float shadows for the FP64 pre-filter: particles x = hi + lo (two floats), node centres hi + lo, node sizes
+//! float shadows for the FP64 pre-filter: particles x = hi + lo (two floats), and one record of three float4 per node
+//!   nrec[3i]     centre rounded to float (hi),             w: child offset (int bits, 0 for a leaf)
+//!   nrec[3i + 1] centre - hi rounded to float (lo),       w: first particle of a leaf (uint bits)
+//!   nrec[3i + 2] half size rounded to nearest float,      w: end particle of a leaf (uint bits)
+//! so that one broadcast load round gives a popped node's box, its children and its particle range
 struct NbPrep
 {
-    const float4* phi = nullptr;
-    const float4* plo = nullptr;
-    const float4* chi = nullptr;
-    const float4* clo = nullptr;
-    const float4* sz  = nullptr;
-    const float* cmax = nullptr; // bound on |coordinate| over particles and node boxes
+    const float4* phi  = nullptr;
+    const float4* plo  = nullptr;
+    const float4* nrec = nullptr;
+    const float* cmax  = nullptr; // bound on |coordinate| over particles and node boxes
 };
 
 size_t nbPrepBytes(size_t n, int numNodes);
 template<class T>
 int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, const T* centers, const T* sizes,
-              int numNodes, void* ws, size_t wsBytes, NbPrep* prep);
+              const int32_t* childOffsets, const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws,
+              size_t wsBytes, NbPrep* prep);
 
 //! node part of nbPrepare only: the particle shadows (T = double) and cmax are set by the caller, cmax already holding
 //! the particles' bound (the node boxes are folded in with an atomic max)
 template<class T>
-int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, int numNodes, void* ws, size_t wsBytes,
-                   NbPrep* prep);
+int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, const int32_t* childOffsets,
+                   const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws, size_t wsBytes, NbPrep* prep);
 
 template<class T>
 NbArgs<T> makeNbArgs(const T* x, const T* y, const T* z, const T* h, uint32_t first, uint32_t last,

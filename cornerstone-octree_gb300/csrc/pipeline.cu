@@ -238,7 +238,9 @@ struct Pipeline final : PipelineBase
             prep.phi  = shadows ? shadowHi.as<float4>() : nullptr;
             prep.plo  = shadows ? shadowLo.as<float4>() : nullptr;
             prep.cmax = cmax;
-            if ((rc = nbPrepareNodes<T>(s, centers.as<T>(), sizes.as<T>(), N, nbPrepWs.p, nbPrepWs.bytes, &prep)))
+            if ((rc = nbPrepareNodes<T>(s, centers.as<T>(), sizes.as<T>(), childOffsets.as<int32_t>(),
+                                        i2l.as<int32_t>(), layout.as<uint32_t>(), N, nbPrepWs.p, nbPrepWs.bytes,
+                                        &prep)))
                 return rc;
         }
         if (cfg.do_neighbors)
@@ -261,8 +263,7 @@ struct Pipeline final : PipelineBase
             {
                 if ((rc = findHalos<K, T>(s, prefixes.as<K>(), childOffsets.as<int32_t>(), parents.as<int32_t>(),
                                           centers.as<T>(), sizes.as<T>(), leaves.as<K>(), sc.as<T>(), ss.as<T>(), box,
-                                          br.focusFirst, br.focusLast, flags.as<uint8_t>(), err + 2, prep.chi,
-                                          prep.sz)))
+                                          br.focusFirst, br.focusLast, flags.as<uint8_t>(), err + 2, prep.nrec)))
                     return rc;
             }
         }
@@ -277,14 +278,14 @@ struct Pipeline final : PipelineBase
             a.errWord   = err + 3;
             if (statsOn)
             {
-                if ((rc = nbStats.ensure(24 * sizeof(unsigned long long)))) return rc;
-                CSG_CUDA_TRY(cudaMemsetAsync(nbStats.p, 0, 24 * sizeof(unsigned long long), s));
+                if ((rc = nbStats.ensure(32 * sizeof(unsigned long long)))) return rc;
+                CSG_CUDA_TRY(cudaMemsetAsync(nbStats.p, 0, 32 * sizeof(unsigned long long), s));
                 a.stats = nbStats.as<unsigned long long>();
             }
             if ((rc = findNeighbors<T>(s, a, prep))) return rc;
             if (statsOn)
             {
-                unsigned long long h[24];
+                unsigned long long h[32];
                 CSG_CUDA_TRY(cudaMemcpyAsync(h, nbStats.p, sizeof(h), cudaMemcpyDeviceToHost, s));
                 CSG_CUDA_TRY(cudaStreamSynchronize(s));
                 std::fprintf(stderr,
@@ -307,6 +308,11 @@ struct Pipeline final : PipelineBase
                              "[cstone_gb300 neighbour stats] slowest warp geometry: rmax %g rmin %g group radius %g "
                              "box half %g C %g\n",
                              asf(h[15]), asf(h[18]), asf(h[16]), asf(h[17]), asf(h[19]));
+                std::fprintf(stderr,
+                             "[cstone_gb300 neighbour stats] candidate batches %.1f per warp, steps %.1f, needing "
+                             "lanes %.1f, min-cost/step-cost %.3f | cycles in batches %.1f%% of warp cycles\n",
+                             double(h[23]) / h[7], double(h[20]) / h[23], double(h[21]) / h[23],
+                             double(h[22]) / (11.0 * double(h[20])), 100.0 * double(h[24]) / double(h[25]));
             }
         }
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_COUNT], s));
