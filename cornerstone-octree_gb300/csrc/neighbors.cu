@@ -455,6 +455,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     __shared__ int sStack[NB_WARPS][NBG_STACK];
     __shared__ unsigned sMaskStack[NB_WARPS][NBG_STACK];
     __shared__ float4 sCand[NB_WARPS][32];
+    // S == 1: the staged candidates as separate x, y, z rows, read four at a time (two float2 pairs)
+    __shared__ __align__(16) float sCx[NB_WARPS][32], sCy[NB_WARPS][32], sCz[NB_WARPS][32];
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int t = lane % G, s = lane / G;
@@ -634,6 +636,20 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         Tin = fminf(float(r2), tsafe);
         Tup = float(r2);
     }
+    // minus the target in the candidates' frame, as float pairs for the packed distance evaluation
+    float2 nb2[3];
+    if constexpr (F64)
+    {
+        nb2[0] = make_float2(-b[0], -b[0]);
+        nb2[1] = make_float2(-b[1], -b[1]);
+        nb2[2] = make_float2(-b[2], -b[2]);
+    }
+    else
+    {
+        nb2[0] = make_float2(-float(xi), -float(xi));
+        nb2[1] = make_float2(-float(yi), -float(yi));
+        nb2[2] = make_float2(-float(zi), -float(zi));
+    }
     auto decideSlow = [&](uint32_t jj, int node) -> bool {
         if constexpr (F64)
             return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
@@ -694,7 +710,13 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         {
             float4 q = base == first ? q0 : stage(base + lane, last);
             __syncwarp();
-            sCand[warp][lane] = q;
+            if constexpr (S == 1)
+            {
+                sCx[warp][lane] = q.x;
+                sCy[warp][lane] = q.y;
+                sCz[warp][lane] = q.z;
+            }
+            else { sCand[warp][lane] = q; }
             __syncwarp();
             int cnt = int(min(32u, last - base));
             long long tc0 = 0;
@@ -718,14 +740,37 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     unsigned inM = 0, ambM = 0;
                     for (int k0 = 0; k0 < cnt; k0 += 8)
                     {
+                        // two candidates per instruction (packed FP32 pairs); the expressions are those of filter()
+                        const float4* vx = reinterpret_cast<const float4*>(&sCx[warp][k0]);
+                        const float4* vy = reinterpret_cast<const float4*>(&sCy[warp][k0]);
+                        const float4* vz = reinterpret_cast<const float4*>(&sCz[warp][k0]);
+                        float4 X[2] = {vx[0], vx[1]}, Y[2] = {vy[0], vy[1]}, Z[2] = {vz[0], vz[1]};
                         unsigned mi = 0, ma = 0;
 #pragma unroll
-                        for (int q8 = 0; q8 < 8; ++q8)
+                        for (int p = 0; p < 4; ++p)
                         {
-                            float e;
-                            filter(sCand[warp][k0 + q8], e);
-                            mi |= unsigned(e < Tin) << q8;
-                            ma |= unsigned(e < Tup) << q8;
+                            const float4& x4 = X[p >> 1];
+                            const float4& y4 = Y[p >> 1];
+                            const float4& z4 = Z[p >> 1];
+                            float2 cx = (p & 1) ? make_float2(x4.z, x4.w) : make_float2(x4.x, x4.y);
+                            float2 cy = (p & 1) ? make_float2(y4.z, y4.w) : make_float2(y4.x, y4.y);
+                            float2 cz = (p & 1) ? make_float2(z4.z, z4.w) : make_float2(z4.x, z4.y);
+                            float2 dx = __fadd2_rn(cx, nb2[0]);
+                            float2 dy = __fadd2_rn(cy, nb2[1]);
+                            float2 dz = __fadd2_rn(cz, nb2[2]);
+                            float2 e;
+                            if constexpr (F64)
+                            {
+                                e = __fmul2_rn(dx, dx);
+                                e = __ffma2_rn(dy, dy, e);
+                                e = __ffma2_rn(dz, dz, e);
+                            }
+                            else
+                            {
+                                e = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
+                            }
+                            mi |= (unsigned(e.x < Tin) | unsigned(e.y < Tin) << 1) << (2 * p);
+                            ma |= (unsigned(e.x < Tup) | unsigned(e.y < Tup) << 1) << (2 * p);
                         }
                         inM |= mi << k0;
                         ambM |= ma << k0;

@@ -99,3 +99,16 @@ def brute_force_neighbors(x, y, z, h, box_lo, box_hi, periodic):
         out.append(idx)
         counts[i] = idx.size
     return out, counts
+
+
+def outside_leaf_box(res):
+    """per sorted particle: True if it lies outside the box of the leaf that its key assigns it to (beyond a relative
+    rounding margin of 1e-12), from an oracle pipeline result"""
+    tree, layout = res["tree"], res["layout"]
+    L = tree.num_leaves if hasattr(tree, "num_leaves") else layout.size - 1
+    leaf = np.repeat(np.arange(L), np.diff(layout[: L + 1]).astype(np.int64))
+    node = tree.leaf_to_internal[tree.num_internal + leaf]
+    p = np.stack([res["x"], res["y"], res["z"]], axis=1)
+    c, s = res["centers"][node], res["sizes"][node]
+    tol = 1e-12 * (np.abs(c) + s)
+    return np.any(np.abs(p - c) > s + tol, axis=1)
