@@ -46,7 +46,9 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
     I mn[3], mx[3];
     if (valid)
     {
-        const T* init = nodeCenters + 3 * size_t(l2i[leaf]);
+        // the leaf's geometric centre, or (no leaf-to-node map) the caller's initial value in sc, as
+        // computeBoundingBoxGpu reads it
+        const T* init = l2i ? nodeCenters + 3 * size_t(l2i[leaf]) : sc + 3 * size_t(leaf);
         for (int k = 0; k < 3; ++k)
             mn[k] = mx[k] = ordKey(init[k]);
         uint32_t first = layout[leaf], last = layout[leaf + 1];

@@ -740,6 +740,153 @@ int rebalanceDecision(cudaStream_t s, const K* tree, const uint32_t* counts, int
     return CS_OK;
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// exclusive scan of int32 (in place allowed) and the emission of a rebalanced leaf array from scanned ops
+// ---------------------------------------------------------------------------------------------------------------
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS   = 4;
+constexpr int SCAN_TILE    = SCAN_THREADS * SCAN_ITEMS;
+
+// block-wide exclusive scan of one value per thread; returns the block total in *total
+__device__ __forceinline__ int scanBlockExclusive(int v, int* sWarp, int* total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) sWarp[warp] = incl;
+    __syncthreads();
+    if (warp == 0)
+    {
+        int w = lane < SCAN_THREADS / 32 ? sWarp[lane] : 0;
+        int wi = w;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            int t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < SCAN_THREADS / 32) sWarp[lane] = wi - w;
+        if (lane == 31) sWarp[SCAN_THREADS / 32] = wi;
+    }
+    __syncthreads();
+    int r  = sWarp[warp] + incl - v;
+    *total = sWarp[SCAN_THREADS / 32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scanTileSumsKernel(const int32_t* __restrict__ in, size_t n,
+                                                                   int32_t* __restrict__ tileSums)
+{
+    __shared__ int sWarp[SCAN_THREADS / 32 + 1];
+    size_t base = size_t(blockIdx.x) * SCAN_TILE + size_t(threadIdx.x) * SCAN_ITEMS;
+    int v       = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+        if (base + k < n) v += in[base + k];
+    int total;
+    scanBlockExclusive(v, sWarp, &total);
+    if (threadIdx.x == 0) tileSums[blockIdx.x] = total;
+}
+
+// one block: exclusive scan of the tile sums (plus init), in place
+__global__ void __launch_bounds__(SCAN_THREADS) scanTileOffsetsKernel(int32_t* tileSums, int numTiles, int32_t init)
+{
+    __shared__ int sWarp[SCAN_THREADS / 32 + 1];
+    int carry = init;
+    for (int b = 0; b < numTiles; b += SCAN_THREADS)
+    {
+        int i = b + threadIdx.x;
+        int v = i < numTiles ? tileSums[i] : 0;
+        int total;
+        int e = scanBlockExclusive(v, sWarp, &total);
+        if (i < numTiles) tileSums[i] = carry + e;
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scanApplyKernel(const int32_t* in, int32_t* out, size_t n,
+                                                                const int32_t* __restrict__ tileOffsets)
+{
+    __shared__ int sWarp[SCAN_THREADS / 32 + 1];
+    size_t base = size_t(blockIdx.x) * SCAN_TILE + size_t(threadIdx.x) * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+    {
+        v[k] = base + k < n ? in[base + k] : 0;
+        sum += v[k];
+    }
+    int total;
+    int e = scanBlockExclusive(sum, sWarp, &total) + tileOffsets[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+    {
+        if (base + k < n) out[base + k] = e;
+        e += v[k];
+    }
+}
+
+size_t exclusiveScanWorkspaceBytes(size_t n) { return (n / SCAN_TILE + 1) * sizeof(int32_t) + 256; }
+
+int exclusiveScanI32(cudaStream_t s, const int32_t* in, int32_t* out, size_t n, int32_t init, void* ws, size_t wsb)
+{
+    if (n == 0) return CS_OK;
+    if (!in || !out || n >= (size_t(1) << 31))
+    {
+        setLastError("exclusive scan: null pointer or n >= 2^31");
+        return CS_ERR_INVALID;
+    }
+    Workspace w;
+    int rc = w.acquire(ws, wsb, exclusiveScanWorkspaceBytes(n), s);
+    if (rc) return rc;
+    int32_t* tiles = static_cast<int32_t*>(w.ptr);
+    unsigned nt    = unsigned((n + SCAN_TILE - 1) / SCAN_TILE);
+    scanTileSumsKernel<<<nt, SCAN_THREADS, 0, s>>>(in, n, tiles);
+    CSG_CHECK_LAUNCH();
+    scanTileOffsetsKernel<<<1, SCAN_THREADS, 0, s>>>(tiles, int(nt), init);
+    CSG_CHECK_LAUNCH();
+    scanApplyKernel<<<nt, SCAN_THREADS, 0, s>>>(in, out, n, tiles);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+// processNode (tree/csarray.hpp:339-366): node i with ops[i+1] - ops[i] = 8^k new nodes emits its 8^k descendants
+// k levels down in key order (k = 0: the node itself; 0 new nodes: merged into its first sibling)
+template<class K>
+__global__ void rebalanceTreeKernel(const K* __restrict__ tree, int numNodes, const int32_t* __restrict__ ops,
+                                    K* __restrict__ newTree)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= numNodes) return;
+    int off  = ops[i];
+    int cnt  = ops[i + 1] - off;
+    K key    = tree[i];
+    K range  = tree[i + 1] - key;
+    K step   = cnt > 0 ? range / K(cnt) : range;
+    for (int j = 0; j < cnt; ++j)
+        newTree[off + j] = key + K(j) * step;
+    if (i == numNodes - 1) newTree[ops[numNodes]] = nodeRange<K>(0);
+}
+
+template<class K>
+int rebalanceTree(cudaStream_t s, const K* tree, int numNodes, const int32_t* ops, K* newTree)
+{
+    if (numNodes <= 0) return CS_OK;
+    if (!tree || !ops || !newTree)
+    {
+        setLastError("rebalance tree: null pointer");
+        return CS_ERR_INVALID;
+    }
+    rebalanceTreeKernel<K><<<iceil(size_t(numNodes), 256), 256, 0, s>>>(tree, numNodes, ops, newTree);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
 template int nodeCounts<uint32_t>(cudaStream_t, const uint32_t*, uint32_t*, int, const uint32_t*, size_t, uint32_t,
                                   void*, size_t);
 template int nodeCounts<uint64_t>(cudaStream_t, const uint64_t*, uint32_t*, int, const uint64_t*, size_t, uint32_t,
@@ -771,6 +918,23 @@ extern "C" int cs_rebalance_decision_u64(cs_stream_t stream, const uint64_t* tre
                                          int32_t num_nodes, unsigned bucket, int32_t* ops, int* converged_dev)
 {
     return rebalanceDecision<uint64_t>(cudaStream_t(stream), tree, counts, num_nodes, bucket, ops, converged_dev);
+}
+
+extern "C" size_t cs_exclusive_scan_workspace_bytes(size_t n) { return exclusiveScanWorkspaceBytes(n); }
+extern "C" int cs_exclusive_scan_i32(cs_stream_t stream, const int32_t* in, int32_t* out, size_t n, int32_t init,
+                                     void* ws, size_t wsb)
+{
+    return exclusiveScanI32(cudaStream_t(stream), in, out, n, init, ws, wsb);
+}
+extern "C" int cs_rebalance_tree_u32(cs_stream_t stream, const uint32_t* tree, int32_t num_nodes,
+                                     const int32_t* node_ops, uint32_t* new_tree)
+{
+    return rebalanceTree<uint32_t>(cudaStream_t(stream), tree, num_nodes, node_ops, new_tree);
+}
+extern "C" int cs_rebalance_tree_u64(cs_stream_t stream, const uint64_t* tree, int32_t num_nodes,
+                                     const int32_t* node_ops, uint64_t* new_tree)
+{
+    return rebalanceTree<uint64_t>(cudaStream_t(stream), tree, num_nodes, node_ops, new_tree);
 }
 
 extern "C" size_t cs_compute_octree_workspace_bytes(int32_t capacity)

@@ -158,6 +158,33 @@ def rebalance_decision(tree, counts, bucket):
     return ops[:L], bool(conv.item())
 
 
+def exclusive_scan(values, init=0, out=None):
+    """exclusiveScan of int32 values (out may be values itself)"""
+    out = torch.empty_like(values) if out is None else out
+    _check(lib.cs_exclusive_scan_i32(_stream(), _p(values), _p(out), C.c_size_t(values.numel()), C.c_int32(init),
+                                     None, C.c_size_t(0)))
+    return out
+
+
+def node_ops(tree, counts, bucket):
+    """computeNodeOpsGpu: decision + exclusive scan; returns (scanned ops[L+1], new leaf count, converged)"""
+    L = tree.numel() - 1
+    ops, conv = rebalance_decision(tree, counts, bucket)
+    full = torch.zeros(L + 1, dtype=torch.int32, device=tree.device)
+    full[:L] = ops
+    exclusive_scan(full, 0, full)
+    return full, int(full[L].item()), conv
+
+
+def rebalance_tree(tree, scanned_ops):
+    """rebalanceTreeGpu's emission: the new leaf array (scanned_ops[L] + 1 keys)"""
+    L = tree.numel() - 1
+    new_tree = torch.empty(int(scanned_ops[L].item()) + 1, dtype=tree.dtype, device=tree.device)
+    fn = lib.cs_rebalance_tree_u32 if key_bits(tree) == 32 else lib.cs_rebalance_tree_u64
+    _check(fn(_stream(), _p(tree), L, _p(scanned_ops), _p(new_tree)))
+    return new_tree
+
+
 def compute_octree(keys, bucket, max_count=0xFFFFFFFF, capacity=None):
     """computeOctree: returns (tree[L+1], counts[L], layout[L+1], iterations)."""
     n = keys.numel()
@@ -242,9 +269,11 @@ def geo_centers(prefixes, box, dtype=torch.float64, kind=HILBERT):
     return c, s
 
 
-def search_boxes(x, y, z, h, layout, first, last, scale, leaf_to_internal_leaves, node_centers):
+def search_boxes(x, y, z, h, layout, first, last, scale, leaf_to_internal_leaves, node_centers, init=None):
+    """computeBoundingBoxGpu for leaves [first, last). With leaf_to_internal_leaves None the boxes start from init
+    (L x 3, the reference's in/out searchCenters) instead of the leaves' geometric centres."""
     L = layout.numel() - 1
-    sc = torch.zeros((L, 3), dtype=x.dtype, device=x.device)
+    sc = torch.zeros((L, 3), dtype=x.dtype, device=x.device) if init is None else init.clone()
     ss = torch.zeros((L, 3), dtype=x.dtype, device=x.device)
     if x.dtype == torch.float32:
         _check(lib.cs_search_boxes_f32(_stream(), _p(x), _p(y), _p(z), _p(h), _p(layout), first, last,

@@ -174,6 +174,21 @@ int cs_rebalance_decision_u32(cs_stream_t stream, const uint32_t* tree, const ui
 int cs_rebalance_decision_u64(cs_stream_t stream, const uint64_t* tree, const uint32_t* counts, int32_t num_nodes,
                               unsigned bucket_size, int32_t* ops, int* converged_dev);
 
+/* cs_exclusive_scan_i32 replaces exclusiveScan(exec, first, last, output, init) (primitives/primitives_gpu.h:158-160)
+ * for int32: out[i] = init + in[0] + ... + in[i-1] for i < n; out == in is allowed. workspace may be NULL (then
+ * it is allocated stream-ordered). With the decision ops of cs_rebalance_decision (num_nodes + 1 entries, the last
+ * one ignored) it gives computeNodeOpsGpu's scanned ops (tree/csarray_gpu.cu:172-196), whose last entry is the new
+ * leaf count.
+ * cs_rebalance_tree replaces rebalanceTreeGpu's emission (processNodes, tree/csarray_gpu.cu:166-231): new_tree
+ * receives node_ops[num_nodes] + 1 keys, the last one the end key 8^maxLevel. */
+size_t cs_exclusive_scan_workspace_bytes(size_t n);
+int cs_exclusive_scan_i32(cs_stream_t stream, const int32_t* in, int32_t* out, size_t n, int32_t init, void* workspace,
+                          size_t workspace_bytes);
+int cs_rebalance_tree_u32(cs_stream_t stream, const uint32_t* tree, int32_t num_nodes, const int32_t* node_ops,
+                          uint32_t* new_tree);
+int cs_rebalance_tree_u64(cs_stream_t stream, const uint64_t* tree, int32_t num_nodes, const int32_t* node_ops,
+                          uint64_t* new_tree);
+
 /* cs_compute_octree replaces computeOctree / the `while(!updateOctreeGpu(...))` build loop (tree/csarray.hpp:429-440,
  * tree/update_gpu.cuh:43-68). Builds the converged cornerstone leaf array of the sorted keys from the root in one
  * cooperative launch (no host round trip per iteration). tree must hold capacity+1 keys, counts capacity entries,
@@ -231,6 +246,8 @@ int cs_geo_centers_u64_f64(cs_stream_t stream, const uint64_t* prefixes, int32_t
  * (focus/octree_focus_mpi.hpp:534-544): for leaves [first_leaf, last_leaf), the box around p -/+ h*scale of the
  * leaf's particles, initialised with the leaf's geometric centre centers[leaf_to_internal[leaf]]
  * (leaf_to_internal = OctreeView.leafToInternal + numInternalNodes). search_centers/sizes hold 3 values per leaf.
+ * With leaf_to_internal = NULL the initial value is read from search_centers[leaf] instead (in/out, node_centers
+ * unused), which is computeBoundingBoxGpu's own contract (the caller fills the centres first).
  * cs_find_halos replaces findHalosGpu (traversal/collisions_gpu.h:46-59, traversal/collisions_gpu.cu:23-77): flags
  * (num_nodes bytes, zeroed by the caller) are set to 1 for every node outside [leaves[first], leaves[last]) that
  * overlaps a search box of a focus leaf. */

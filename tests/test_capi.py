@@ -69,15 +69,36 @@ def test_invalid_arguments_are_rejected_without_gpu(lib):
     assert b"exceeds" in lib.cs_last_error()
 
 
-def test_cpp_shim_compiles_against_reference_headers():
+def test_cpp_shim_compiles_and_links_against_reference_headers(tmp_path, lib):
+    """the header-only shim defines the reference's own declarations (checked by its headers) and every C-ABI call
+    it makes resolves in the library"""
     ref = "/root/reference/include"
     if not os.path.isdir(ref):
         pytest.skip("reference headers not present")
-    shim = os.path.join(ROOT, "include", "cstone_gb300", "cstone_gpu_shim.hpp")
-    if not os.path.exists(shim):
-        pytest.skip("shim not present")
-    src = '#include "cstone_gb300/cstone_gpu_shim.hpp"\n'
-    r = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", "-x", "c++", "-", "-I", ref,
-                        "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include"],
-                       input=src, capture_output=True, text=True)
+    src = tmp_path / "main.cpp"
+    src.write_text('''#include "cstone_gb300/cstone_gpu_shim.hpp"
+int main(int argc, char**)
+{
+    if (argc > 5)
+    {
+        auto e = cstone::execution::gpuStream(0);
+        cstone::Box<double> b(0, 1);
+        cstone::computeSfcKeys(e, (double*)0, (double*)0, (double*)0, (cstone::HilbertKey<uint64_t>*)0, 0, b);
+        cstone::computeNodeOpsGpu(e, (uint64_t*)0, 0, (unsigned*)0, 64u, (int*)0);
+    }
+    return 0;
+}
+''')
+    obj, exe = tmp_path / "main.o", tmp_path / "a.out"
+    inc = ["-I", ref, "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include"]
+    r = subprocess.run(["g++", "-std=c++20", "-c", str(src), "-o", str(obj), *inc], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run(["g++", str(obj), "-o", str(exe), "-L", os.path.dirname(LIB), "-lcstone_gb300",
+                        "-L", "/usr/local/cuda/lib64", "-lcudart"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    syms = subprocess.run(["nm", "-C", str(obj)], capture_output=True, text=True).stdout
+    for name in ("cstone::computeSfcKeys", "cstone::sortByKey", "cstone::computeNodeCountsGpu",
+                 "cstone::computeNodeOpsGpu", "cstone::rebalanceTreeGpu", "cstone::buildOctreeGpu",
+                 "cstone::computeGeoCentersGpu", "cstone::computeBoundingBoxGpu", "cstone::findHalosGpu",
+                 "cstone::exclusiveScan"):
+        assert name in syms, name

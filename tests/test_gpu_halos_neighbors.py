@@ -48,6 +48,11 @@ def test_halos(cs, O, dtype, bnd, focus):
     assert np.array_equal(sc[first:last].cpu().numpy(), rsc[first:last])
     assert np.array_equal(ss[first:last].cpu().numpy(), rss[first:last])
     assert np.array_equal(flags.cpu().numpy(), rflags)
+    # computeBoundingBoxGpu's own contract: the caller fills the leaves' centres, the call updates them in place
+    init = c.view(-1, 3)[tl2i.long()]
+    sc2, ss2 = cs.search_boxes(tx, ty, tz, th, layout, first, last, 2.0, None, None, init=init)
+    torch.cuda.synchronize()
+    assert torch.equal(sc2[first:last], sc[first:last]) and torch.equal(ss2[first:last], ss[first:last])
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])

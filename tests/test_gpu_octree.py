@@ -97,6 +97,41 @@ def test_node_counts_and_decision(cs, O, bits):
         assert np.array_equal(ops.cpu().numpy(), rops) and conv == rconv
 
 
+@pytest.mark.parametrize("n", [0, 1, 2047, 2048, 2049, 100000, 3000001])
+def test_exclusive_scan(cs, n):
+    """exclusiveScan (primitives/primitives_gpu.h:158-160) on int32, out of place and in place, with an init value"""
+    rng = np.random.default_rng(n)
+    v = rng.integers(-50, 1000, n).astype(np.int32)
+    ref = (np.concatenate([[0], np.cumsum(v.astype(np.int64))[:-1]]) + 7).astype(np.int32) if n else v
+    t = torch.from_numpy(v).to(dev())
+    out = cs.exclusive_scan(t, 7)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref)
+    cs.exclusive_scan(t, 7, t)
+    torch.cuda.synchronize()
+    assert np.array_equal(t.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_node_ops_and_rebalance_tree(cs, O, bits):
+    """computeNodeOpsGpu + rebalanceTreeGpu (tree/csarray_gpu.cu:172-231): scanned ops, the new leaf count, the
+    converged flag and the emitted leaves equal the oracle's rebalance step"""
+    keys = gaussian_keys(40000, bits, 12)
+    tree, _, _ = O.compute_octree(keys, 16, bits)
+    keys2 = gaussian_keys(60000, bits, 14)
+    counts = O.node_counts(tree, keys2, bits)
+    for bucket in (4, 16, 100, 1 << 20):
+        rops, rconv = O.rebalance_decision(tree, counts, bucket, bits)
+        rnew = O.rebalance_tree(tree, rops, bits)
+        tt = _tkeys(tree, bits)
+        ops, L2, conv = cs.node_ops(tt, torch.from_numpy(counts.view(np.int32)).to(dev()), bucket)
+        new_tree = cs.rebalance_tree(tt, ops)
+        torch.cuda.synchronize()
+        assert L2 == rnew.size - 1 and conv == rconv, bucket
+        assert np.array_equal(ops.cpu().numpy()[:-1], np.concatenate([[0], np.cumsum(rops)[:-1]]).astype(np.int32))
+        assert np.array_equal(keys_u(new_tree), rnew), bucket
+
+
 @pytest.mark.parametrize("bits", [32, 64])
 def test_update_octree_steps(cs, O, bits):
     n = 50000
