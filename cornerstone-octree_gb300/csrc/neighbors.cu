@@ -1018,11 +1018,21 @@ __device__ __forceinline__ void nodeLinks(int i, const int32_t* childOffsets, co
     w2 = __uint_as_float(e);
 }
 
+// the node count from the host, or from a leaf count in device memory (N = L + (L - 1) / 7)
+__device__ __forceinline__ int nodeCount(const int* Ldev, int Nhost)
+{
+    if (!Ldev) return Nhost;
+    int L = *Ldev;
+    return L + (L - 1) / 7;
+}
+
 __global__ void prepNodesKernel(const double* __restrict__ centers, const double* __restrict__ sizes,
                                 const int32_t* __restrict__ childOffsets, const int32_t* __restrict__ i2l,
-                                const uint32_t* __restrict__ layout, int N, float4* __restrict__ nrec, float* cmax)
+                                const uint32_t* __restrict__ layout, int Nhost, const int* Ldev,
+                                float4* __restrict__ nrec, float* cmax)
 {
-    float m = 0.f;
+    float m     = 0.f;
+    const int N = nodeCount(Ldev, Nhost);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
     {
         float h[3], l[3], s[3];
@@ -1048,9 +1058,11 @@ __global__ void prepNodesKernel(const double* __restrict__ centers, const double
 // records of a float tree (centre, zero low part, size) and the magnitude bound C
 __global__ void prepNodesF32Kernel(const float* __restrict__ centers, const float* __restrict__ sizes,
                                    const int32_t* __restrict__ childOffsets, const int32_t* __restrict__ i2l,
-                                   const uint32_t* __restrict__ layout, int N, float4* __restrict__ nrec, float* cmax)
+                                   const uint32_t* __restrict__ layout, int Nhost, const int* Ldev,
+                                   float4* __restrict__ nrec, float* cmax)
 {
-    float m = 0.f;
+    float m     = 0.f;
+    const int N = nodeCount(Ldev, Nhost);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
     {
         float c[3], s[3];
@@ -1105,12 +1117,14 @@ int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, cons
         if (n) prepParticlesKernel<<<g, 256, 0, s>>>(x, y, z, n, phi, plo, cmax);
         CSG_CHECK_LAUNCH();
         if (numNodes)
-            prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nrec, cmax);
+            prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nullptr, nrec,
+                                               cmax);
     }
     else
     {
         if (numNodes)
-            prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nrec, cmax);
+            prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nullptr, nrec,
+                                                  cmax);
     }
     CSG_CHECK_LAUNCH();
     *prep = NbPrep{phi, plo, nrec, cmax};
@@ -1119,7 +1133,8 @@ int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, cons
 
 template<class T>
 int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, const int32_t* childOffsets,
-                   const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws, size_t wsBytes, NbPrep* prep)
+                   const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws, size_t wsBytes, NbPrep* prep,
+                   const int* Ldev)
 {
     Arena ar{static_cast<char*>(ws), 0, wsBytes};
     ar.take<float4>(0);
@@ -1135,9 +1150,10 @@ int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, const int32
     if (numNodes)
     {
         if constexpr (std::is_same_v<T, double>)
-            prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nrec, cmax);
+            prepNodesKernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, Ldev, nrec, cmax);
         else
-            prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, nrec, cmax);
+            prepNodesF32Kernel<<<gn, 256, 0, s>>>(centers, sizes, childOffsets, i2l, layout, numNodes, Ldev, nrec,
+                                                  cmax);
         CSG_CHECK_LAUNCH();
     }
     prep->nrec = nrec;
@@ -1145,9 +1161,9 @@ int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, const int32
 }
 
 template int nbPrepareNodes<float>(cudaStream_t, const float*, const float*, const int32_t*, const int32_t*,
-                                   const uint32_t*, int, void*, size_t, NbPrep*);
+                                   const uint32_t*, int, void*, size_t, NbPrep*, const int*);
 template int nbPrepareNodes<double>(cudaStream_t, const double*, const double*, const int32_t*, const int32_t*,
-                                    const uint32_t*, int, void*, size_t, NbPrep*);
+                                    const uint32_t*, int, void*, size_t, NbPrep*, const int*);
 
 template int nbPrepare<float>(cudaStream_t, const float*, const float*, const float*, size_t, const float*,
                               const float*, const int32_t*, const int32_t*, const uint32_t*, int, void*, size_t,

@@ -55,9 +55,11 @@ int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, cons
 
 //! node part of nbPrepare only: the particle shadows (T = double) and cmax are set by the caller, cmax already holding
 //! the particles' bound (the node boxes are folded in with an atomic max)
+//! Ldev (may be null): the leaf count in device memory; numNodes is then the capacity's node count
 template<class T>
 int nbPrepareNodes(cudaStream_t s, const T* centers, const T* sizes, const int32_t* childOffsets,
-                   const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws, size_t wsBytes, NbPrep* prep);
+                   const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws, size_t wsBytes, NbPrep* prep,
+                   const int* Ldev = nullptr);
 
 template<class T>
 NbArgs<T> makeNbArgs(const T* x, const T* y, const T* z, const T* h, uint32_t first, uint32_t last,

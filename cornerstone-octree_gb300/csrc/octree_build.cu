@@ -221,6 +221,7 @@ struct BuildArgs
     int updateMode;
     const uint32_t* countsIn; // UPDATE
     int Lin;                  // UPDATE
+    const int* LinDev;        // UPDATE: the input leaf count in device memory (replaces Lin when set)
     // outputs
     K* treeOut;
     uint32_t* countsOut;
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
     const unsigned tid = threadIdx.x;
     BuildState* st     = a.st;
 
-    int L   = a.updateMode ? a.Lin : 1;
+    int L   = a.updateMode ? (a.LinDev ? *a.LinDev : a.Lin) : 1;
     int cur = 0;
     if (!a.updateMode && b == 0 && tid == 0)
     {
@@ -571,7 +572,7 @@ size_t octreeBuildWorkspaceBytes(int capacity, bool update)
 template<class K>
 int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32_t maxCount, const K* treeIn,
                 const uint32_t* countsIn, int Lin, K* treeOut, uint32_t* countsOut, uint32_t* layoutOut, int capacity,
-                void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus)
+                void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus, const int* LinDev)
 {
     bool update = treeIn != nullptr;
     if (bucket == 0)
@@ -579,7 +580,7 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
         setLastError("octree: bucket size must be positive");
         return CS_ERR_INVALID;
     }
-    if (capacity < 1 || (update && Lin > capacity))
+    if (capacity < 1 || (update && !LinDev && Lin > capacity))
     {
         setLastError("octree: capacity %d too small", capacity);
         return CS_ERR_INVALID;
@@ -599,7 +600,9 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
     CSG_CUDA_TRY(cudaMemsetAsync(l.st, 0, sizeof(BuildState), s));
     if (update)
     {
-        CSG_CUDA_TRY(cudaMemcpyAsync(l.tree[0], treeIn, (size_t(Lin) + 1) * sizeof(K), cudaMemcpyDeviceToDevice, s));
+        // with the count in device memory the whole capacity is copied (the host does not know Lin)
+        size_t keysIn = LinDev ? size_t(capacity) + 1 : size_t(Lin) + 1;
+        CSG_CUDA_TRY(cudaMemcpyAsync(l.tree[0], treeIn, keysIn * sizeof(K), cudaMemcpyDeviceToDevice, s));
     }
 
     int G = buildGridSize();
@@ -620,6 +623,7 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
     a.updateMode = update ? 1 : 0;
     a.countsIn   = countsIn;
     a.Lin        = Lin;
+    a.LinDev     = LinDev;
     a.treeOut    = treeOut;
     a.countsOut  = countsOut;
     a.layoutOut  = layoutOut;
@@ -630,7 +634,19 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
                                              0, s));
     if (res) res->stateDev = &l.st->L;
     if (!sync) return CS_OK;
+    return octreeBuildFinish<K>(s, ws, wsBytes, capacity, update, res);
+}
 
+template<class K>
+int octreeBuildFinish(cudaStream_t s, void* ws, size_t wsBytes, int capacity, bool update, BuildResult* res)
+{
+    Arena ar{static_cast<char*>(ws), 0, wsBytes};
+    BuildLayout<K> l = buildLayout<K>(ar, capacity, update);
+    if (!ar.ok())
+    {
+        setLastError("octree: workspace too small");
+        return CS_ERR_INVALID;
+    }
     BuildState h;
     CSG_CUDA_TRY(cudaMemcpyAsync(&h, l.st, sizeof(BuildState), cudaMemcpyDeviceToHost, s));
     CSG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -663,14 +679,40 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
     return CS_OK;
 }
 
+// after an update build without host synchronisation: the new leaf count becomes the current one only if the build
+// succeeded; on failure (capacity) the input count stays, so every later kernel of the step stays within its buffers
+__global__ void commitLeafCountKernel(const BuildState* st, int* Ldev)
+{
+    if (st->err == 0) *Ldev = st->L;
+}
+
+template<class K>
+int commitLeafCount(cudaStream_t s, void* ws, size_t wsBytes, int capacity, int* Ldev)
+{
+    Arena ar{static_cast<char*>(ws), 0, wsBytes};
+    BuildLayout<K> l = buildLayout<K>(ar, capacity, true);
+    if (!ar.ok())
+    {
+        setLastError("octree: workspace too small");
+        return CS_ERR_INVALID;
+    }
+    commitLeafCountKernel<<<1, 1, 0, s>>>(l.st, Ldev);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template int commitLeafCount<uint32_t>(cudaStream_t, void*, size_t, int, int*);
+template int commitLeafCount<uint64_t>(cudaStream_t, void*, size_t, int, int*);
+template int octreeBuildFinish<uint32_t>(cudaStream_t, void*, size_t, int, bool, BuildResult*);
+template int octreeBuildFinish<uint64_t>(cudaStream_t, void*, size_t, int, bool, BuildResult*);
 template size_t octreeBuildWorkspaceBytes<uint32_t>(int, bool);
 template size_t octreeBuildWorkspaceBytes<uint64_t>(int, bool);
 template int octreeBuild<uint32_t>(cudaStream_t, const uint32_t*, size_t, unsigned, uint32_t, const uint32_t*,
                                    const uint32_t*, int, uint32_t*, uint32_t*, uint32_t*, int, void*, size_t,
-                                   BuildResult*, bool, FocusQuery<uint32_t>);
+                                   BuildResult*, bool, FocusQuery<uint32_t>, const int*);
 template int octreeBuild<uint64_t>(cudaStream_t, const uint64_t*, size_t, unsigned, uint32_t, const uint64_t*,
                                    const uint32_t*, int, uint64_t*, uint32_t*, uint32_t*, int, void*, size_t,
-                                   BuildResult*, bool, FocusQuery<uint64_t>);
+                                   BuildResult*, bool, FocusQuery<uint64_t>, const int*);
 
 // ---------------------------------------------------------------------------------------------------------------
 // standalone counts and decisions

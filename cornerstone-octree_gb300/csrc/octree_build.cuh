@@ -38,7 +38,17 @@ size_t octreeBuildWorkspaceBytes(int capacity, bool update);
 template<class K>
 int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32_t maxCount, const K* treeIn,
                 const uint32_t* countsIn, int Lin, K* treeOut, uint32_t* countsOut, uint32_t* layoutOut, int capacity,
-                void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus = FocusQuery<K>{});
+                void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus = FocusQuery<K>{},
+                const int* LinDev = nullptr);
+
+/*! after an octreeBuild with sync = false (e.g. replayed from a CUDA graph): read its state block from the same
+ *  workspace, synchronise, fill res and map the device error bits to a status, as the sync path does */
+template<class K>
+int octreeBuildFinish(cudaStream_t s, void* ws, size_t wsBytes, int capacity, bool update, BuildResult* res);
+
+//! after an update octreeBuild with sync = false: *Ldev = the new leaf count if the build succeeded (else unchanged)
+template<class K>
+int commitLeafCount(cudaStream_t s, void* ws, size_t wsBytes, int capacity, int* Ldev);
 
 template<class K>
 int nodeCounts(cudaStream_t s, const K* tree, uint32_t* counts, int numNodes, const K* keys, size_t n,

@@ -22,11 +22,32 @@ __device__ __forceinline__ int binaryKeyWeight(K key, unsigned level)
     return ret;
 }
 
-template<class K>
-__global__ void createLayoutKernel(const K* __restrict__ leaves, int L, int I, K* __restrict__ prefixes,
-                                   uint32_t* __restrict__ order)
+// L, I, N from the host, or from a leaf count in device memory (then the launch covers a capacity and the slots
+// [N, capacity) of the node arrays are padding)
+struct LinkSizes
 {
-    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    int L, I, N;
+};
+__device__ __forceinline__ LinkSizes linkSizes(const int* Ldev, int Lhost)
+{
+    int L = Ldev ? *Ldev : Lhost;
+    int I = (L - 1) / 7;
+    return {L, I, L + I};
+}
+
+template<class K>
+__global__ void createLayoutKernel(const K* __restrict__ leaves, const int* Ldev, int Lhost, int Ncap,
+                                   K* __restrict__ prefixes, uint32_t* __restrict__ order)
+{
+    int tid          = blockIdx.x * blockDim.x + threadIdx.x;
+    const LinkSizes z = linkSizes(Ldev, Lhost);
+    const int L = z.L, I = z.I;
+    if (Ldev && tid >= z.N && tid < Ncap)
+    {
+        // padding sorts behind every real prefix (ties with an all-ones prefix keep their larger index)
+        prefixes[tid] = ~K(0);
+        order[tid]    = uint32_t(tid);
+    }
     if (tid >= L) return;
     K key                 = leaves[tid];
     K next                = leaves[tid + 1];
@@ -46,10 +67,12 @@ __global__ void createLayoutKernel(const K* __restrict__ leaves, int L, int I, K
     }
 }
 
-__global__ void invertOrderKernel(const uint32_t* __restrict__ order, int N, int I, int32_t* __restrict__ i2l,
-                                  int32_t* __restrict__ l2i)
+__global__ void invertOrderKernel(const uint32_t* __restrict__ order, const int* Ldev, int Lhost,
+                                  int32_t* __restrict__ i2l, int32_t* __restrict__ l2i)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i             = blockIdx.x * blockDim.x + threadIdx.x;
+    const LinkSizes z = linkSizes(Ldev, Lhost);
+    const int N = z.N, I = z.I;
     if (i >= N) return;
     uint32_t v = order[i];
     if (v < uint32_t(N)) l2i[v] = i;
@@ -57,9 +80,11 @@ __global__ void invertOrderKernel(const uint32_t* __restrict__ order, int N, int
 }
 
 template<class K>
-__global__ void levelRangeKernel(const K* __restrict__ prefixes, int N, int32_t* __restrict__ levelRange)
+__global__ void levelRangeKernel(const K* __restrict__ prefixes, const int* Ldev, int Lhost,
+                                 int32_t* __restrict__ levelRange)
 {
     constexpr int maxL = KeyTraits<K>::maxLevel;
+    const int N        = linkSizes(Ldev, Lhost).N;
     int level          = threadIdx.x;
     if (level <= maxL)
     {
@@ -77,11 +102,12 @@ __global__ void levelRangeKernel(const K* __restrict__ prefixes, int N, int32_t*
 }
 
 template<class K>
-__global__ void linkKernel(const K* __restrict__ prefixes, int I, const int32_t* __restrict__ l2i,
-                           const int32_t* __restrict__ levelRange, int32_t* __restrict__ childOffsets,
-                           int32_t* __restrict__ parents)
+__global__ void linkKernel(const K* __restrict__ prefixes, const int* Ldev, int Lhost,
+                           const int32_t* __restrict__ l2i, const int32_t* __restrict__ levelRange,
+                           int32_t* __restrict__ childOffsets, int32_t* __restrict__ parents)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i       = blockIdx.x * blockDim.x + threadIdx.x;
+    const int I = linkSizes(Ldev, Lhost).I;
     if (i >= I) return;
     int idxA       = l2i[i];
     K prefix       = prefixes[idxA];
@@ -119,13 +145,14 @@ size_t buildLinkWorkspaceBytes(int L)
 
 template<class K>
 int buildLink(cudaStream_t s, const K* leaves, int L, const cs_octree_view& v, int prefixBits, void* ws,
-              size_t wsBytes, uint32_t* errWord)
+              size_t wsBytes, uint32_t* errWord, const int* Ldev)
 {
     if (L < 1)
     {
         setLastError("build octree: need at least one leaf");
         return CS_ERR_INVALID;
     }
+    // with Ldev, L is the leaf capacity and the arrays of v hold the capacity's node count
     int I = (L - 1) / 7, N = L + I;
     if (v.num_leaf_nodes != L || v.num_internal_nodes != I || v.num_nodes != N)
     {
@@ -153,7 +180,7 @@ int buildLink(cudaStream_t s, const K* leaves, int L, const cs_octree_view& v, i
         errWord = err;
     }
 
-    createLayoutKernel<K><<<iceil(L, 256), 256, 0, s>>>(leaves, L, I, prefixes, ord);
+    createLayoutKernel<K><<<iceil(Ldev ? N : L, 256), 256, 0, s>>>(leaves, Ldev, L, N, prefixes, ord);
     CSG_CHECK_LAUNCH();
     bool inAlt = false;
     int rc = radixSortPairs<K>(s, prefixes, ord, altKeys, ordB, N, 0, bits, false, sortBase, sortWs, errWord, &inAlt);
@@ -161,15 +188,15 @@ int buildLink(cudaStream_t s, const K* leaves, int L, const cs_octree_view& v, i
     uint32_t* sortedOrd = inAlt ? ordB : ord;
     if (inAlt) CSG_CUDA_TRY(cudaMemcpyAsync(prefixes, altKeys, size_t(N) * sizeof(K), cudaMemcpyDeviceToDevice, s));
 
-    invertOrderKernel<<<iceil(N, 256), 256, 0, s>>>(sortedOrd, N, I, v.internal_to_leaf, v.leaf_to_internal);
+    invertOrderKernel<<<iceil(N, 256), 256, 0, s>>>(sortedOrd, Ldev, L, v.internal_to_leaf, v.leaf_to_internal);
     CSG_CHECK_LAUNCH();
-    levelRangeKernel<K><<<1, 32, 0, s>>>(prefixes, N, v.level_range);
+    levelRangeKernel<K><<<1, 32, 0, s>>>(prefixes, Ldev, L, v.level_range);
     CSG_CHECK_LAUNCH();
     CSG_CUDA_TRY(cudaMemsetAsync(v.child_offsets, 0, (size_t(N) + 1) * sizeof(int32_t), s));
     if (I > 0)
     {
-        linkKernel<K><<<iceil(I, 256), 256, 0, s>>>(prefixes, I, v.leaf_to_internal, v.level_range, v.child_offsets,
-                                                   v.parents);
+        linkKernel<K><<<iceil(I, 256), 256, 0, s>>>(prefixes, Ldev, L, v.leaf_to_internal, v.level_range,
+                                                   v.child_offsets, v.parents);
         CSG_CHECK_LAUNCH();
     }
     return CS_OK;
@@ -178,9 +205,9 @@ int buildLink(cudaStream_t s, const K* leaves, int L, const cs_octree_view& v, i
 template size_t buildLinkWorkspaceBytes<uint32_t>(int);
 template size_t buildLinkWorkspaceBytes<uint64_t>(int);
 template int buildLink<uint32_t>(cudaStream_t, const uint32_t*, int, const cs_octree_view&, int, void*, size_t,
-                                 uint32_t*);
+                                 uint32_t*, const int*);
 template int buildLink<uint64_t>(cudaStream_t, const uint64_t*, int, const cs_octree_view&, int, void*, size_t,
-                                 uint32_t*);
+                                 uint32_t*, const int*);
 
 // ---------------------------------------------------------------------------------------------------------------
 // node geometry: centerAndSize (sfc/box.hpp:318-335) of hilbertIBox / mortonIBox
@@ -193,10 +220,11 @@ struct GeoParams
 };
 
 template<class K, class T, int Kind>
-__global__ void geoCentersKernel(const K* __restrict__ prefixes, int N, T* __restrict__ centers,
+__global__ void geoCentersKernel(const K* __restrict__ prefixes, int Nhost, const int* Ldev, T* __restrict__ centers,
                                  T* __restrict__ sizes, GeoParams<T> g)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int i       = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = Ldev ? linkSizes(Ldev, 0).N : Nhost;
     if (i >= N) return;
     K prefix          = prefixes[i];
     K start           = decodePlaceholderBit<K>(prefix);
@@ -225,7 +253,8 @@ __global__ void geoCentersKernel(const K* __restrict__ prefixes, int N, T* __res
 }
 
 template<class K, class T>
-int geoCenters(cudaStream_t s, const K* prefixes, int N, T* centers, T* sizes, const cs_box& box, int kind)
+int geoCenters(cudaStream_t s, const K* prefixes, int N, T* centers, T* sizes, const cs_box& box, int kind,
+               const int* Ldev)
 {
     if (N <= 0) return CS_OK;
     auto bp = makeBoxParams<T>(box);
@@ -236,16 +265,21 @@ int geoCenters(cudaStream_t s, const K* prefixes, int N, T* centers, T* sizes, c
         g.lo[k]   = bp.lo[k];
         g.half[k] = T(0.5) * uL * bp.len[k];
     }
-    if (kind == CS_HILBERT) geoCentersKernel<K, T, CS_HILBERT><<<iceil(N, 256), 256, 0, s>>>(prefixes, N, centers, sizes, g);
-    else geoCentersKernel<K, T, CS_MORTON><<<iceil(N, 256), 256, 0, s>>>(prefixes, N, centers, sizes, g);
+    if (kind == CS_HILBERT)
+        geoCentersKernel<K, T, CS_HILBERT><<<iceil(N, 256), 256, 0, s>>>(prefixes, N, Ldev, centers, sizes, g);
+    else geoCentersKernel<K, T, CS_MORTON><<<iceil(N, 256), 256, 0, s>>>(prefixes, N, Ldev, centers, sizes, g);
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }
 
-template int geoCenters<uint32_t, float>(cudaStream_t, const uint32_t*, int, float*, float*, const cs_box&, int);
-template int geoCenters<uint32_t, double>(cudaStream_t, const uint32_t*, int, double*, double*, const cs_box&, int);
-template int geoCenters<uint64_t, float>(cudaStream_t, const uint64_t*, int, float*, float*, const cs_box&, int);
-template int geoCenters<uint64_t, double>(cudaStream_t, const uint64_t*, int, double*, double*, const cs_box&, int);
+template int geoCenters<uint32_t, float>(cudaStream_t, const uint32_t*, int, float*, float*, const cs_box&, int,
+                                         const int*);
+template int geoCenters<uint32_t, double>(cudaStream_t, const uint32_t*, int, double*, double*, const cs_box&, int,
+                                          const int*);
+template int geoCenters<uint64_t, float>(cudaStream_t, const uint64_t*, int, float*, float*, const cs_box&, int,
+                                         const int*);
+template int geoCenters<uint64_t, double>(cudaStream_t, const uint64_t*, int, double*, double*, const cs_box&, int,
+                                          const int*);
 
 } // namespace csg
 

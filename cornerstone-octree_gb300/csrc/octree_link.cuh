@@ -13,9 +13,13 @@ size_t buildLinkWorkspaceBytes(int L);
  *  timeouts (nullptr = internal). */
 template<class K>
 int buildLink(cudaStream_t s, const K* leaves, int L, const cs_octree_view& v, int prefixBits, void* ws,
-              size_t wsBytes, uint32_t* errWord);
+              size_t wsBytes, uint32_t* errWord, const int* Ldev = nullptr);
+
+//! with Ldev (device leaf count) L is a capacity: every launch covers it, the kernels use the device count, the
+//! prefix sort runs over the capacity's node count with padding, and the host needs no synchronisation (graphs)
 
 template<class K, class T>
-int geoCenters(cudaStream_t s, const K* prefixes, int N, T* centers, T* sizes, const cs_box& box, int kind);
+int geoCenters(cudaStream_t s, const K* prefixes, int N, T* centers, T* sizes, const cs_box& box, int kind,
+               const int* Ldev = nullptr);
 
 } // namespace csg

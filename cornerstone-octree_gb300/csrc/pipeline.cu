@@ -70,6 +70,10 @@ struct PipelineBase
     virtual int outputs(cs_pipeline_outputs* o) = 0;
     virtual size_t deviceBytes() const          = 0;
     virtual int copyBack(cudaStream_t s, uint32_t* nc, uint8_t* flags, size_t flagsCap) = 0;
+    virtual int step(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, size_t n,
+                     const cs_box& box, bool useGraph, cs_pipeline_result* res) = 0;
+    virtual void resetSteps() = 0;
+    int graphReplays = 0; // steps of the last step sequence that were replayed from a captured graph
     cudaEvent_t ev[ST_COUNT + 1] = {};
     float stageMs[ST_COUNT]      = {};
     int lastN                    = 0;
@@ -87,6 +91,33 @@ struct Pipeline final : PipelineBase
     DevBuf prefixes, childOffsets, parents, levelRange, i2l, l2i, linkWs;
     DevBuf centers, sizes, sc, ss, flags;
     DevBuf nbPrepWs, nb, nc, nbStats;
+    // incremental time steps (step()): the current and the next leaf array with their counts, the current leaf
+    // count in device memory, the leaf capacity every buffer of a step is sized for, and one captured graph per
+    // direction of the leaf ping-pong
+    DevBuf incLeaves[2], incCounts[2], incL;
+    int incCur = -1, incCap = 0, incLhost = 0;
+    size_t incN = 0;
+    struct GraphKey
+    {
+        const void *x = nullptr, *y = nullptr, *z = nullptr, *h = nullptr;
+        size_t n      = 0;
+        cs_box box{};
+        int cap       = 0;
+        bool valid    = false;
+        bool operator==(const GraphKey& o) const
+        {
+            return valid && o.valid && x == o.x && y == o.y && z == o.z && h == o.h && n == o.n && cap == o.cap &&
+                   std::memcmp(&box, &o.box, sizeof(cs_box)) == 0;
+        }
+    };
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    GraphKey gkey[2];
+    // graph steps run on this stream, ordered after the caller's (which may be the legacy default stream, on which
+    // no capture is possible)
+    cudaStream_t gstream = nullptr;
+    cudaEvent_t joinEv   = nullptr;
+    const void* outLeaves      = nullptr;
+    const uint32_t* outCounts  = nullptr;
     // opt-in traversal statistics of the neighbour search, printed to stderr (CSTONE_GB300_NB_STATS=1)
     bool statsOn = std::getenv("CSTONE_GB300_NB_STATS") != nullptr;
     int capacity = 0;
@@ -102,8 +133,280 @@ struct Pipeline final : PipelineBase
     }
     ~Pipeline() override
     {
+        dropGraphs();
+        if (gstream) cudaStreamDestroy(gstream);
+        if (joinEv) cudaEventDestroy(joinEv);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+    }
+
+    void dropGraphs()
+    {
+        for (int c = 0; c < 2; ++c)
+        {
+            if (gexec[c]) cudaGraphExecDestroy(gexec[c]);
+            gexec[c]       = nullptr;
+            gkey[c].valid  = false;
+        }
+    }
+
+    void resetSteps() override
+    {
+        dropGraphs();
+        incCur = -1;
+    }
+
+    // grow a buffer keeping its first keep bytes (stream-ordered copy, then the old buffer is released)
+    static int growKeep(DevBuf& b, size_t need, size_t keep, cudaStream_t s)
+    {
+        if (need <= b.bytes) return CS_OK;
+        DevBuf nb;
+        int rc = nb.ensure(need);
+        if (rc) return rc;
+        if (keep && b.p) CSG_CUDA_TRY(cudaMemcpyAsync(nb.p, b.p, std::min(keep, b.bytes), cudaMemcpyDeviceToDevice, s));
+        CSG_CUDA_TRY(cudaStreamSynchronize(s));
+        std::swap(b.p, nb.p);
+        std::swap(b.bytes, nb.bytes);
+        return CS_OK;
+    }
+
+    // every buffer of an incremental step, sized for cap leaves: nothing is allocated inside a graph capture
+    int allocSteps(cudaStream_t s, size_t nIn, int cap)
+    {
+        int rc;
+        const int keyBits = 3 * KeyTraits<K>::maxLevel;
+        const int Ncap    = cap + (cap - 1) / 7;
+        for (DevBuf* b : {&keys, &keysAlt})
+            if ((rc = b->ensure(nIn * sizeof(K)))) return rc;
+        for (DevBuf* b : {&order, &orderAlt, &nc})
+            if ((rc = b->ensure(nIn * sizeof(uint32_t)))) return rc;
+        for (DevBuf* b : {&xs, &ys, &zs, &hs})
+            if ((rc = b->ensure(nIn * sizeof(T)))) return rc;
+        if ((rc = packed.ensure(nIn * sizeof(PackedT<T>)))) return rc;
+        if (std::is_same_v<T, double> && cfg.do_neighbors)
+            for (DevBuf* b : {&shadowHi, &shadowLo})
+                if ((rc = b->ensure(nIn * sizeof(float4)))) return rc;
+        if ((rc = sortWs.ensure(radixSortWorkspaceBytes<K>(nIn, 0, keyBits)))) return rc;
+        if ((rc = errWords.ensure(64))) return rc;
+        for (int c = 0; c < 2; ++c)
+        {
+            size_t keepL = incCur >= 0 ? (size_t(incLhost) + 1) * sizeof(K) : 0;
+            size_t keepC = incCur >= 0 ? size_t(incLhost) * sizeof(uint32_t) : 0;
+            if ((rc = growKeep(incLeaves[c], (size_t(cap) + 1) * sizeof(K), keepL, s))) return rc;
+            if ((rc = growKeep(incCounts[c], size_t(cap) * sizeof(uint32_t), keepC, s))) return rc;
+        }
+        if ((rc = incL.ensure(sizeof(int)))) return rc;
+        if ((rc = layout.ensure((size_t(cap) + 1) * sizeof(uint32_t)))) return rc;
+        if ((rc = buildWs.ensure(octreeBuildWorkspaceBytes<K>(cap, true)))) return rc;
+        if ((rc = prefixes.ensure(size_t(Ncap) * sizeof(K)))) return rc;
+        if ((rc = childOffsets.ensure((size_t(Ncap) + 1) * sizeof(int32_t)))) return rc;
+        if ((rc = parents.ensure(size_t(std::max(1, (Ncap - 1) / 8)) * sizeof(int32_t)))) return rc;
+        if ((rc = levelRange.ensure(size_t(KeyTraits<K>::maxLevel + 2) * sizeof(int32_t)))) return rc;
+        if ((rc = i2l.ensure(size_t(Ncap) * sizeof(int32_t)))) return rc;
+        if ((rc = l2i.ensure(size_t(Ncap) * sizeof(int32_t)))) return rc;
+        if ((rc = linkWs.ensure(buildLinkWorkspaceBytes<K>(cap)))) return rc;
+        if ((rc = centers.ensure(3 * size_t(Ncap) * sizeof(T)))) return rc;
+        if ((rc = sizes.ensure(3 * size_t(Ncap) * sizeof(T)))) return rc;
+        if ((rc = nbPrepWs.ensure(nbPrepBytes(0, Ncap)))) return rc;
+        if ((rc = flags.ensure(size_t(Ncap)))) return rc;
+        if (cfg.do_neighbors)
+            if ((rc = nb.ensure(std::max<size_t>(1, nIn * cfg.ngmax) * sizeof(uint32_t)))) return rc;
+        return CS_OK;
+    }
+
+    // one incremental step from leaf array cur, every launch sized by the capacity and every count read from device
+    // memory: no host synchronisation and no allocation, so the whole step can be captured into a CUDA graph
+    int enqueueStep(cudaStream_t s, int cur, const T* x, const T* y, const T* z, const T* h, size_t nIn,
+                    const cs_box& box)
+    {
+        int rc;
+        const int nxt      = cur ^ 1;
+        const int keyBits  = 3 * KeyTraits<K>::maxLevel;
+        const int cap      = incCap;
+        const int Icap     = (cap - 1) / 7, Ncap = cap + Icap;
+        constexpr bool F64 = std::is_same_v<T, double>;
+        const bool shadows = F64 && cfg.do_neighbors;
+        uint32_t* err      = errWords.as<uint32_t>();
+        float* cmax        = reinterpret_cast<float*>(err + 8);
+        int* Ldev          = incL.as<int>();
+        CSG_CUDA_TRY(cudaMemsetAsync(err, 0, 64, s));
+
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_KEYS], s));
+        if ((rc = sfcKeysPacked<T, K>(s, x, y, z, h, keys.as<K>(), packed.as<PackedT<T>>(), nIn, box, cfg.sfc_kind)))
+            return rc;
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_SORT], s));
+        bool inAlt = false;
+        rc = radixSortPairs<K>(s, keys.as<K>(), order.as<uint32_t>(), keysAlt.as<K>(), orderAlt.as<uint32_t>(), nIn,
+                               0, keyBits, true, sortWs.p, sortWs.bytes, err, &inAlt);
+        if (rc) return rc;
+        sortedKeys  = inAlt ? keysAlt.as<K>() : keys.as<K>();
+        sortedOrder = inAlt ? orderAlt.as<uint32_t>() : order.as<uint32_t>();
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_GATHER], s));
+        if ((rc = gatherPacked<T>(s, sortedOrder, nIn, packed.as<PackedT<T>>(), xs.as<T>(), ys.as<T>(), zs.as<T>(),
+                                  hs.as<T>(), shadows ? shadowHi.as<float4>() : nullptr,
+                                  shadows ? shadowLo.as<float4>() : nullptr, cmax)))
+            return rc;
+
+        // one updateOctree step: decision on the previous counts, rebalance, recount against the new keys
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_BUILD], s));
+        BuildResult br;
+        rc = octreeBuild<K>(s, sortedKeys, nIn, cfg.bucket_size, cfg.max_count, incLeaves[cur].as<K>(),
+                            incCounts[cur].as<uint32_t>(), 0, incLeaves[nxt].as<K>(), incCounts[nxt].as<uint32_t>(),
+                            layout.as<uint32_t>(), cap, buildWs.p, buildWs.bytes, &br, false, FocusQuery<K>{}, Ldev);
+        if (rc) return rc;
+        if ((rc = commitLeafCount<K>(s, buildWs.p, buildWs.bytes, cap, Ldev))) return rc;
+
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_LINK], s));
+        cs_octree_view v{cap, Icap, Ncap, prefixes.p, childOffsets.as<int32_t>(), parents.as<int32_t>(),
+                         levelRange.as<int32_t>(), i2l.as<int32_t>(), l2i.as<int32_t>()};
+        if ((rc = buildLink<K>(s, incLeaves[nxt].as<K>(), cap, v, 0, linkWs.p, linkWs.bytes, err + 1, Ldev)))
+            return rc;
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_GEO], s));
+        if ((rc = geoCenters<K, T>(s, prefixes.as<K>(), Ncap, centers.as<T>(), sizes.as<T>(), box, cfg.sfc_kind,
+                                   Ldev)))
+            return rc;
+
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_NBPREP], s));
+        NbPrep prep{};
+        if (cfg.do_neighbors)
+        {
+            prep.phi  = shadows ? shadowHi.as<float4>() : nullptr;
+            prep.plo  = shadows ? shadowLo.as<float4>() : nullptr;
+            prep.cmax = cmax;
+            if ((rc = nbPrepareNodes<T>(s, centers.as<T>(), sizes.as<T>(), childOffsets.as<int32_t>(),
+                                        i2l.as<int32_t>(), layout.as<uint32_t>(), Ncap, nbPrepWs.p, nbPrepWs.bytes,
+                                        &prep, Ldev)))
+                return rc;
+        }
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_HALOS], s));
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_NEIGHBORS], s));
+        if (cfg.do_neighbors)
+        {
+            cs_ns_view nv{cap, Ncap, childOffsets.as<int32_t>(), parents.as<int32_t>(), i2l.as<int32_t>(),
+                          layout.as<uint32_t>(), centers.p, sizes.p, cfg.search_ext};
+            NbArgs<T> a = makeNbArgs<T>(xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), 0, uint32_t(nIn), box, nv,
+                                        cfg.ngmax, nb.as<uint32_t>(), nc.as<uint32_t>());
+            a.errWord   = err + 3;
+            if ((rc = findNeighbors<T>(s, a, prep))) return rc;
+        }
+        CSG_CUDA_TRY(cudaEventRecord(ev[ST_COUNT], s));
+        return CS_OK;
+    }
+
+    int step(cudaStream_t s, const void* xv, const void* yv, const void* zv, const void* hv, size_t nIn,
+             const cs_box& box, bool useGraph, cs_pipeline_result* res) override
+    {
+        int rc;
+        if (incCur < 0 || nIn != incN)
+        {
+            // the first step of a sequence builds from the root and becomes the current tree; the step buffers are
+            // sized first (from an estimate), so that the root build's outputs are not moved afterwards
+            dropGraphs();
+            graphReplays = 0;
+            incCur       = -1; // nothing to keep yet
+            incCap = std::max(incCap, int(std::min<size_t>(size_t(1) << 29,
+                                                           nIn / std::max(1u, cfg.bucket_size) * 2 + 4096)));
+            if ((rc = allocSteps(s, nIn, incCap))) return rc;
+            if ((rc = run(s, xv, yv, zv, hv, nIn, box, 0, 0, res, false))) return rc;
+            if (last.num_leaves + last.num_leaves / 4 + 4096 > incCap)
+            {
+                incCap = last.num_leaves + last.num_leaves / 4 + 4096;
+                if ((rc = allocSteps(s, nIn, incCap))) return rc;
+                if ((rc = run(s, xv, yv, zv, hv, nIn, box, 0, 0, res, false))) return rc;
+            }
+            incCur      = -1;
+            const int L = last.num_leaves;
+            CSG_CUDA_TRY(cudaMemcpyAsync(incLeaves[0].p, leaves.p, (size_t(L) + 1) * sizeof(K),
+                                         cudaMemcpyDeviceToDevice, s));
+            CSG_CUDA_TRY(cudaMemcpyAsync(incCounts[0].p, counts.p, size_t(L) * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToDevice, s));
+            incLhost = L;
+            CSG_CUDA_TRY(cudaMemcpyAsync(incL.p, &incLhost, sizeof(int), cudaMemcpyHostToDevice, s));
+            CSG_CUDA_TRY(cudaStreamSynchronize(s));
+            incCur = 0;
+            incN   = nIn;
+            return CS_OK;
+        }
+        const T *x = static_cast<const T*>(xv), *y = static_cast<const T*>(yv), *z = static_cast<const T*>(zv),
+                *h = static_cast<const T*>(hv);
+        n = nIn;
+        if ((rc = allocSteps(s, nIn, incCap))) return rc;
+        const int cur = incCur;
+        if (useGraph)
+        {
+            if (!gstream) CSG_CUDA_TRY(cudaStreamCreateWithFlags(&gstream, cudaStreamNonBlocking));
+            if (!joinEv) CSG_CUDA_TRY(cudaEventCreateWithFlags(&joinEv, cudaEventDisableTiming));
+            CSG_CUDA_TRY(cudaEventRecord(joinEv, s));
+            CSG_CUDA_TRY(cudaStreamWaitEvent(gstream, joinEv, 0));
+            s = gstream; // the rest of the step, including its final synchronisation, runs there
+            GraphKey k;
+            k.x = xv, k.y = yv, k.z = zv, k.h = hv, k.n = nIn, k.box = box, k.cap = incCap, k.valid = true;
+            if (!gexec[cur] || !(gkey[cur] == k))
+            {
+                if (gexec[cur]) cudaGraphExecDestroy(gexec[cur]);
+                gexec[cur] = nullptr;
+                CSG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                int erc = enqueueStep(s, cur, x, y, z, h, nIn, box);
+                cudaGraph_t g = nullptr;
+                cudaError_t ce = cudaStreamEndCapture(s, &g);
+                if (erc || ce != cudaSuccess)
+                {
+                    if (g) cudaGraphDestroy(g);
+                    cudaGetLastError();
+                    if (!erc) setLastError("pipeline step: graph capture failed: %s", cudaGetErrorString(ce));
+                    return erc ? erc : CS_ERR_CUDA;
+                }
+                cudaError_t ie = cudaGraphInstantiate(&gexec[cur], g, 0);
+                cudaGraphDestroy(g);
+                if (ie != cudaSuccess)
+                {
+                    gexec[cur] = nullptr;
+                    setLastError("pipeline step: graph instantiation failed: %s", cudaGetErrorString(ie));
+                    return CS_ERR_CUDA;
+                }
+                gkey[cur] = k;
+            }
+            CSG_CUDA_TRY(cudaGraphLaunch(gexec[cur], s));
+            graphReplays++;
+        }
+        else if ((rc = enqueueStep(s, cur, x, y, z, h, nIn, box)))
+            return rc;
+
+        BuildResult br;
+        rc = octreeBuildFinish<K>(s, buildWs.p, buildWs.bytes, incCap, true, &br);
+        if (rc == CS_ERR_CAPACITY)
+        {
+            // the new leaf array did not fit: grow every buffer of the step and redo it from the same input
+            incCap = br.numLeaves + br.numLeaves / 4 + 4096;
+            dropGraphs();
+            if ((rc = allocSteps(s, nIn, incCap))) return rc;
+            CSG_CUDA_TRY(cudaMemcpyAsync(incL.p, &incLhost, sizeof(int), cudaMemcpyHostToDevice, s));
+            if ((rc = enqueueStep(s, cur, x, y, z, h, nIn, box))) return rc;
+            rc = octreeBuildFinish<K>(s, buildWs.p, buildWs.bytes, incCap, true, &br);
+        }
+        if (rc) return rc;
+        uint32_t herr[4] = {0, 0, 0, 0};
+        CSG_CUDA_TRY(cudaMemcpyAsync(herr, errWords.p, sizeof(herr), cudaMemcpyDeviceToHost, s));
+        CSG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (herr[0] | herr[1])
+        {
+            setLastError("pipeline step: a bounded device wait timed out (sort look-back)");
+            return CS_ERR_TIMEOUT;
+        }
+        if (herr[3])
+        {
+            setLastError("pipeline step: neighbour traversal stack overflow (malformed tree)");
+            return CS_ERR_DEVICE;
+        }
+        incCur   = cur ^ 1;
+        incLhost = br.numLeaves;
+        const int L = br.numLeaves, N = L + (L - 1) / 7;
+        last        = cs_pipeline_result{L, N, 1, 0, 0, br.maxDepth};
+        lastN       = 1;
+        outLeaves   = incLeaves[incCur].p;
+        outCounts   = incCounts[incCur].as<uint32_t>();
+        if (res) *res = last;
+        return CS_OK;
     }
 
     size_t deviceBytes() const override
@@ -319,6 +622,9 @@ struct Pipeline final : PipelineBase
 
         last             = cs_pipeline_result{L, N, br.iterations, br.focusFirst, br.focusLast, br.maxDepth};
         lastN            = 1;
+        outLeaves        = leaves.p;
+        outCounts        = counts.as<uint32_t>();
+        incCur           = -1; // a plain run ends any step sequence
         if (res) *res    = last;
         return CS_OK;
     }
@@ -370,8 +676,8 @@ struct Pipeline final : PipelineBase
         o->y               = ys.p;
         o->z               = zs.p;
         o->h               = hs.p;
-        o->leaves          = leaves.p;
-        o->counts          = counts.as<uint32_t>();
+        o->leaves          = const_cast<void*>(outLeaves);
+        o->counts          = const_cast<uint32_t*>(outCounts);
         o->layout          = layout.as<uint32_t>();
         o->octree          = cs_octree_view{L, I, N, prefixes.p, childOffsets.as<int32_t>(), parents.as<int32_t>(),
                                    levelRange.as<int32_t>(), i2l.as<int32_t>(), l2i.as<int32_t>()};
@@ -442,6 +748,35 @@ extern "C" int cs_pipeline_run_host(cs_pipeline p, cs_stream_t stream, const voi
     if (rc) return rc;
     return p->impl->copyBack(cudaStream_t(stream), ncHost, flagsHost, flagsCap);
 }
+
+extern "C" int cs_pipeline_step(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
+                                const void* h, size_t n, const cs_box* box, int use_graph, cs_pipeline_result* res)
+{
+    if (!p || !box || !x || !y || !z || !h)
+    {
+        setLastError("pipeline step: null argument");
+        return CS_ERR_INVALID;
+    }
+    if (n == 0 || n >= (size_t(1) << 30))
+    {
+        setLastError("pipeline step: n = %zu outside [1, 2^30)", n);
+        return CS_ERR_INVALID;
+    }
+    return p->impl->step(cudaStream_t(stream), x, y, z, h, n, *box, use_graph != 0, res);
+}
+
+extern "C" int cs_pipeline_reset_steps(cs_pipeline p)
+{
+    if (!p)
+    {
+        setLastError("pipeline reset: null argument");
+        return CS_ERR_INVALID;
+    }
+    p->impl->resetSteps();
+    return CS_OK;
+}
+
+extern "C" int cs_pipeline_graph_replays(cs_pipeline p) { return p ? p->impl->graphReplays : 0; }
 
 extern "C" int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out)
 {

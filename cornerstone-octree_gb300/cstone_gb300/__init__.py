@@ -375,6 +375,19 @@ class Pipeline:
                                         _p(flags_out), C.c_size_t(fcap), C.byref(self.result)))
         return self.result
 
+    def step(self, x, y, z, h, box, use_graph=True):
+        """one incremental time step (the first of a sequence builds from the root); device tensors"""
+        self._n = x.numel()
+        _check(lib.cs_pipeline_step(self.handle, _stream(), _p(x), _p(y), _p(z), _p(h), C.c_size_t(x.numel()),
+                                    C.byref(box), int(use_graph), C.byref(self.result)))
+        return self.result
+
+    def reset_steps(self):
+        _check(lib.cs_pipeline_reset_steps(self.handle))
+
+    def graph_replays(self):
+        return lib.cs_pipeline_graph_replays(self.handle)
+
     def stage_times(self):
         ms = (C.c_float * len(STAGES))()
         _check(lib.cs_pipeline_stage_times(self.handle, ms, len(STAGES)))

@@ -347,6 +347,23 @@ int cs_pipeline_run_host(cs_pipeline p, cs_stream_t stream, const void* x, const
 int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out);
 /* bytes of device memory the pipeline holds */
 size_t cs_pipeline_device_bytes(cs_pipeline p);
+/* Incremental time steps: the reference's per-step path with one updateOctree step from the previous tree instead of
+ * a build from the root (updateOctreeGpu, tree/update_gpu.cuh:43-68, as driven by Domain::sync each time step).
+ * The first call of a sequence (or a call with a different n) builds from the root like cs_pipeline_run; every later
+ * call recomputes keys, re-sorts, applies one rebalance decision to the previous leaf array using the previous
+ * counts, recounts the new leaves against the new keys, relinks, recomputes node geometry and the neighbours.
+ * Halos are not part of a step. Inputs are device pointers. With use_graph = 1 the step is captured once into a CUDA
+ * graph (one per direction of the leaf ping-pong; recaptured when the input pointers, n or the box change) and
+ * replayed; every launch of a step is sized by a leaf capacity and reads the current leaf count from device memory,
+ * so a step synchronises the host once, at its end. A step whose new tree outgrows the capacity is redone uncaptured
+ * with larger buffers. Results (cs_pipeline_get_outputs) are those of the last step. */
+int cs_pipeline_step(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z, const void* h,
+                     size_t n, const cs_box* box, int use_graph, cs_pipeline_result* result);
+/* the next cs_pipeline_step builds from the root again (drops the captured graphs) */
+int cs_pipeline_reset_steps(cs_pipeline p);
+/* steps of the current sequence that were replayed from a captured graph */
+int cs_pipeline_graph_replays(cs_pipeline p);
+
 /* device time in ms of each stage of the last run: keys, sort, gather, build, link, geometry, float node boxes
  * (node preparation of the halo and neighbour searches), halos, neighbours (count <= 9 values); waits for the last
  * run to finish */

@@ -95,3 +95,51 @@ def test_pipeline_repeated_runs_reuse_buffers(cs, O):
         torch.cuda.synchronize()
         for k in ("sorted_keys", "leaves", "counts", "neighbor_counts"):
             assert torch.equal(a[k], b[k]), (n, k)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_pipeline_incremental_steps(cs, O, use_graph):
+    """incremental time steps as in the 64M FP32 workload at reduced size: uniform [0,1]^3 periodic, Morton64,
+    bucket 32, every step displaces each particle by N(0, 0.1 * spacing) with periodic wrap, then one updateOctree
+    step from the previous tree, relink, geometry and neighbours (h = 1.2 * spacing, ngmax 150). Each step equals the
+    oracle's keys -> sort -> updateOctree -> link -> geometry -> neighbours on the same positions."""
+    n, bucket, ngmax, steps = 1 << 16, 32, 150, 5
+    spacing = n ** (-1 / 3)
+    x, y, z = (O.philox_uniform(11, s, n, 0.0, 1.0).astype(np.float32) for s in range(3))
+    h = np.full(n, 1.2 * spacing, np.float32)
+    obox = O.make_box(0.0, 1.0, 1)
+    box = cs.make_box(0.0, 1.0, cs.PERIODIC)
+    pipe = cs.Pipeline(32, 64, cs.MORTON, bucket, ngmax, 1.0, 1.0, False, True)
+    tx, ty, tz, th = to_dev(x, y, z, h)
+    rng = np.random.default_rng(5)
+    tree = counts = None
+    for step in range(steps):
+        if step:
+            for a in (x, y, z):
+                a += rng.normal(0.0, 0.1 * spacing, n).astype(np.float32)
+                a[a < 0] += np.float32(1.0)
+                a[a >= 1] -= np.float32(1.0)
+            for t, a in ((tx, x), (ty, y), (tz, z)):
+                t.copy_(torch.from_numpy(a))
+        res = pipe.step(tx, ty, tz, th, box, use_graph)
+        out = pipe.outputs()
+        torch.cuda.synchronize()
+        keys = O.sfc_keys(x, y, z, obox, 0, 64)
+        sk, perm = O.sort_by_key(keys)
+        if step == 0:
+            tree, counts, _ = O.compute_octree(sk, bucket, 64)
+        else:
+            tree, counts, _ = O.update_octree(sk, bucket, tree, counts, 64)
+        assert np.array_equal(keys_u(out["sorted_keys"]), sk), step
+        assert np.array_equal(u32(out["order"]), perm), step
+        assert np.array_equal(keys_u(out["leaves"]), tree), step
+        assert np.array_equal(u32(out["counts"]), counts), step
+        otree = O.build_octree(tree, 64)
+        assert np.array_equal(keys_u(out["prefixes"]), otree.prefixes), step
+        assert np.array_equal(out["child_offsets"].cpu().numpy(), otree.child_offsets), step
+        cen, siz = O.node_fp_centers(otree.prefixes, obox, np.float32, 0, 64)
+        assert np.array_equal(out["centers"].cpu().numpy(), cen), step
+        xs, ys, zs = x[perm], y[perm], z[perm]
+        nb, nc = O.find_neighbors(xs, ys, zs, h, 0, n, obox, otree, O.layout_from_counts(counts), cen, siz, ngmax)
+        neighbor_lists_equal(u32(out["neighbors"]), u32(out["neighbor_counts"]), nb, nc, ngmax)
+    assert pipe.graph_replays() == (steps - 1 if use_graph else 0)
