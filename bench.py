@@ -43,7 +43,10 @@ def parse():
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--n", type=int, default=16 * 1024 * 1024)
+    p.add_argument("--n", type=int, default=None, help="particles (default 16M plummer, 64M incremental)")
+    p.add_argument("--workload", default="plummer", choices=["plummer", "incremental"],
+                   help="plummer: the 16M keys->neighbours pass (default); incremental: 64M FP32 time steps with one "
+                        "updateOctree step each, replayed from CUDA graphs")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=1 << 20, help="particles of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -217,11 +220,91 @@ def run_reference(args, world, rank):
 # GPU arm
 # ---------------------------------------------------------------------------------------------------------------
 
+def run_incremental(args, world, rank, local):
+    """64M FP32 particles uniform in [0,1]^3, periodic; every step displaces each particle by N(0, 0.1 * spacing)
+    (periodic wrap) and runs one incremental pipeline step: Morton64 keys, sort, one updateOctree step from the
+    previous tree (bucket 32), link, geometry, neighbours (h = 1.2 * spacing, ngmax 150). The first step builds from
+    the root; the warm-up steps capture the two graphs of the leaf ping-pong."""
+    import torch
+
+    import cstone_gb300 as cs
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.n or 64 * 1024 * 1024
+    spacing = n ** (-1.0 / 3)
+    g = torch.Generator(device=dev).manual_seed(args.seed + rank)
+    x, y, z = (torch.rand(n, generator=g, device=dev, dtype=torch.float32) for _ in range(3))
+    h = torch.full((n,), 1.2 * spacing, device=dev, dtype=torch.float32)
+    box = cs.make_box(0.0, 1.0, cs.PERIODIC)
+
+    def displace():
+        for a in (x, y, z):
+            a.add_(torch.randn(n, generator=g, device=dev, dtype=torch.float32), alpha=0.1 * spacing)
+            a.sub_(torch.floor(a))  # periodic wrap into [0, 1)
+
+    def timed(pipe, use_graph, steps):
+        wall, dev_ms, stage_acc = 0.0, 0.0, None
+        for _ in range(steps):
+            displace()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pipe.step(x, y, z, h, box, use_graph)
+            wall += time.perf_counter() - t0
+            st = pipe.stage_times()
+            dev_ms += sum(st.values())
+            stage_acc = st if stage_acc is None else {k: stage_acc[k] + st[k] for k in st}
+        return wall * 1e3 / steps, dev_ms / steps, {k: round(v / steps, 4) for k, v in stage_acc.items()}
+
+    pipe = cs.Pipeline(32, 64, cs.MORTON, 32, 150, 1.0, 1.0, False, True)
+    pipe.step(x, y, z, h, box, True)  # root build
+    for _ in range(max(3, args.warmup)):
+        displace()
+        pipe.step(x, y, z, h, box, True)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        barrier(world)
+        g_wall, g_dev, g_st = timed(pipe, True, args.steps)
+        barrier(world)
+    replays = pipe.graph_replays()
+    res = pipe.result
+    nc = pipe.outputs()["neighbor_counts"]
+    mean_nc = float(nc.double().mean())
+    del nc, pipe  # release the first pipeline's buffers (about 45 GB at 64M) before the second one
+    torch.cuda.synchronize()
+    # the same steps without graphs, for comparison
+    plain = cs.Pipeline(32, 64, cs.MORTON, 32, 150, 1.0, 1.0, False, True)
+    plain.step(x, y, z, h, box, False)
+    for _ in range(max(3, args.warmup)):
+        displace()
+        plain.step(x, y, z, h, box, False)
+    p_wall, p_dev, _ = timed(plain, False, args.steps)
+    ms = max_over_ranks(g_wall, world)
+    if rank == 0:
+        line = {"metric": "Mparticles/s incremental step (64M FP32 uniform periodic, Morton64, CUDA graph)",
+                "value": round(world * n / (ms * 1e-3) / 1e6, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": max(3, args.warmup), "ms_per_step": round(ms, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "incremental-steps", "n_particles_per_gpu": n, "bucket_size": 32,
+                           "ngmax": 150, "keys": "morton64", "box": "periodic [0,1]^3", "sigma": "0.1 spacing",
+                           "h": "1.2 spacing", "l2": f"inputs ({12 * n >> 20} MB) larger than L2",
+                           "parallelism": f"replicas x{world}"},
+                "device_ms_per_step": round(g_dev, 3), "graph_replays": replays,
+                "ungraphed": {"ms_per_step": round(p_wall, 3), "device_ms_per_step": round(p_dev, 3)},
+                "stages_ms": g_st, "clocks": clocks.summary(),
+                "tree": {"leaves": res.num_leaves, "nodes": res.num_nodes, "max_depth": res.max_depth},
+                "mean_neighbors": round(mean_nc, 2)}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload == "incremental":
+        run_incremental(args, world, rank, local)
         return
 
     import numpy as np
@@ -232,7 +315,7 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    n = args.n
+    n = args.n or 16 * 1024 * 1024
     x, y, z = W.plummer(n, args.seed + rank)
     lo, hi = W.tight_box(x, y, z)
     box = cs.make_box(lo, hi)
@@ -339,10 +422,11 @@ def main():
 def gpu_launches_per_step(res):
     """kernels this library launches in one pipeline step (memsets and copies not counted): keys 1, sort 1 histogram
     + 1 scan + one pass per 8 key bits, gather 1, build 1 cooperative, link 1 layout + prefix sort + invert +
-    levelRange + link, geometry 1, halos 2, neighbour node prep 1, neighbours 1 (no periodic axis here)"""
+    levelRange + link, geometry 1, halos 2, neighbour node prep 1 + outside-leaf marks 1, neighbours 1 (no periodic
+    axis here)"""
     key_passes = (63 + 7) // 8
     prefix_passes = (3 * res.max_depth + 1 + 7) // 8
-    return 1 + (2 + key_passes) + 1 + 1 + (1 + 2 + prefix_passes + 3) + 1 + 2 + 1 + 1
+    return 1 + (2 + key_passes) + 1 + 1 + (1 + 2 + prefix_passes + 3) + 1 + 2 + 2 + 1
 
 
 if __name__ == "__main__":

@@ -402,13 +402,29 @@ constexpr int NBG_STACK = 192;
 // exact decision of a pair in the ambiguous band (T = double): d2 < r2 and the reference's path condition
 __device__ __noinline__ bool pairDecideF64(double xi, double yi, double zi, double r2, double cellR2, double kappa,
                                            const double* x, const double* y, const double* z, uint32_t j, int leafNode,
-                                           const int32_t* parents, const double* centers, const double* sizes)
+                                           const int32_t* parents, const double* centers, const double* sizes,
+                                           bool contained)
 {
     double dx = __dsub_rn(x[j], xi), dy = __dsub_rn(y[j], yi), dz = __dsub_rn(z[j], zi);
     double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     if (!(d2 < r2)) return false;
+    // the path-safe shortcut needs the candidate inside its leaf's box (then inside every ancestor's)
     double ts = cellR2 * (1.0 - 0x1p-46) - 4.0 * kappa * sqrt(cellR2) - 4.0 * kappa * kappa;
-    if (d2 < ts) return true;
+    if (contained && d2 < ts) return true;
+    BoxParams<double> nb{};
+    for (int n = leafNode;;)
+    {
+        if (!cellOverlapsExact<double>(xi, yi, zi, false, cellR2, centers + 3 * size_t(n), sizes + 3 * size_t(n), nb))
+            return false;
+        if (n == 0) return true;
+        n = parents[(n - 1) / 8];
+    }
+}
+
+// the reference's cell tests on the path from a leaf to the root, exact in FP64 (no periodic axis)
+__device__ __noinline__ bool pathExactF64(double xi, double yi, double zi, double cellR2, int leafNode,
+                                          const int32_t* parents, const double* centers, const double* sizes)
+{
     BoxParams<double> nb{};
     for (int n = leafNode;;)
     {
@@ -597,22 +613,23 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         return mayHitBox(cc, sz);
     };
 
-    // decision for one candidate of the lane's target that survived the first distance filter
-    auto decide = [&](uint32_t jj, float d2, int node) -> bool {
+    // decision for one candidate of the lane's target that survived the first distance filter; outside: the
+    // candidate lies outside its leaf's box (no path-safe shortcut)
+    auto decide = [&](uint32_t jj, float d2, int node, bool outside) -> bool {
         bool in;
         if constexpr (F64)
         {
-            in = d2 < Tacc;
+            in = !outside && d2 < Tacc;
             if (!in)
             {
                 if constexpr (Stats) stExact++;
                 in = pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
-                                   a.centers, a.sizes);
+                                   a.centers, a.sizes, !outside);
             }
         }
         else
         {
-            in = d2 < tsafe;
+            in = !outside && d2 < tsafe;
             if (!in)
             {
                 if constexpr (Stats) stExact++;
@@ -650,10 +667,10 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         nb2[1] = make_float2(-float(yi), -float(yi));
         nb2[2] = make_float2(-float(zi), -float(zi));
     }
-    auto decideSlow = [&](uint32_t jj, int node) -> bool {
+    auto decideSlow = [&](uint32_t jj, int node, bool contained) -> bool {
         if constexpr (F64)
             return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
-                                 a.centers, a.sizes);
+                                 a.centers, a.sizes, contained);
         else
             return pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
                                 reinterpret_cast<const float*>(a.centers), reinterpret_cast<const float*>(a.sizes));
@@ -692,15 +709,40 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     };
 
     // a leaf with its record r0..r2: the lanes whose sphere may reach it test its particles, 32 per batch
-    auto processLeaf = [&](int node, unsigned pmask, float4 r0, float4 r1, float4 r2) {
-        const uint32_t first = __float_as_uint(r1.w), last = __float_as_uint(r2.w);
+    auto processLeaf = [&](int node, unsigned pmask, float4 recA, float4 recB, float4 recC, bool anyOut) {
+        const uint32_t first = __float_as_uint(recB.w), last = __float_as_uint(recC.w);
         // the first batch is loaded before the lanes' box test, so that the two latencies overlap
         float4 q0 = stage(first + lane, last);
         float cc[3], sz[3];
-        frameOf(r0, r1, r2, cc, sz);
+        frameOf(recA, recB, recC, cc, sz);
         bool need     = ((pmask >> lane) & 1u) && mayHitBox(cc, sz);
         unsigned mask = __ballot_sync(0xffffffffu, need);
         if (mask == 0) return;
+        // a leaf holding particles outside its box: whether this lane's path to it passes the reference's cell tests.
+        // An upper bound of |x_i - box|^2 below Tsafe proves it (the ancestors contain the leaf); otherwise the path
+        // is walked once, exactly
+        bool leafPass = true;
+        if (anyOut && need)
+        {
+            float n2u = 0.f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+            {
+                float D = fabsf(__fsub_rn(cc[k], b[k]));
+                float u = __fmaf_ru(4.5f * EPS, D + sz[k], __fmaf_ru(1.05f, A, delta));
+                float d = fmaxf(__fadd_ru(__fsub_ru(D, sz[k]), u), 0.f);
+                n2u     = __fmaf_ru(d, d, n2u);
+            }
+            if (!(n2u < tsafe))
+            {
+                if constexpr (F64)
+                    leafPass = pathExactF64(xi, yi, zi, cellR2, node, a.parents, a.centers, a.sizes);
+                else
+                    leafPass = pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
+                                            reinterpret_cast<const float*>(a.centers),
+                                            reinterpret_cast<const float*>(a.sizes));
+            }
+        }
         if constexpr (Stats)
         {
             stLeaves++;
@@ -709,6 +751,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         for (uint32_t base = first; base < last; base += 32)
         {
             float4 q = base == first ? q0 : stage(base + lane, last);
+            // candidates of this batch that lie outside their leaf's box (only in marked leaves)
+            const unsigned outB =
+                anyOut ? __ballot_sync(0xffffffffu, base + lane < last && prep.pout[base + lane]) : 0u;
             __syncwarp();
             if constexpr (S == 1)
             {
@@ -776,6 +821,26 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                         ambM |= ma << k0;
                     }
                     ambM &= ~inM;
+                    // candidates outside their leaf's box: no path-safe shortcut; a neighbour iff within r and the
+                    // lane's path to the leaf passes (T = float: e < Tup is exactly d2 < r2)
+                    unsigned flagged = (inM | ambM) & outB;
+                    inM &= ~outB;
+                    ambM &= ~outB;
+                    if (flagged && leafPass)
+                    {
+                        if constexpr (F64)
+                        {
+                            const PbcArgs open{}; // group warps have no periodic sphere
+                            while (flagged)
+                            {
+                                int k = __ffs(flagged) - 1;
+                                flagged &= flagged - 1;
+                                if (pairExactF64(xi, yi, zi, false, r2, a.x, a.y, a.z, base + k, open))
+                                    inM |= 1u << k;
+                            }
+                        }
+                        else { inM |= flagged; }
+                    }
                     if constexpr (Stats)
                     {
                         stPair += cnt;
@@ -785,7 +850,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     {
                         int k = __ffs(ambM) - 1;
                         ambM &= ambM - 1;
-                        if (decideSlow(base + k, node)) inM |= 1u << k;
+                        if (decideSlow(base + k, node, true)) inM |= 1u << k;
                     }
                     if (i >= base && i - base < 32u) inM &= ~(1u << (i - base));
                     while (inM)
@@ -809,7 +874,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     {
                         float e;
                         if constexpr (Stats) stPair++;
-                        in = filter(sCand[warp][k], e) && decide(jj, e, node);
+                        in = filter(sCand[warp][k], e) && decide(jj, e, node, (outB >> k) & 1u);
                     }
                     unsigned hits = __ballot_sync(0xffffffffu, in);
                     unsigned mine = hits & tmask;
@@ -870,11 +935,11 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         unsigned pmask = maskStack[top - 1];
         --top;
         const float4* rec = prep.nrec + 3 * size_t(node);
-        float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
-        int c0    = __float_as_int(r0.w);
-        if (c0 == 0)
+        float4 recA = rec[0], recB = rec[1], recC = rec[2];
+        int c0      = __float_as_int(recA.w);
+        if (c0 <= 0) // a leaf; -1: it holds particles outside its box
         {
-            processLeaf(node, pmask, r0, r1, r2);
+            processLeaf(node, pmask, recA, recB, recC, c0 < 0);
             continue;
         }
         if constexpr (Stats) stNodes++;
@@ -1083,6 +1148,82 @@ __global__ void prepNodesF32Kernel(const float* __restrict__ centers, const floa
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m));
 }
 
+// one warp per node: the particles of a leaf that lie outside its box (the exact test in T, as the reference's node
+// boxes are T values), and a marker in the leaf's record (child offset -1) when it holds any. For T = double most
+// particles are decided in FP32 on the float shadows: with u = 2^-24 the FP32 value of |x - c| - s is within
+// 4 u (|x| + |c| + s) of the exact one, so a value below -8 u (|hi| + |c_hi| + s_f) proves the particle inside.
+template<class T>
+__global__ void markOutsideKernel(const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z,
+                                  const float4* __restrict__ phi, const T* __restrict__ centers,
+                                  const T* __restrict__ sizes, int Nhost, const int* Ldev, float4* __restrict__ nrec,
+                                  uint8_t* __restrict__ pout)
+{
+    const int node = int((size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (node >= nodeCount(Ldev, Nhost)) return;
+    // the node's record: float box, child offset, particle range (one load round)
+    const float4 ch = nrec[3 * size_t(node)], cl = nrec[3 * size_t(node) + 1], sz = nrec[3 * size_t(node) + 2];
+    if (__float_as_int(ch.w) != 0) return;
+    const uint32_t first = __float_as_uint(cl.w), last = __float_as_uint(sz.w);
+    bool any = false;
+    for (uint32_t j0 = first; j0 < last; j0 += 32)
+    {
+        const uint32_t j = j0 + lane;
+        bool o           = false;
+        if (j < last)
+        {
+            bool inside = false;
+            if constexpr (std::is_same_v<T, double>)
+            {
+                constexpr float U8 = 8.f * 5.9604644775390625e-8f;
+                float4 p           = phi[j];
+                float P[3] = {p.x, p.y, p.z}, C[3] = {ch.x, ch.y, ch.z}, S[3] = {sz.x, sz.y, sz.z};
+                inside = true;
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                {
+                    float d = __fsub_rn(fabsf(__fsub_rn(P[k], C[k])), S[k]);
+                    float E = __fmul_ru(U8, __fadd_ru(__fadd_ru(fabsf(P[k]), fabsf(C[k])), S[k]));
+                    inside  = inside && d < -E;
+                }
+            }
+            if (!inside)
+            {
+                const T* c = centers + 3 * size_t(node);
+                const T* s = sizes + 3 * size_t(node);
+                o = RN<T>::abs_(RN<T>::sub(x[j], c[0])) > s[0] || RN<T>::abs_(RN<T>::sub(y[j], c[1])) > s[1] ||
+                    RN<T>::abs_(RN<T>::sub(z[j], c[2])) > s[2];
+            }
+            pout[j] = o ? 1 : 0;
+        }
+        any |= __any_sync(0xffffffffu, o);
+    }
+    if (any && lane == 0) nrec[3 * size_t(node)].w = __int_as_float(-1);
+}
+
+template<class T>
+int nbMarkOutside(cudaStream_t s, const T* x, const T* y, const T* z, const float4* phi, const T* centers,
+                  const T* sizes, const int32_t* childOffsets, const int32_t* i2l, const uint32_t* layout,
+                  int numNodes, const NbPrep& prep, uint8_t* pout, const int* Ldev)
+{
+    if (numNodes <= 0) return CS_OK;
+    if (std::is_same_v<T, double> && !phi)
+    {
+        setLastError("find neighbors: the outside marks of FP64 particles need the float shadows");
+        return CS_ERR_INVALID;
+    }
+    markOutsideKernel<T><<<iceil(size_t(numNodes) * 32, 256), 256, 0, s>>>(x, y, z, phi, centers, sizes, numNodes,
+                                                                          Ldev, const_cast<float4*>(prep.nrec), pout);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template int nbMarkOutside<float>(cudaStream_t, const float*, const float*, const float*, const float4*,
+                                  const float*, const float*, const int32_t*, const int32_t*, const uint32_t*, int,
+                                  const NbPrep&, uint8_t*, const int*);
+template int nbMarkOutside<double>(cudaStream_t, const double*, const double*, const double*, const float4*,
+                                   const double*, const double*, const int32_t*, const int32_t*, const uint32_t*, int,
+                                   const NbPrep&, uint8_t*, const int*);
+
 size_t nbPrepBytes(size_t n, int numNodes)
 {
     Arena ar;
@@ -1090,6 +1231,7 @@ size_t nbPrepBytes(size_t n, int numNodes)
     ar.take<float4>(n);
     ar.take<float4>(3 * size_t(numNodes));
     ar.take<float>(1);
+    ar.take<uint8_t>(n);
     return ar.size + 256;
 }
 
@@ -1102,8 +1244,9 @@ int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, cons
     Arena ar{static_cast<char*>(ws), 0, wsBytes};
     float4* phi  = ar.take<float4>(F64 ? n : 0);
     float4* plo  = ar.take<float4>(F64 ? n : 0);
-    float4* nrec = ar.take<float4>(3 * size_t(numNodes));
-    float* cmax  = ar.take<float>(1);
+    float4* nrec  = ar.take<float4>(3 * size_t(numNodes));
+    float* cmax   = ar.take<float>(1);
+    uint8_t* pout = ar.take<uint8_t>(n);
     if (!ar.ok())
     {
         setLastError("find neighbors: workspace too small");
@@ -1127,8 +1270,10 @@ int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, cons
                                                   cmax);
     }
     CSG_CHECK_LAUNCH();
-    *prep = NbPrep{phi, plo, nrec, cmax};
-    return CS_OK;
+    *prep  = NbPrep{phi, plo, nrec, cmax, pout};
+    int rc = nbMarkOutside<T>(s, x, y, z, F64 ? phi : nullptr, centers, sizes, childOffsets, i2l, layout, numNodes,
+                              *prep, pout);
+    return rc;
 }
 
 template<class T>
@@ -1249,13 +1394,10 @@ int findNeighborsEntry(cudaStream_t s, const T* x, const T* y, const T* z, const
     }
     if (last == first) return CS_OK;
     NbArgs<T> a = makeNbArgs<T>(x, y, z, h, first, last, box, v, ngmax, nb, nc);
-    // the float shadows cover every particle a leaf can reference: [0, layout[L])
+    // the float shadows and the outside flags cover every particle a leaf can reference: [0, layout[L])
     uint32_t nAll = 0;
-    if constexpr (std::is_same_v<T, double>)
-    {
-        CSG_CUDA_TRY(cudaMemcpyAsync(&nAll, v.layout + v.num_leaf_nodes, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        CSG_CUDA_TRY(cudaStreamSynchronize(s));
-    }
+    CSG_CUDA_TRY(cudaMemcpyAsync(&nAll, v.layout + v.num_leaf_nodes, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CSG_CUDA_TRY(cudaStreamSynchronize(s));
     Workspace w;
     size_t need = nbPrepBytes(nAll, v.num_nodes);
     int rc      = w.acquire(nullptr, 0, need, s);

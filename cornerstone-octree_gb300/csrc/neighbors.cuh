@@ -45,9 +45,22 @@ struct NbPrep
     const float4* plo  = nullptr;
     const float4* nrec = nullptr;
     const float* cmax  = nullptr; // bound on |coordinate| over particles and node boxes
+    //! per particle: 1 if it lies outside the box of its own leaf. The reference quantises a coordinate as
+    //! int(floor(x * m) - xmin * m) (sfc/sfc.hpp:142-160), which can put a point into the finest cell below its
+    //! geometric one, so near a leaf's upper faces a particle may lie outside its leaf's box by up to one finest
+    //! cell. Such a candidate never takes the path-safe shortcut (it gets the exact ancestor walk).
+    const uint8_t* pout = nullptr;
 };
 
 size_t nbPrepBytes(size_t n, int numNodes);
+
+//! pout[j] for every particle of every leaf, and the marker (child offset -1) in the records of the leaves that hold
+//! any outside particle; after the node records of prep are built. phi: the float shadows (T = double, may be null).
+//! Launch over the nodes (Ldev: leaf count in device memory, numNodes then the capacity's node count)
+template<class T>
+int nbMarkOutside(cudaStream_t s, const T* x, const T* y, const T* z, const float4* phi, const T* centers,
+                  const T* sizes, const int32_t* childOffsets, const int32_t* i2l, const uint32_t* layout,
+                  int numNodes, const NbPrep& prep, uint8_t* pout, const int* Ldev = nullptr);
 template<class T>
 int nbPrepare(cudaStream_t s, const T* x, const T* y, const T* z, size_t n, const T* centers, const T* sizes,
               const int32_t* childOffsets, const int32_t* i2l, const uint32_t* layout, int numNodes, void* ws,

@@ -86,6 +86,7 @@ struct Pipeline final : PipelineBase
     DevBuf keys, keysAlt, order, orderAlt;
     DevBuf xs, ys, zs, hs;
     DevBuf packed, shadowHi, shadowLo; // x,y,z,h records of the keys pass; float shadows made by the gather
+    DevBuf pout;                       // per particle: outside its leaf's box (neighbour search)
     DevBuf sortWs, errWords;
     DevBuf buildWs, leaves, counts, layout;
     DevBuf prefixes, childOffsets, parents, levelRange, i2l, l2i, linkWs;
@@ -210,15 +211,22 @@ struct Pipeline final : PipelineBase
         if ((rc = nbPrepWs.ensure(nbPrepBytes(0, Ncap)))) return rc;
         if ((rc = flags.ensure(size_t(Ncap)))) return rc;
         if (cfg.do_neighbors)
+        {
             if ((rc = nb.ensure(std::max<size_t>(1, nIn * cfg.ngmax) * sizeof(uint32_t)))) return rc;
+            if ((rc = pout.ensure(nIn))) return rc;
+        }
         return CS_OK;
     }
 
     // one incremental step from leaf array cur, every launch sized by the capacity and every count read from device
     // memory: no host synchronisation and no allocation, so the whole step can be captured into a CUDA graph
     int enqueueStep(cudaStream_t s, int cur, const T* x, const T* y, const T* z, const T* h, size_t nIn,
-                    const cs_box& box)
+                    const cs_box& box, bool capturing)
     {
+        // inside a capture a stage event must be an external record node to be recorded at replay
+        auto rec = [&](cudaEvent_t e) {
+            return capturing ? cudaEventRecordWithFlags(e, s, cudaEventRecordExternal) : cudaEventRecord(e, s);
+        };
         int rc;
         const int nxt      = cur ^ 1;
         const int keyBits  = 3 * KeyTraits<K>::maxLevel;
@@ -231,24 +239,24 @@ struct Pipeline final : PipelineBase
         int* Ldev          = incL.as<int>();
         CSG_CUDA_TRY(cudaMemsetAsync(err, 0, 64, s));
 
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_KEYS], s));
+        CSG_CUDA_TRY(rec(ev[ST_KEYS]));
         if ((rc = sfcKeysPacked<T, K>(s, x, y, z, h, keys.as<K>(), packed.as<PackedT<T>>(), nIn, box, cfg.sfc_kind)))
             return rc;
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_SORT], s));
+        CSG_CUDA_TRY(rec(ev[ST_SORT]));
         bool inAlt = false;
         rc = radixSortPairs<K>(s, keys.as<K>(), order.as<uint32_t>(), keysAlt.as<K>(), orderAlt.as<uint32_t>(), nIn,
                                0, keyBits, true, sortWs.p, sortWs.bytes, err, &inAlt);
         if (rc) return rc;
         sortedKeys  = inAlt ? keysAlt.as<K>() : keys.as<K>();
         sortedOrder = inAlt ? orderAlt.as<uint32_t>() : order.as<uint32_t>();
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_GATHER], s));
+        CSG_CUDA_TRY(rec(ev[ST_GATHER]));
         if ((rc = gatherPacked<T>(s, sortedOrder, nIn, packed.as<PackedT<T>>(), xs.as<T>(), ys.as<T>(), zs.as<T>(),
                                   hs.as<T>(), shadows ? shadowHi.as<float4>() : nullptr,
                                   shadows ? shadowLo.as<float4>() : nullptr, cmax)))
             return rc;
 
         // one updateOctree step: decision on the previous counts, rebalance, recount against the new keys
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_BUILD], s));
+        CSG_CUDA_TRY(rec(ev[ST_BUILD]));
         BuildResult br;
         rc = octreeBuild<K>(s, sortedKeys, nIn, cfg.bucket_size, cfg.max_count, incLeaves[cur].as<K>(),
                             incCounts[cur].as<uint32_t>(), 0, incLeaves[nxt].as<K>(), incCounts[nxt].as<uint32_t>(),
@@ -256,17 +264,17 @@ struct Pipeline final : PipelineBase
         if (rc) return rc;
         if ((rc = commitLeafCount<K>(s, buildWs.p, buildWs.bytes, cap, Ldev))) return rc;
 
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_LINK], s));
+        CSG_CUDA_TRY(rec(ev[ST_LINK]));
         cs_octree_view v{cap, Icap, Ncap, prefixes.p, childOffsets.as<int32_t>(), parents.as<int32_t>(),
                          levelRange.as<int32_t>(), i2l.as<int32_t>(), l2i.as<int32_t>()};
         if ((rc = buildLink<K>(s, incLeaves[nxt].as<K>(), cap, v, 0, linkWs.p, linkWs.bytes, err + 1, Ldev)))
             return rc;
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_GEO], s));
+        CSG_CUDA_TRY(rec(ev[ST_GEO]));
         if ((rc = geoCenters<K, T>(s, prefixes.as<K>(), Ncap, centers.as<T>(), sizes.as<T>(), box, cfg.sfc_kind,
                                    Ldev)))
             return rc;
 
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_NBPREP], s));
+        CSG_CUDA_TRY(rec(ev[ST_NBPREP]));
         NbPrep prep{};
         if (cfg.do_neighbors)
         {
@@ -277,9 +285,14 @@ struct Pipeline final : PipelineBase
                                         i2l.as<int32_t>(), layout.as<uint32_t>(), Ncap, nbPrepWs.p, nbPrepWs.bytes,
                                         &prep, Ldev)))
                 return rc;
+            if ((rc = nbMarkOutside<T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), prep.phi, centers.as<T>(),
+                                       sizes.as<T>(), childOffsets.as<int32_t>(), i2l.as<int32_t>(),
+                                       layout.as<uint32_t>(), Ncap, prep, pout.as<uint8_t>(), Ldev)))
+                return rc;
+            prep.pout = pout.as<uint8_t>();
         }
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_HALOS], s));
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_NEIGHBORS], s));
+        CSG_CUDA_TRY(rec(ev[ST_HALOS]));
+        CSG_CUDA_TRY(rec(ev[ST_NEIGHBORS]));
         if (cfg.do_neighbors)
         {
             cs_ns_view nv{cap, Ncap, childOffsets.as<int32_t>(), parents.as<int32_t>(), i2l.as<int32_t>(),
@@ -289,7 +302,7 @@ struct Pipeline final : PipelineBase
             a.errWord   = err + 3;
             if ((rc = findNeighbors<T>(s, a, prep))) return rc;
         }
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_COUNT], s));
+        CSG_CUDA_TRY(rec(ev[ST_COUNT]));
         return CS_OK;
     }
 
@@ -346,7 +359,7 @@ struct Pipeline final : PipelineBase
                 if (gexec[cur]) cudaGraphExecDestroy(gexec[cur]);
                 gexec[cur] = nullptr;
                 CSG_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                int erc = enqueueStep(s, cur, x, y, z, h, nIn, box);
+                int erc = enqueueStep(s, cur, x, y, z, h, nIn, box, true);
                 cudaGraph_t g = nullptr;
                 cudaError_t ce = cudaStreamEndCapture(s, &g);
                 if (erc || ce != cudaSuccess)
@@ -369,7 +382,7 @@ struct Pipeline final : PipelineBase
             CSG_CUDA_TRY(cudaGraphLaunch(gexec[cur], s));
             graphReplays++;
         }
-        else if ((rc = enqueueStep(s, cur, x, y, z, h, nIn, box)))
+        else if ((rc = enqueueStep(s, cur, x, y, z, h, nIn, box, false)))
             return rc;
 
         BuildResult br;
@@ -381,7 +394,7 @@ struct Pipeline final : PipelineBase
             dropGraphs();
             if ((rc = allocSteps(s, nIn, incCap))) return rc;
             CSG_CUDA_TRY(cudaMemcpyAsync(incL.p, &incLhost, sizeof(int), cudaMemcpyHostToDevice, s));
-            if ((rc = enqueueStep(s, cur, x, y, z, h, nIn, box))) return rc;
+            if ((rc = enqueueStep(s, cur, x, y, z, h, nIn, box, false))) return rc;
             rc = octreeBuildFinish<K>(s, buildWs.p, buildWs.bytes, incCap, true, &br);
         }
         if (rc) return rc;
@@ -413,7 +426,7 @@ struct Pipeline final : PipelineBase
     {
         size_t t = 0;
         for (const DevBuf* b : {&inX, &inY, &inZ, &inH, &keys, &keysAlt, &order, &orderAlt, &xs, &ys, &zs, &hs,
-                                &packed, &shadowHi, &shadowLo, &sortWs, &errWords, &buildWs, &leaves, &counts,
+                                &packed, &shadowHi, &shadowLo, &pout, &sortWs, &errWords, &buildWs, &leaves, &counts,
                                 &layout, &prefixes, &childOffsets,
                                 &parents, &levelRange, &i2l, &l2i, &linkWs, &centers, &sizes, &sc, &ss, &flags,
                                 &nbPrepWs, &nb, &nc})
@@ -547,7 +560,15 @@ struct Pipeline final : PipelineBase
                 return rc;
         }
         if (cfg.do_neighbors)
+        {
             if ((rc = nb.ensure(std::max<size_t>(1, n * cfg.ngmax) * sizeof(uint32_t)))) return rc;
+            if ((rc = pout.ensure(n))) return rc;
+            if ((rc = nbMarkOutside<T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), prep.phi, centers.as<T>(),
+                                       sizes.as<T>(), childOffsets.as<int32_t>(), i2l.as<int32_t>(),
+                                       layout.as<uint32_t>(), N, prep, pout.as<uint8_t>())))
+                return rc;
+            prep.pout = pout.as<uint8_t>();
+        }
 
         // ---- halos for the focus leaves ----
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_HALOS], s));

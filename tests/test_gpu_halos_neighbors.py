@@ -12,7 +12,10 @@ def _setup(O, cs, x, y, z, h, box_lo, box_hi, bnd, bucket, kind=1, bits=64):
     obox = O.make_box(box_lo, box_hi, bnd)
     ref = O.pipeline(x, y, z, h, obox, bucket, 1, kind, bits, with_neighbors=False)
     tx, ty, tz, th = to_dev(ref["x"], ref["y"], ref["z"], ref["h"])
-    leaves = torch.from_numpy(ref["leaves"].view(np.int64)).to(dev())
+    if bits == 32:
+        leaves = torch.from_numpy(ref["leaves"].astype(np.uint32).view(np.int32)).to(dev())
+    else:
+        leaves = torch.from_numpy(ref["leaves"].view(np.int64)).to(dev())
     o = cs.build_octree(leaves)
     layout = torch.from_numpy(ref["layout"].view(np.int32)).to(dev())
     box = cs.make_box(box_lo, box_hi, bnd)
@@ -125,3 +128,35 @@ def test_neighbors_duplicates(cs, O):
     nb, nc = cs.find_neighbors(tx, ty, tz, th, 0, n, box, o, layout, c, s, ngmax)
     torch.cuda.synchronize()
     neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_neighbors_particles_outside_their_leaf_box(cs, O, bits):
+    """The reference quantises int(floor(x * m) - xmin * m), which can key a point into the finest cell below its
+    geometric one, so the point lies outside its leaf's box and the reference's traversal rejects some pairs within
+    the radius. The GPU search rejects the same pairs. With 32-bit keys this input (the brute-force test's gaussian
+    generator) holds such a pair."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from kat_util import brute_force_neighbors
+
+    radius, n = 0.0624, 2500
+    lo, hi = np.array((-1.2, -0.213, -5.1)), np.array((0.23, 3.213, 1.23))
+    rng = np.random.default_rng(713159802)
+    pts = []
+    for k in range(3):
+        v = rng.normal((lo[k] + hi[k]) / 2, (hi[k] - lo[k]) / 5, 4 * n)
+        pts.append(v[(v >= lo[k]) & (v < hi[k])][:n])
+    x, y, z = pts
+    h = np.full(n, radius / 2)
+    ngmax = n
+    ref, obox, box, o, layout, c, s, (tx, ty, tz, th) = _setup(O, cs, x, y, z, h, tuple(lo), tuple(hi), 0, 64, 1,
+                                                                bits)
+    rnb, rnc = O.find_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], 0, n, obox, ref["tree"], ref["layout"],
+                                ref["centers"], ref["sizes"], ngmax)
+    nb, nc = cs.find_neighbors(tx, ty, tz, th, 0, n, box, o, layout, c, s, ngmax)
+    torch.cuda.synchronize()
+    neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)
+    if bits == 32:
+        _, counts = brute_force_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], lo, hi, False)
+        assert (counts != rnc).any()  # the case is exercised: the reference drops a pair within the radius

@@ -124,6 +124,8 @@ def test_pipeline_incremental_steps(cs, O, use_graph):
         res = pipe.step(tx, ty, tz, th, box, use_graph)
         out = pipe.outputs()
         torch.cuda.synchronize()
+        st = pipe.stage_times()  # the stage events are recorded inside replayed graphs too
+        assert all(v >= 0 for v in st.values()) and st["neighbors"] > 0, st
         keys = O.sfc_keys(x, y, z, obox, 0, 64)
         sk, perm = O.sort_by_key(keys)
         if step == 0:
