@@ -418,4 +418,34 @@ struct Workspace
     }
 };
 
+// a device buffer that only grows (the pipeline and batch objects keep theirs across calls)
+struct DevBuf
+{
+    void* p      = nullptr;
+    size_t bytes = 0;
+    DevBuf()     = default;
+    DevBuf(const DevBuf&)            = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    int ensure(size_t need)
+    {
+        if (need <= bytes) return CS_OK;
+        if (p) cudaFree(p);
+        p     = nullptr;
+        bytes = 0;
+        size_t alloc = need + need / 8 + 256;
+        CSG_CUDA_TRY(cudaMalloc(&p, alloc));
+        bytes = alloc;
+        return CS_OK;
+    }
+    template<class T>
+    T* as() const
+    {
+        return static_cast<T*>(p);
+    }
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
 } // namespace csg

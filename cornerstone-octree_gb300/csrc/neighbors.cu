@@ -403,7 +403,7 @@ constexpr int NBG_STACK = 192;
 __device__ __noinline__ bool pairDecideF64(double xi, double yi, double zi, double r2, double cellR2, double kappa,
                                            const double* x, const double* y, const double* z, uint32_t j, int leafNode,
                                            const int32_t* parents, const double* centers, const double* sizes,
-                                           bool contained)
+                                           bool contained, int rootNode)
 {
     double dx = __dsub_rn(x[j], xi), dy = __dsub_rn(y[j], yi), dz = __dsub_rn(z[j], zi);
     double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
@@ -416,35 +416,37 @@ __device__ __noinline__ bool pairDecideF64(double xi, double yi, double zi, doub
     {
         if (!cellOverlapsExact<double>(xi, yi, zi, false, cellR2, centers + 3 * size_t(n), sizes + 3 * size_t(n), nb))
             return false;
-        if (n == 0) return true;
+        if (n <= rootNode) return true;
         n = parents[(n - 1) / 8];
     }
 }
 
 // the reference's cell tests on the path from a leaf to the root, exact in FP64 (no periodic axis)
 __device__ __noinline__ bool pathExactF64(double xi, double yi, double zi, double cellR2, int leafNode,
-                                          const int32_t* parents, const double* centers, const double* sizes)
+                                          const int32_t* parents, const double* centers, const double* sizes,
+                                          int rootNode)
 {
     BoxParams<double> nb{};
     for (int n = leafNode;;)
     {
         if (!cellOverlapsExact<double>(xi, yi, zi, false, cellR2, centers + 3 * size_t(n), sizes + 3 * size_t(n), nb))
             return false;
-        if (n == 0) return true;
+        if (n <= rootNode) return true;
         n = parents[(n - 1) / 8];
     }
 }
 
 // the reference's path condition for a float pair already known to be within r (T = float)
 __device__ __noinline__ bool pathCheckF32(float xi, float yi, float zi, float cellR2, int leafNode,
-                                          const int32_t* parents, const float* centers, const float* sizes)
+                                          const int32_t* parents, const float* centers, const float* sizes,
+                                          int rootNode)
 {
     BoxParams<float> nb{};
     for (int n = leafNode;;)
     {
         if (!cellOverlapsExact<float>(xi, yi, zi, false, cellR2, centers + 3 * size_t(n), sizes + 3 * size_t(n), nb))
             return false;
-        if (n == 0) return true;
+        if (n <= rootNode) return true;
         n = parents[(n - 1) / 8];
     }
 }
@@ -549,22 +551,36 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         Tout     = __fadd_ru(__fadd_ru(__fmul_ru(r2hi, 1.f + 24 * EPS), m), q);
     }
 
-    // ---- bounding box of the warp's search spheres, widened by the frame's rounding ----
-    float gc[3], gh[3];
-    {
+    // ---- the warp's group bounds, per pass over the lanes whose targets share a traversal root ----
+    // bounding box of the lanes' search spheres (widened by the frame's rounding), bounding sphere around its
+    // centre, largest radius; the first node of the traversal (0, or the root of the lanes' set)
+    float gc[3], gh[3], gR2 = 0.f, rmax = 0.f;
+    unsigned activeMask = 0;
+    int rootNode        = 0;
+    auto groupBounds = [&](bool inPass) {
         float rad = __fmul_ru(rr, 1.f + 64 * EPS);
 #pragma unroll
         for (int k = 0; k < 3; ++k)
         {
             float slack = __fmaf_ru(2 * EPS, fabsf(b[k]), delta);
-            float lo    = active ? __fsub_rd(__fsub_rd(b[k], rad), slack) : INFINITY;
-            float hi    = active ? __fadd_ru(__fadd_ru(b[k], rad), slack) : -INFINITY;
+            float lo    = inPass ? __fsub_rd(__fsub_rd(b[k], rad), slack) : INFINITY;
+            float hi    = inPass ? __fadd_ru(__fadd_ru(b[k], rad), slack) : -INFINITY;
             lo          = warpMinF(lo);
             hi          = warpMaxF(hi);
             gc[k]       = 0.5f * (lo + hi);
             gh[k]       = __fmul_ru(__fsub_ru(hi, lo), 0.5f);
         }
-    }
+        // group bounding sphere around the box centre gc: every point of every lane's sphere is within gR of gc, so
+        // it cuts the corners of the box (which matter where the density rises steeply, e.g. towards a Plummer core)
+        activeMask = __ballot_sync(0xffffffffu, inPass);
+        rmax       = warpMaxF(inPass ? rr : 0.f);
+        float e0 = b[0] - gc[0], e1 = b[1] - gc[1], e2 = b[2] - gc[2];
+        float dc = __fsqrt_ru(__fmaf_ru(e2, e2, __fmaf_ru(e1, e1, __fmul_ru(e0, e0))));
+        float sl = __fmaf_ru(2 * EPS, fmaxf(fabsf(b[0]), fmaxf(fabsf(b[1]), fabsf(b[2]))), delta);
+        float gr = inPass ? __fadd_ru(__fadd_ru(__fmul_ru(dc, 1.f + 8 * EPS), __fmul_ru(rr, 1.f + 64 * EPS)), sl) : 0.f;
+        gr       = warpMaxF(gr);
+        gR2      = __fmul_ru(gr, gr);
+    };
 
     const unsigned ngmax = a.ngmax;
     uint32_t* myNb       = a.nb + size_t(i - a.first) * ngmax;
@@ -624,7 +640,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             {
                 if constexpr (Stats) stExact++;
                 in = pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
-                                   a.centers, a.sizes, !outside);
+                                   a.centers, a.sizes, !outside, rootNode);
             }
         }
         else
@@ -635,7 +651,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                 if constexpr (Stats) stExact++;
                 in = pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
                                   reinterpret_cast<const float*>(a.centers),
-                                  reinterpret_cast<const float*>(a.sizes));
+                                  reinterpret_cast<const float*>(a.sizes), rootNode);
             }
         }
         return in && jj != i;
@@ -670,10 +686,10 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     auto decideSlow = [&](uint32_t jj, int node, bool contained) -> bool {
         if constexpr (F64)
             return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
-                                 a.centers, a.sizes, contained);
+                                 a.centers, a.sizes, contained, rootNode);
         else
             return pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
-                                reinterpret_cast<const float*>(a.centers), reinterpret_cast<const float*>(a.sizes));
+                                reinterpret_cast<const float*>(a.centers), reinterpret_cast<const float*>(a.sizes), rootNode);
     };
     // first filter: FP32 distance of the staged candidate; returns d2 and whether it can be a neighbour
     auto filter = [&](float4 c, float& d2) -> bool {
@@ -736,11 +752,11 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             if (!(n2u < tsafe))
             {
                 if constexpr (F64)
-                    leafPass = pathExactF64(xi, yi, zi, cellR2, node, a.parents, a.centers, a.sizes);
+                    leafPass = pathExactF64(xi, yi, zi, cellR2, node, a.parents, a.centers, a.sizes, rootNode);
                 else
                     leafPass = pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
                                             reinterpret_cast<const float*>(a.centers),
-                                            reinterpret_cast<const float*>(a.sizes));
+                                            reinterpret_cast<const float*>(a.sizes), rootNode);
             }
         }
         if constexpr (Stats)
@@ -896,38 +912,46 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
 
     // A warp whose targets are spread far apart (sparse regions, jumps of the curve) has a bounding box much larger
     // than its spheres; it then tests every child per lane against the lane's own sphere and carries the lanes that
-    // remain alive on the stack, as the per-particle traversal does, instead of using the box.
-    // group bounding sphere around the box centre gc: every point of every lane's sphere is within gR of gc, so it
-    // cuts the corners of the box (which matter where the density rises steeply, e.g. towards a Plummer core)
-    const unsigned activeMask = __ballot_sync(0xffffffffu, active);
-    float rmax                = warpMaxF(active ? rr : 0.f);
-    float gR2;
-    {
-        float e0 = b[0] - gc[0], e1 = b[1] - gc[1], e2 = b[2] - gc[2];
-        float dc = __fsqrt_ru(__fmaf_ru(e2, e2, __fmaf_ru(e1, e1, __fmul_ru(e0, e0))));
-        float sl = __fmaf_ru(2 * EPS, fmaxf(fabsf(b[0]), fmaxf(fabsf(b[1]), fabsf(b[2]))), delta);
-        float gr = active ? __fadd_ru(__fadd_ru(__fmul_ru(dc, 1.f + 8 * EPS), __fmul_ru(rr, 1.f + 64 * EPS)), sl) : 0.f;
-        gr       = warpMaxF(gr);
-        gR2      = __fmul_ru(gr, gr);
-    }
-    // a warp whose targets are spread over more than a few radii tests children per lane (see below); so does a
-    // warp whose group bounds turn out to enclose many more nodes than its spheres (it switches after
-    // LOOSE_AFTER expansions, several times what a compact warp needs)
-    bool loose                 = __fsqrt_ru(gR2) > 3.f * rmax;
-    constexpr int LOOSE_AFTER  = 96;
-    int expansions             = 0;
+    // remain alive on the stack, as the per-particle traversal does, instead of using the box. So does a warp whose
+    // group bounds turn out to enclose many more nodes than its spheres (after LOOSE_AFTER expansions, several times
+    // what a compact warp needs).
+    constexpr int LOOSE_AFTER = 96;
+    bool loose                = false;
+    int expansions            = 0;
     long long t0              = Stats ? clock64() : 0;
     float rminW               = Stats ? warpMinF(active ? rr : INFINITY) : 0.f;
+    int* stack                = sStack[warp];
+    unsigned* maskStack       = sMaskStack[warp];
 
-    int* stack          = sStack[warp];
-    unsigned* maskStack = sMaskStack[warp];
-    int top             = 0;
+    // one pass per set among the warp's targets (batched trees; a single pass otherwise)
+    int mySet = 0, passSet = 0, lastSet = 0;
+    if (a.numSets)
+    {
+        int lo = 0, hi = a.numSets;
+        while (lo + 1 < hi)
+        {
+            int mid = (lo + hi) >> 1;
+            if (__ldg(a.setOffsets + mid) <= i) lo = mid;
+            else hi = mid;
+        }
+        mySet   = lo;
+        passSet = __reduce_min_sync(0xffffffffu, active ? unsigned(mySet) : 0xffffffffu);
+        lastSet = int(__reduce_max_sync(0xffffffffu, active ? unsigned(mySet) : 0u));
+    }
+    for (;; ++passSet)
+    {
+    const bool inPass = active && (!a.numSets || mySet == passSet);
+    groupBounds(inPass);
+    rootNode   = a.numSets ? __ldg(a.setRoots + passSet) : 0;
+    loose      = __fsqrt_ru(gR2) > 3.f * rmax;
+    expansions = 0;
+    int top    = 0;
     if (lane == 0)
     {
-        stack[0]     = 0;
+        stack[0]     = rootNode;
         maskStack[0] = activeMask;
     }
-    top = 1;
+    top = activeMask ? 1 : 0;
     __syncwarp();
     while (top > 0)
     {
@@ -998,6 +1022,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         top += __popc(m);
         __syncwarp();
     }
+    if (!a.numSets || passSet >= lastSet) break;
+    } // passes
     if (active && s == 0) a.nc[i - a.first] = nc;
     if constexpr (Stats)
     {

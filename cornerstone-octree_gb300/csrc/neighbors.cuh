@@ -32,6 +32,11 @@ struct NbArgs
     uint32_t* errWord = nullptr;
     //! targets per warp of the group traversal (8, 16 or 32)
     int groupSize = 32;
+    //! many independent sets in one tree (may be null): the sorted particles of set s are [setOffsets[s],
+    //! setOffsets[s + 1]) and its traversal starts at node setRoots[s] instead of the root
+    const uint32_t* setOffsets = nullptr;
+    const int32_t* setRoots    = nullptr;
+    int numSets                = 0;
 };
 
 //! float shadows for the FP64 pre-filter: particles x = hi + lo (two floats), and one record of three float4 per node

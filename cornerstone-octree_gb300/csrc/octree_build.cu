@@ -124,14 +124,30 @@ __device__ __forceinline__ unsigned log8ceil32(unsigned v)
     return 10u - (lz - 2u) / 3u;
 }
 
+// per-set buckets and the merge floor of a batched tree (BatchTree); numSets = 0: one tree, the build's bucket
+struct SetRules
+{
+    const uint32_t* setBucket = nullptr;
+    int setShift              = 0;
+    int numSets               = 0;
+    unsigned minMergeLevel    = 0;
+};
+
 // calculateNodeOp with siblingAndLevel (tree/csarray.hpp:250-290); cnt(i) gives the (capped) leaf count
 template<class K, class CountFn>
-__device__ __forceinline__ int nodeOp(const K* tree, int i, unsigned bucket, CountFn cnt)
+__device__ __forceinline__ int nodeOp(const K* tree, int i, unsigned bucketAll, CountFn cnt, const SetRules& sr = {})
 {
     K node         = ldcg(tree + i);
     unsigned level = treeLevel<K>(ldcg(tree + i + 1) - node);
-    int sib        = -1;
-    if (level > 0)
+    unsigned long long bucket = bucketAll;
+    if (sr.numSets)
+    {
+        // the set's own bucket; filler nodes past the last set never change (empty, never merged)
+        K set  = node >> sr.setShift;
+        bucket = set < K(sr.numSets) ? (unsigned long long)__ldg(sr.setBucket + set) : ~0ull;
+    }
+    int sib = -1;
+    if (level > sr.minMergeLevel)
     {
         sib = int(octalDigit<K>(node, level));
         if (ldcg(tree + i - sib + 8) != ldcg(tree + i - sib) + nodeRange<K>(level - 1)) sib = -1;
@@ -142,10 +158,10 @@ __device__ __forceinline__ int nodeOp(const K* tree, int i, unsigned bucket, Cou
 #pragma unroll
         for (int s = 0; s < 8; ++s)
             parent += cnt(i - sib + s);
-        if (parent <= (unsigned long long)bucket) return 0;
+        if (parent <= bucket) return 0;
     }
     constexpr unsigned L = KeyTraits<K>::maxLevel;
-    unsigned c           = cnt(i);
+    unsigned long long c = cnt(i);
     if (c > bucket * 512u && level + 3 < L) return 4096;
     if (c > bucket * 64u && level + 2 < L) return 512;
     if (c > bucket * 8u && level + 1 < L) return 64;
@@ -222,6 +238,8 @@ struct BuildArgs
     const uint32_t* countsIn; // UPDATE
     int Lin;                  // UPDATE
     const int* LinDev;        // UPDATE: the input leaf count in device memory (replaces Lin when set)
+    int initL;                // BUILD from a given leaf array (batched sets): its leaf count, 0 = from the root
+    SetRules rules;
     // outputs
     K* treeOut;
     uint32_t* countsOut;
@@ -240,9 +258,9 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
     const unsigned tid = threadIdx.x;
     BuildState* st     = a.st;
 
-    int L   = a.updateMode ? (a.LinDev ? *a.LinDev : a.Lin) : 1;
+    int L   = a.updateMode ? (a.LinDev ? *a.LinDev : a.Lin) : (a.initL ? a.initL : 1);
     int cur = 0;
-    if (!a.updateMode && b == 0 && tid == 0)
+    if (!a.updateMode && !a.initL && b == 0 && tid == 0)
     {
         a.tree[0][0] = 0;
         a.tree[0][1] = nodeRange<K>(0);
@@ -273,7 +291,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
             if (a.updateMode)
             {
                 const uint32_t* cin = a.countsIn;
-                op = nodeOp<K>(tr, i, a.bucket, [cin](int j) { return __ldg(cin + j); });
+                op = nodeOp<K>(tr, i, a.bucket, [cin](int j) { return __ldg(cin + j); }, a.rules);
                 csum += __ldg(cin + i);
             }
             else
@@ -281,10 +299,13 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
                 // computeOctree seeds the root with the uncapped key count (tree/csarray.hpp:433-434); every later
                 // count is capped at maxCount as computeNodeCounts does
                 uint32_t mc = iter == 0 ? 0xffffffffu : a.maxCount;
-                op = nodeOp<K>(tr, i, a.bucket, [of, mc](int j) {
-                    uint32_t c = ldcg(of + j + 1) - ldcg(of + j);
-                    return c < mc ? c : mc;
-                });
+                op = nodeOp<K>(
+                    tr, i, a.bucket,
+                    [of, mc](int j) {
+                        uint32_t c = ldcg(of + j + 1) - ldcg(of + j);
+                        return c < mc ? c : mc;
+                    },
+                    a.rules);
             }
             a.ops[i] = op;
             sum += op;
@@ -572,9 +593,15 @@ size_t octreeBuildWorkspaceBytes(int capacity, bool update)
 template<class K>
 int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32_t maxCount, const K* treeIn,
                 const uint32_t* countsIn, int Lin, K* treeOut, uint32_t* countsOut, uint32_t* layoutOut, int capacity,
-                void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus, const int* LinDev)
+                void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus, const int* LinDev,
+                const BatchTree<K>* batch)
 {
     bool update = treeIn != nullptr;
+    if (batch && (update || batch->initL < 1 || batch->initL > capacity || !batch->initTree || !batch->initOff))
+    {
+        setLastError("octree: invalid batched start (leaves %d, capacity %d)", batch ? batch->initL : 0, capacity);
+        return CS_ERR_INVALID;
+    }
     if (bucket == 0)
     {
         setLastError("octree: bucket size must be positive");
@@ -605,6 +632,14 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
         CSG_CUDA_TRY(cudaMemcpyAsync(l.tree[0], treeIn, keysIn * sizeof(K), cudaMemcpyDeviceToDevice, s));
     }
 
+    if (batch)
+    {
+        CSG_CUDA_TRY(cudaMemcpyAsync(l.tree[0], batch->initTree, (size_t(batch->initL) + 1) * sizeof(K),
+                                     cudaMemcpyDeviceToDevice, s));
+        CSG_CUDA_TRY(cudaMemcpyAsync(l.off[0], batch->initOff, (size_t(batch->initL) + 1) * sizeof(uint32_t),
+                                     cudaMemcpyDeviceToDevice, s));
+    }
+
     int G = buildGridSize();
     BuildArgs<K> a;
     a.keys       = keys;
@@ -624,6 +659,9 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
     a.countsIn   = countsIn;
     a.Lin        = Lin;
     a.LinDev     = LinDev;
+    a.initL      = batch ? batch->initL : 0;
+    a.rules      = batch ? SetRules{batch->setBucket, batch->setShift, batch->numSets, unsigned(batch->minMergeLevel)}
+                         : SetRules{};
     a.treeOut    = treeOut;
     a.countsOut  = countsOut;
     a.layoutOut  = layoutOut;
@@ -709,10 +747,10 @@ template size_t octreeBuildWorkspaceBytes<uint32_t>(int, bool);
 template size_t octreeBuildWorkspaceBytes<uint64_t>(int, bool);
 template int octreeBuild<uint32_t>(cudaStream_t, const uint32_t*, size_t, unsigned, uint32_t, const uint32_t*,
                                    const uint32_t*, int, uint32_t*, uint32_t*, uint32_t*, int, void*, size_t,
-                                   BuildResult*, bool, FocusQuery<uint32_t>, const int*);
+                                   BuildResult*, bool, FocusQuery<uint32_t>, const int*, const BatchTree<uint32_t>*);
 template int octreeBuild<uint64_t>(cudaStream_t, const uint64_t*, size_t, unsigned, uint32_t, const uint64_t*,
                                    const uint32_t*, int, uint64_t*, uint32_t*, uint32_t*, int, void*, size_t,
-                                   BuildResult*, bool, FocusQuery<uint64_t>, const int*);
+                                   BuildResult*, bool, FocusQuery<uint64_t>, const int*, const BatchTree<uint64_t>*);
 
 // ---------------------------------------------------------------------------------------------------------------
 // standalone counts and decisions

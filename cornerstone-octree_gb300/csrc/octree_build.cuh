@@ -35,11 +35,27 @@ size_t octreeBuildWorkspaceBytes(int capacity, bool update);
 
 /*! Build (treeIn == nullptr: computeOctree from the root) or update (one updateOctree step from treeIn/countsIn).
  *  With sync == false the call only enqueues work; the state block (see BuildResult::stateDev) holds the outcome. */
+//! many independent sets in one tree: set s owns the key range [s << setShift, (s + 1) << setShift) (an aligned
+//! subtree rooted at level minMergeLevel), uses bucket size setBucket[s], and no node at or above minMergeLevel is
+//! merged; the build starts from initTree (set roots and empty filler nodes, initL leaves) with particle offsets
+//! initOff instead of the root
+template<class K>
+struct BatchTree
+{
+    const K* initTree           = nullptr;
+    const uint32_t* initOff     = nullptr;
+    int initL                   = 0;
+    const uint32_t* setBucket   = nullptr;
+    int setShift                = 0;
+    int numSets                 = 0;
+    int minMergeLevel           = 0;
+};
+
 template<class K>
 int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32_t maxCount, const K* treeIn,
                 const uint32_t* countsIn, int Lin, K* treeOut, uint32_t* countsOut, uint32_t* layoutOut, int capacity,
                 void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus = FocusQuery<K>{},
-                const int* LinDev = nullptr);
+                const int* LinDev = nullptr, const BatchTree<K>* batch = nullptr);
 
 /*! after an octreeBuild with sync = false (e.g. replayed from a CUDA graph): read its state block from the same
  *  workspace, synchronise, fill res and map the device error bits to a status, as the sync path does */

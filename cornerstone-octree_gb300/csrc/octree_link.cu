@@ -10,6 +10,8 @@
 #include "octree_link.cuh"
 #include "radix_sort.cuh"
 
+#include <vector>
+
 namespace csg
 {
 
@@ -271,6 +273,92 @@ int geoCenters(cudaStream_t s, const K* prefixes, int N, T* centers, T* sizes, c
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }
+
+// batched sets in one 64-bit tree: node key = (set << 30) | the set's 32-bit key, set roots at level rootLevel; every
+// node at or below a set root gets the geometry the set's own 32-bit tree gives it (its box, its levels); the nodes
+// above the set roots and the empty filler nodes get a zero box (never traversed)
+template<class T, int Kind>
+__global__ void geoCentersBatchKernel(const uint64_t* __restrict__ prefixes, int N, T* __restrict__ centers,
+                                      T* __restrict__ sizes, const GeoParams<T>* __restrict__ sets, int numSets,
+                                      unsigned rootLevel)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    uint64_t prefix = prefixes[i];
+    uint64_t start  = decodePlaceholderBit<uint64_t>(prefix);
+    unsigned level  = decodePrefixLength<uint64_t>(prefix) / 3;
+    uint64_t set    = start >> 30;
+    if (level < rootLevel || set >= uint64_t(numSets))
+    {
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            centers[3 * size_t(i) + k] = sizes[3 * size_t(i) + k] = T(0);
+        return;
+    }
+    const uint32_t rel = uint32_t(start & ((uint64_t(1) << 30) - 1));
+    unsigned cube      = (1u << KeyTraits<uint32_t>::maxLevel) >> (level - rootLevel);
+    unsigned ix, iy, iz;
+    if (Kind == CS_HILBERT)
+    {
+        decodeHilbert<uint32_t>(rel, ix, iy, iz);
+        unsigned mask = ~(cube - 1u);
+        ix &= mask;
+        iy &= mask;
+        iz &= mask;
+    }
+    else { decodeMorton<uint32_t>(rel, ix, iy, iz); }
+    const GeoParams<T> g = sets[set];
+    unsigned imin[3]     = {ix, iy, iz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        int a0                     = int(imin[k]);
+        int b0                     = a0 + int(cube);
+        centers[3 * size_t(i) + k] = RN<T>::add(g.lo[k], RN<T>::mul(T(b0 + a0), g.half[k]));
+        sizes[3 * size_t(i) + k]   = RN<T>::mul(T(b0 - a0), g.half[k]);
+    }
+}
+
+template<class T>
+size_t geoParamsBytes(int numSets)
+{
+    return size_t(numSets) * sizeof(GeoParams<T>) + 256;
+}
+
+template<class T>
+int geoCentersBatched(cudaStream_t s, const uint64_t* prefixes, int N, T* centers, T* sizes, const cs_box* boxes,
+                      int numSets, int kind, void* paramsDev, unsigned rootLevel)
+{
+    if (N <= 0) return CS_OK;
+    std::vector<GeoParams<T>> g(numSets);
+    const T uL = T(1) / T(int(1u << KeyTraits<uint32_t>::maxLevel));
+    for (int j = 0; j < numSets; ++j)
+    {
+        auto bp = makeBoxParams<T>(boxes[j]);
+        for (int k = 0; k < 3; ++k)
+        {
+            g[j].lo[k]   = bp.lo[k];
+            g[j].half[k] = T(0.5) * uL * bp.len[k];
+        }
+    }
+    auto* gd = static_cast<GeoParams<T>*>(paramsDev);
+    CSG_CUDA_TRY(cudaMemcpyAsync(gd, g.data(), g.size() * sizeof(GeoParams<T>), cudaMemcpyHostToDevice, s));
+    if (kind == CS_HILBERT)
+        geoCentersBatchKernel<T, CS_HILBERT><<<iceil(N, 256), 256, 0, s>>>(prefixes, N, centers, sizes, gd, numSets,
+                                                                           rootLevel);
+    else
+        geoCentersBatchKernel<T, CS_MORTON><<<iceil(N, 256), 256, 0, s>>>(prefixes, N, centers, sizes, gd, numSets,
+                                                                          rootLevel);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template size_t geoParamsBytes<float>(int);
+template size_t geoParamsBytes<double>(int);
+template int geoCentersBatched<float>(cudaStream_t, const uint64_t*, int, float*, float*, const cs_box*, int, int,
+                                      void*, unsigned);
+template int geoCentersBatched<double>(cudaStream_t, const uint64_t*, int, double*, double*, const cs_box*, int, int,
+                                       void*, unsigned);
 
 template int geoCenters<uint32_t, float>(cudaStream_t, const uint32_t*, int, float*, float*, const cs_box&, int,
                                          const int*);

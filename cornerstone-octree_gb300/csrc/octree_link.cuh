@@ -22,4 +22,13 @@ template<class K, class T>
 int geoCenters(cudaStream_t s, const K* prefixes, int N, T* centers, T* sizes, const cs_box& box, int kind,
                const int* Ldev = nullptr);
 
+//! node geometry of batched sets in one 64-bit tree (keys (s << 30) | 32-bit key of set s, set roots at rootLevel):
+//! every node of a set's subtree gets the centre and half size its set's own 32-bit tree gives it, with the set's
+//! box; paramsDev holds geoParamsBytes(numSets) of device memory
+template<class T>
+size_t geoParamsBytes(int numSets);
+template<class T>
+int geoCentersBatched(cudaStream_t s, const uint64_t* prefixes, int N, T* centers, T* sizes, const cs_box* boxes,
+                      int numSets, int kind, void* paramsDev, unsigned rootLevel);
+
 } // namespace csg

@@ -21,32 +21,6 @@
 namespace csg
 {
 
-struct DevBuf
-{
-    void* p      = nullptr;
-    size_t bytes = 0;
-    int ensure(size_t need)
-    {
-        if (need <= bytes) return CS_OK;
-        if (p) cudaFree(p);
-        p     = nullptr;
-        bytes = 0;
-        size_t alloc = need + need / 8 + 256;
-        CSG_CUDA_TRY(cudaMalloc(&p, alloc));
-        bytes = alloc;
-        return CS_OK;
-    }
-    template<class T>
-    T* as() const
-    {
-        return static_cast<T*>(p);
-    }
-    ~DevBuf()
-    {
-        if (p) cudaFree(p);
-    }
-};
-
 enum Stage
 {
     ST_KEYS,

@@ -166,6 +166,58 @@ template int sfcKeysPacked(cudaStream_t, const float*, const float*, const float
 template int sfcKeysPacked(cudaStream_t, const double*, const double*, const double*, const double*, uint64_t*,
                            double4_32a*, size_t, const cs_box&, int);
 
+template<class T, int Kind>
+__global__ void __launch_bounds__(256)
+    sfcKeysBatchKernel(const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z,
+                       const T* __restrict__ h, size_t n, const uint32_t* __restrict__ setOffsets, int numSets,
+                       const KeyParams<T, uint32_t>* __restrict__ kps, uint64_t* __restrict__ keys,
+                       PackedT<T>* __restrict__ packed)
+{
+    size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        // the set holding particle i: last s with setOffsets[s] <= i
+        int lo = 0, hi = numSets;
+        while (lo + 1 < hi)
+        {
+            int mid = (lo + hi) >> 1;
+            if (__ldg(setOffsets + mid) <= i) lo = mid;
+            else hi = mid;
+        }
+        T px = __ldcs(x + i), py = __ldcs(y + i), pz = __ldcs(z + i), ph = __ldcs(h + i);
+        uint32_t k = sfc3D<T, uint32_t>(px, py, pz, kps[lo], Kind);
+        keys[i]    = (uint64_t(lo) << 30) | uint64_t(k);
+        PackedT<T> r;
+        r.x       = px;
+        r.y       = py;
+        r.z       = pz;
+        r.w       = ph;
+        packed[i] = r;
+    }
+}
+
+template<class T>
+int sfcKeysBatched(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, size_t n, const uint32_t* setOffsets,
+                   int numSets, const KeyParams<T, uint32_t>* kps, int kind, uint64_t* keys, PackedT<T>* packed)
+{
+    if (n == 0) return CS_OK;
+    unsigned thr  = 256;
+    size_t blocks = (n + thr - 1) / thr;
+    unsigned grid = unsigned(blocks < size_t(smCount()) * 16 ? blocks : size_t(smCount()) * 16);
+    if (kind == CS_HILBERT)
+        sfcKeysBatchKernel<T, CS_HILBERT><<<grid, thr, 0, s>>>(x, y, z, h, n, setOffsets, numSets, kps, keys, packed);
+    else
+        sfcKeysBatchKernel<T, CS_MORTON><<<grid, thr, 0, s>>>(x, y, z, h, n, setOffsets, numSets, kps, keys, packed);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
+template int sfcKeysBatched<float>(cudaStream_t, const float*, const float*, const float*, const float*, size_t,
+                                   const uint32_t*, int, const KeyParams<float, uint32_t>*, int, uint64_t*, float4*);
+template int sfcKeysBatched<double>(cudaStream_t, const double*, const double*, const double*, const double*, size_t,
+                                    const uint32_t*, int, const KeyParams<double, uint32_t>*, int, uint64_t*,
+                                    double4_32a*);
+
 template<class T, bool Shadow>
 __global__ void __launch_bounds__(256) gatherPackedKernel(const uint32_t* __restrict__ perm, size_t n,
                                                           const PackedT<T>* __restrict__ packed, T* __restrict__ xs,

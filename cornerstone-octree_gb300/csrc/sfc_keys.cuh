@@ -35,6 +35,13 @@ struct Packed<double>
 template<class T>
 using PackedT = typename Packed<T>::type;
 
+//! many independent sets: set s holds input particles [setOffsets[s], setOffsets[s + 1]) and its own box (kps[s]);
+//! keys[i] = (s << 30) | the set's 32-bit key of particle i, so one sort of the combined keys sorts every set by its
+//! own key and keeps the sets apart; the particles are packed as in sfcKeysPacked
+template<class T>
+int sfcKeysBatched(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, size_t n, const uint32_t* setOffsets,
+                   int numSets, const KeyParams<T, uint32_t>* kps, int kind, uint64_t* keys, PackedT<T>* packed);
+
 //! keys as sfcKeys (no removeKey entries), and the particles packed into one record each
 template<class T, class K>
 int sfcKeysPacked(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, K* keys, PackedT<T>* packed,

@@ -422,6 +422,80 @@ class Pipeline:
         return out
 
 
+# ---------------------------------------------------------------------------------------------------------------
+# many independent sets (cs_batch_*)
+# ---------------------------------------------------------------------------------------------------------------
+
+class BatchConfig(C.Structure):
+    _fields_ = [("coord_bits", C.c_int), ("sfc_kind", C.c_int), ("ngmax", C.c_uint), ("search_ext", C.c_float),
+                ("do_neighbors", C.c_int)]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [("num_sets", C.c_int32), ("num_leaves", C.c_int32), ("num_nodes", C.c_int32),
+                ("iterations", C.c_int32), ("num_particles", C.c_uint64)]
+
+
+class BatchOutputs(C.Structure):
+    _fields_ = [("order", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p), ("h", C.c_void_p),
+                ("leaves", C.c_void_p), ("counts", C.c_void_p), ("layout", C.c_void_p),
+                ("set_leaf_begin", C.c_void_p), ("set_roots", C.c_void_p), ("set_offsets", C.c_void_p),
+                ("octree", OctreeView), ("centers", C.c_void_p), ("sizes", C.c_void_p), ("neighbors", C.c_void_p),
+                ("neighbor_counts", C.c_void_p)]
+
+
+lib.cs_batch_device_bytes.restype = C.c_size_t
+lib.cs_batch_device_bytes.argtypes = [C.c_void_p]
+
+
+class Batch:
+    """many independent sets: keys -> segmented sort -> one build of every set -> link -> geometry -> neighbours"""
+
+    def __init__(self, coord_bits=32, kind=MORTON, ngmax=100, search_ext=1.0, do_neighbors=True):
+        self.cfg = BatchConfig(coord_bits, kind, ngmax, search_ext, int(do_neighbors))
+        self.coord_bits = coord_bits
+        self.handle = C.c_void_p()
+        _check(lib.cs_batch_create(C.byref(self.handle), C.byref(self.cfg)))
+        self.result = BatchResult()
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            lib.cs_batch_destroy(self.handle)
+            self.handle = None
+
+    def run(self, x, y, z, h, offsets, boxes, buckets):
+        """x..h: device tensors of all sets concatenated; offsets: S + 1 ints; boxes: S cs_box; buckets: S ints"""
+        S = len(boxes)
+        off = (C.c_uint32 * (S + 1))(*[int(v) for v in offsets])
+        bx = (Box * S)(*boxes)
+        bk = (C.c_uint32 * S)(*[int(v) for v in buckets])
+        _check(lib.cs_batch_run(self.handle, _stream(), _p(x), _p(y), _p(z), _p(h), off, S, bx, bk,
+                                C.byref(self.result)))
+        return self.result
+
+    def device_bytes(self):
+        return lib.cs_batch_device_bytes(self.handle)
+
+    def outputs(self):
+        """torch views of the device results of the last run (no copies)"""
+        o = BatchOutputs()
+        _check(lib.cs_batch_get_outputs(self.handle, C.byref(o)))
+        r = self.result
+        n, L, N, S = int(r.num_particles), r.num_leaves, r.num_nodes, r.num_sets
+        tdt = torch.float64 if self.coord_bits == 64 else torch.float32
+        out = dict(order=_wrap(o.order, n, torch.int32), x=_wrap(o.x, n, tdt), y=_wrap(o.y, n, tdt),
+                   z=_wrap(o.z, n, tdt), h=_wrap(o.h, n, tdt), leaves=_wrap(o.leaves, L + 1, torch.int64),
+                   counts=_wrap(o.counts, L, torch.int32), layout=_wrap(o.layout, L + 1, torch.int32),
+                   set_leaf_begin=_wrap(o.set_leaf_begin, S + 1, torch.int32),
+                   set_roots=_wrap(o.set_roots, S, torch.int32), set_offsets=_wrap(o.set_offsets, S + 1, torch.int32),
+                   prefixes=_wrap(o.octree.prefixes, N, torch.int64),
+                   centers=_wrap(o.centers, 3 * N, tdt).view(N, 3), sizes=_wrap(o.sizes, 3 * N, tdt).view(N, 3),
+                   neighbor_counts=_wrap(o.neighbor_counts, n, torch.int32))
+        if o.neighbors:
+            out["neighbors"] = _wrap(o.neighbors, n * self.cfg.ngmax, torch.int32).view(n, self.cfg.ngmax)
+        return out
+
+
 def _wrap(ptr, count, dtype):
     """non-owning torch view of device memory held by the library"""
     if count == 0 or not ptr:

@@ -369,6 +369,56 @@ int cs_pipeline_graph_replays(cs_pipeline p);
  * run to finish */
 int cs_pipeline_stage_times(cs_pipeline p, float* ms, int count);
 
+/* ---- batched independent sets ----------------------------------------------------------------------------------
+ * No counterpart call in the reference, which builds one tree per call: many independent particle sets of uneven size
+ * go through keys -> sort -> build -> link -> geometry -> neighbours in one sequence of launches, with results equal
+ * to running each set on its own through cs_pipeline_run (same coordinate type, 32-bit keys of the given curve, the
+ * set's bucket size, ngmax, no halos). Each set's 32-bit key is combined with its index into one 64-bit key
+ * (set << 30) | key, so one stable sort orders every set and keeps them apart, and one cooperative cornerstone build
+ * over the combined keys builds every set's tree at once: each set is the subtree rooted at level 11, with its own
+ * bucket size and no merge at or above that level; the neighbour traversal of a particle starts at its set's root.
+ * Sets may be empty; the total is below 2^30 particles. Inputs are device arrays of all sets concatenated; the set
+ * offsets (num_sets + 1), boxes and bucket sizes are host arrays. */
+typedef struct cs_batch_s* cs_batch;
+typedef struct
+{
+    int coord_bits;   /* 32 or 64 */
+    int sfc_kind;     /* CS_MORTON or CS_HILBERT (32-bit keys per set; geometry decoded with the same curve) */
+    unsigned ngmax;   /* stored neighbours per particle */
+    float search_ext; /* searchExtFactor of the neighbour search */
+    int do_neighbors;
+} cs_batch_config;
+typedef struct
+{
+    int32_t num_sets;
+    int32_t num_leaves; /* of the combined tree, over all sets (+ a few empty filler leaves) */
+    int32_t num_nodes;
+    int32_t iterations; /* rebalance iterations until every set converged */
+    uint64_t num_particles;
+} cs_batch_result;
+typedef struct
+{
+    const uint32_t* order;           /* sorted position -> input position (over all sets) */
+    const void *x, *y, *z, *h;       /* sorted coordinates and h; set s occupies [set_offsets[s], set_offsets[s+1]) */
+    const uint64_t* leaves;          /* combined leaf keys, num_leaves + 1 */
+    const uint32_t* counts;          /* particles per leaf */
+    const uint32_t* layout;          /* first sorted particle of each leaf, num_leaves + 1 */
+    const int32_t* set_leaf_begin;   /* set s owns leaves [set_leaf_begin[s], set_leaf_begin[s+1]), num_sets + 1 */
+    const int32_t* set_roots;        /* node index of each set's root in the combined tree */
+    const uint32_t* set_offsets;     /* device copy of the set offsets */
+    cs_octree_view octree;           /* the combined tree (uint64_t prefixes) */
+    const void *centers, *sizes;     /* per node, with each set's box */
+    const uint32_t* neighbors;       /* num_particles x ngmax, sorted positions over all sets */
+    const uint32_t* neighbor_counts; /* uncapped counts */
+} cs_batch_outputs;
+int cs_batch_create(cs_batch* out, const cs_batch_config* cfg);
+int cs_batch_destroy(cs_batch b);
+int cs_batch_run(cs_batch b, cs_stream_t stream, const void* x, const void* y, const void* z, const void* h,
+                 const uint32_t* set_offsets_host, int32_t num_sets, const cs_box* boxes_host,
+                 const uint32_t* buckets_host, cs_batch_result* result);
+int cs_batch_get_outputs(cs_batch b, cs_batch_outputs* out);
+size_t cs_batch_device_bytes(cs_batch b);
+
 #ifdef __cplusplus
 }
 #endif
