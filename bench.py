@@ -44,9 +44,11 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=None, help="particles (default 16M plummer, 64M incremental)")
-    p.add_argument("--workload", default="plummer", choices=["plummer", "incremental"],
+    p.add_argument("--sets", type=int, default=4096, help="sets of the batched workload")
+    p.add_argument("--workload", default="plummer", choices=["plummer", "incremental", "batched"],
                    help="plummer: the 16M keys->neighbours pass (default); incremental: 64M FP32 time steps with one "
-                        "updateOctree step each, replayed from CUDA graphs")
+                        "updateOctree step each, replayed from CUDA graphs; batched: 4096 uneven FP32 sets in "
+                        "one batched run per chunk against a per-set loop of the single-set pipeline")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=1 << 20, help="particles of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -297,6 +299,101 @@ def run_incremental(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_batched(args, world, rank, local):
+    """4096 independent FP32 sets, sizes log-uniform in [2^10, 2^20], uniform or Plummer (50/50), Morton32 keys,
+    bucket sizes from {16, 32, 64}, per-set constant h for about 60 neighbours, ngmax 100: the batched path (one run
+    per chunk of at most 64M particles, bounded by the neighbour lists' memory) against a per-set loop of the
+    single-set pipeline on the same device-resident sets. Reports sets/s of both and whether every set's neighbour
+    counts agree."""
+    import numpy as np
+    import torch
+
+    import cstone_gb300 as cs
+    from cstone_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ngmax = 100
+    sets = W.batched_sets(args.sets, args.seed + rank, dev)
+    total = sum(st["n"] for st in sets)
+    chunk_cap = 64 * 1024 * 1024
+    chunks, cur, acc = [], [], 0
+    for st in sets:
+        if cur and acc + st["n"] > chunk_cap:
+            chunks.append(cur)
+            cur, acc = [], 0
+        cur.append(st)
+        acc += st["n"]
+    chunks.append(cur)
+    packed = []
+    for ch in chunks:
+        offs = np.concatenate([[0], np.cumsum([st["n"] for st in ch])])
+        xyzh = [torch.cat([st[c] for st in ch]) for c in "xyzh"]
+        packed.append((offs, xyzh, [cs.make_box(st["lo"], st["hi"]) for st in ch], [st["bucket"] for st in ch]))
+    torch.cuda.synchronize()
+
+    batch = cs.Batch(32, cs.MORTON, ngmax)
+
+    def batched_pass():
+        for offs, (x, y, z, h), boxes, buckets in packed:
+            batch.run(x, y, z, h, offs, boxes, buckets)
+
+    pipes = {b: cs.Pipeline(32, 32, cs.MORTON, b, ngmax, 1.0, 1.0, False, True) for b in (16, 32, 64)}
+
+    def per_set_pass(check=False):
+        bad = 0
+        for ci, (offs, (x, y, z, h), boxes, buckets) in enumerate(packed):
+            if check:
+                batch.run(x, y, z, h, offs, boxes, buckets)
+                bnc = batch.outputs()["neighbor_counts"]
+            for j in range(len(buckets)):
+                a, e = int(offs[j]), int(offs[j + 1])
+                if e == a:
+                    continue
+                pipe = pipes[buckets[j]]
+                pipe.run(x[a:e], y[a:e], z[a:e], h[a:e], boxes[j])
+                if check:
+                    pnc = pipe.outputs()["neighbor_counts"]
+                    bad += int(not torch.equal(pnc, bnc[a:e]))
+        return bad
+
+    steps = max(1, min(args.steps, 3))
+    batched_pass()  # warm-up: buffers sized by the largest chunk
+    per_set_pass()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            batched_pass()
+        torch.cuda.synchronize()
+        tb = (time.perf_counter() - t0) / steps
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            per_set_pass()
+        torch.cuda.synchronize()
+        tp = (time.perf_counter() - t0) / steps
+        barrier(world)
+    mismatched = per_set_pass(check=True)
+    tb = max_over_ranks(tb, world)
+    if rank == 0:
+        line = {"metric": "sets/s batched (4096 uneven FP32 sets, Morton32, build + neighbours)",
+                "value": round(world * args.sets / tb, 3), "unit": "sets/s", "n_gpus": world, "steps": steps,
+                "warmup": 1, "ms_per_step": round(tb * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "batched-sets", "sets": args.sets, "particles": total,
+                           "sizes": "log-uniform [2^10, 2^20]", "mix": "uniform / Plummer 50/50",
+                           "keys": "morton32", "buckets": "{16, 32, 64}", "ngmax": ngmax, "neighbours": "about 60",
+                           "chunks": len(chunks), "chunk_particles_max": chunk_cap,
+                           "parallelism": f"replicas x{world}"},
+                "particles_per_s": round(total / tb / 1e6, 3),
+                "per_set_loop": {"sets_per_s": round(args.sets / tp, 3), "ms_per_pass": round(tp * 1e3, 3),
+                                 "particles_per_s_M": round(total / tp / 1e6, 3)},
+                "identical_neighbor_counts": mismatched == 0, "mismatched_sets": mismatched,
+                "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -305,6 +402,9 @@ def main():
         return
     if args.workload == "incremental":
         run_incremental(args, world, rank, local)
+        return
+    if args.workload == "batched":
+        run_batched(args, world, rank, local)
         return
 
     import numpy as np

@@ -45,6 +45,49 @@ def plummer(n, seed, rmax=100.0):
     return x - x.mean(), y - y.mean(), z - z.mean()
 
 
+def batched_sets(num_sets, seed, device, lo_exp=10, hi_exp=20, k=60):
+    """The batched workload: num_sets independent FP32 sets, sizes n_s = floor(2^(lo_exp + (hi_exp - lo_exp) u))
+    (log-uniform), uniform in the unit cube or Plummer with a tight box (alternating 50/50), bucket sizes drawn from
+    {16, 32, 64}, per-set constant h: for a uniform set 0.5 * (3 k / (4 pi n / V))^(1/3) (about k neighbours within
+    2h), for a Plummer set the same formula on the volume of the sphere holding half the particles (about k
+    neighbours at the half-mass radius). Generated on the device with a seeded torch generator.
+    Returns (list of dicts with n, x, y, z, h device tensors, lo, hi, bucket)."""
+    g = torch.Generator(device=device).manual_seed(seed)
+    rng = np.random.default_rng(seed)
+    sets = []
+    for s in range(num_sets):
+        n = int(2 ** (lo_exp + (hi_exp - lo_exp) * rng.random()))
+        bucket = int(rng.choice([16, 32, 64]))
+        if s % 2 == 0:
+            x, y, z = (torch.rand(n, generator=g, device=device, dtype=torch.float32) for _ in range(3))
+            lo, hi = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
+            hval = 0.5 * (3 * k / (4 * np.pi * n)) ** (1 / 3)
+        else:
+            u = torch.rand(3, int(n * 1.01) + 64, generator=g, device=device, dtype=torch.float64)
+            r = 1.0 / torch.sqrt(u[0].clamp_min(1e-300) ** (-2.0 / 3.0) - 1.0)
+            keep = r < 100.0
+            r, u1, u2 = r[keep][:n], u[1][keep][:n], u[2][keep][:n]
+            while r.numel() < n:  # rare: top up the rejected ones
+                v = torch.rand(3, n, generator=g, device=device, dtype=torch.float64)
+                rr = 1.0 / torch.sqrt(v[0].clamp_min(1e-300) ** (-2.0 / 3.0) - 1.0)
+                kk = rr < 100.0
+                m = n - r.numel()
+                r = torch.cat([r, rr[kk][:m]])
+                u1 = torch.cat([u1, v[1][kk][:m]])
+                u2 = torch.cat([u2, v[2][kk][:m]])
+            zz = (1.0 - 2.0 * u1) * r
+            phi = 2.0 * np.pi * u2
+            rho = torch.sqrt(r * r - zz * zz)
+            x, y, z = (a.float() for a in (rho * torch.cos(phi), rho * torch.sin(phi), zz))
+            lo = (float(x.min()), float(y.min()), float(z.min()))
+            hi = (float(x.max()), float(y.max()), float(z.max()))
+            rhalf = 1.0 / np.sqrt(0.5 ** (-2.0 / 3.0) - 1.0)  # half-mass radius of a Plummer sphere of scale 1
+            hval = 0.5 * (3 * k / (4 * np.pi * (n / 2) / (4 / 3 * np.pi * rhalf ** 3))) ** (1 / 3)
+        h = torch.full((n,), hval, device=device, dtype=torch.float32)
+        sets.append(dict(n=n, x=x, y=y, z=z, h=h, lo=lo, hi=hi, bucket=bucket))
+    return sets
+
+
 def tight_box(x, y, z):
     return (float(x.min()), float(y.min()), float(z.min())), (float(x.max()), float(y.max()), float(z.max()))
 
