@@ -582,6 +582,12 @@ static BuildLayout<K> buildLayout(Arena& ar, int capacity, bool update)
     return l;
 }
 
+std::mutex& cooperativeBuildMutex()
+{
+    static std::mutex m;
+    return m;
+}
+
 template<class K>
 size_t octreeBuildWorkspaceBytes(int capacity, bool update)
 {
@@ -639,6 +645,9 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
         CSG_CUDA_TRY(cudaMemcpyAsync(l.off[0], batch->initOff, (size_t(batch->initL) + 1) * sizeof(uint32_t),
                                      cudaMemcpyDeviceToDevice, s));
     }
+
+    std::unique_lock<std::mutex> coop(cooperativeBuildMutex(), std::defer_lock);
+    if (sync) coop.lock(); // held until octreeBuildFinish below has synchronised
 
     int G = buildGridSize();
     BuildArgs<K> a;

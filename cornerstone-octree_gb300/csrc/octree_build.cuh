@@ -2,6 +2,8 @@
 #pragma once
 #include "cs_common.cuh"
 
+#include <mutex>
+
 namespace csg
 {
 
@@ -65,6 +67,11 @@ int octreeBuildFinish(cudaStream_t s, void* ws, size_t wsBytes, int capacity, bo
 //! after an update octreeBuild with sync = false: *Ldev = the new leaf count if the build succeeded (else unchanged)
 template<class K>
 int commitLeafCount(cudaStream_t s, void* ws, size_t wsBytes, int capacity, int* Ldev);
+
+//! cooperative builds launched by concurrent host threads must not overlap on the device (each grid is sized for the
+//! whole GPU and waits at grid barriers for all its blocks): octreeBuild with sync holds this lock from its launch
+//! until the build has finished; a caller that launches without sync and finishes later holds it over both
+std::mutex& cooperativeBuildMutex();
 
 template<class K>
 int nodeCounts(cudaStream_t s, const K* tree, uint32_t* counts, int numNodes, const K* keys, size_t n,

@@ -5,6 +5,7 @@
 // rebalance iteration; here the whole rebalance loop is one cooperative launch).
 #include "cs_common.cuh"
 #include "halos.cuh"
+#include "pipeline.cuh"
 #include "neighbors.cuh"
 #include "octree_build.cuh"
 #include "octree_link.cuh"
@@ -16,42 +17,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <type_traits>
 
 namespace csg
 {
-
-enum Stage
-{
-    ST_KEYS,
-    ST_SORT,
-    ST_GATHER,
-    ST_BUILD,
-    ST_LINK,
-    ST_GEO,
-    ST_NBPREP,
-    ST_HALOS,
-    ST_NEIGHBORS,
-    ST_COUNT
-};
-
-struct PipelineBase
-{
-    cs_pipeline_config cfg{};
-    virtual ~PipelineBase() = default;
-    virtual int run(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, size_t n,
-                    const cs_box& box, uint64_t f0, uint64_t f1, cs_pipeline_result* res, bool hostIn) = 0;
-    virtual int outputs(cs_pipeline_outputs* o) = 0;
-    virtual size_t deviceBytes() const          = 0;
-    virtual int copyBack(cudaStream_t s, uint32_t* nc, uint8_t* flags, size_t flagsCap) = 0;
-    virtual int step(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, size_t n,
-                     const cs_box& box, bool useGraph, cs_pipeline_result* res) = 0;
-    virtual void resetSteps() = 0;
-    int graphReplays = 0; // steps of the last step sequence that were replayed from a captured graph
-    cudaEvent_t ev[ST_COUNT + 1] = {};
-    float stageMs[ST_COUNT]      = {};
-    int lastN                    = 0;
-};
 
 template<class T, class K>
 struct Pipeline final : PipelineBase
@@ -319,6 +289,8 @@ struct Pipeline final : PipelineBase
         n = nIn;
         if ((rc = allocSteps(s, nIn, incCap))) return rc;
         const int cur = incCur;
+        // the step's cooperative build runs between here and octreeBuildFinish (graph or not)
+        std::lock_guard<std::mutex> coop(cooperativeBuildMutex());
         if (useGraph)
         {
             if (!gstream) CSG_CUDA_TRY(cudaStreamCreateWithFlags(&gstream, cudaStreamNonBlocking));
@@ -685,6 +657,56 @@ struct Pipeline final : PipelineBase
     }
 };
 
+// splitmix64's finaliser (Steele, Lea, Flood 2014) as the mixing step of the neighbour checksum
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__global__ void neighborChecksumKernel(const uint32_t* __restrict__ nb, const uint32_t* __restrict__ nc, size_t n,
+                                       unsigned ngmax, unsigned long long* out)
+{
+    unsigned long long acc = 0;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    {
+        uint32_t c = nc[i];
+        unsigned m = c < ngmax ? c : ngmax;
+        uint64_t h = mix64(uint64_t(i) * 0x9e3779b97f4a7c15ull ^ c);
+        for (unsigned k = 0; k < m; ++k)
+            h = mix64(h ^ nb[i * ngmax + k]);
+        acc += h;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+uint64_t neighborChecksum(cudaStream_t s, const uint32_t* nb, const uint32_t* nc, size_t n, unsigned ngmax,
+                          uint64_t* scratchDev)
+{
+    uint64_t h = 0;
+    if (cudaMemsetAsync(scratchDev, 0, sizeof(uint64_t), s) != cudaSuccess) return 0;
+    unsigned g = unsigned(std::min<size_t>((n + 255) / 256, size_t(smCount()) * 8));
+    if (n && ngmax) neighborChecksumKernel<<<std::max(1u, g), 256, 0, s>>>(nb, nc, n, ngmax,
+                                                                           reinterpret_cast<unsigned long long*>(scratchDev));
+    cudaMemcpyAsync(&h, scratchDev, sizeof(h), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    return h;
+}
+
+std::unique_ptr<PipelineBase> makePipeline(int coordBits, int keyBits, const cs_pipeline_config& cfg)
+{
+    std::unique_ptr<PipelineBase> p;
+    if (coordBits == 64 && keyBits == 64) p = std::make_unique<Pipeline<double, uint64_t>>();
+    else if (coordBits == 64) p = std::make_unique<Pipeline<double, uint32_t>>();
+    else if (keyBits == 64) p = std::make_unique<Pipeline<float, uint64_t>>();
+    else p = std::make_unique<Pipeline<float, uint32_t>>();
+    p->cfg = cfg;
+    return p;
+}
+
 } // namespace csg
 
 using namespace csg;
@@ -703,12 +725,8 @@ extern "C" int cs_pipeline_create(cs_pipeline* out, int coord_bits, int key_bits
         return CS_ERR_INVALID;
     }
     auto* p = new cs_pipeline_s;
-    if (coord_bits == 64 && key_bits == 64) p->impl = std::make_unique<Pipeline<double, uint64_t>>();
-    else if (coord_bits == 64) p->impl = std::make_unique<Pipeline<double, uint32_t>>();
-    else if (key_bits == 64) p->impl = std::make_unique<Pipeline<float, uint64_t>>();
-    else p->impl = std::make_unique<Pipeline<float, uint32_t>>();
-    p->impl->cfg = *cfg;
-    *out         = p;
+    p->impl = makePipeline(coord_bits, key_bits, *cfg);
+    *out    = p;
     return CS_OK;
 }
 

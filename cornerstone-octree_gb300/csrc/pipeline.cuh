@@ -1,0 +1,50 @@
+// Internal interface of the whole-path object (pipeline.cu), shared with the request server (server.cu).
+#pragma once
+#include "cs_common.cuh"
+
+#include <memory>
+
+namespace csg
+{
+
+enum Stage
+{
+    ST_KEYS,
+    ST_SORT,
+    ST_GATHER,
+    ST_BUILD,
+    ST_LINK,
+    ST_GEO,
+    ST_NBPREP,
+    ST_HALOS,
+    ST_NEIGHBORS,
+    ST_COUNT
+};
+
+struct PipelineBase
+{
+    cs_pipeline_config cfg{};
+    virtual ~PipelineBase() = default;
+    virtual int run(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, size_t n,
+                    const cs_box& box, uint64_t f0, uint64_t f1, cs_pipeline_result* res, bool hostIn) = 0;
+    virtual int outputs(cs_pipeline_outputs* o) = 0;
+    virtual size_t deviceBytes() const          = 0;
+    virtual int copyBack(cudaStream_t s, uint32_t* nc, uint8_t* flags, size_t flagsCap) = 0;
+    virtual int step(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, size_t n,
+                     const cs_box& box, bool useGraph, cs_pipeline_result* res) = 0;
+    virtual void resetSteps() = 0;
+    int graphReplays = 0; // steps of the last step sequence that were replayed from a captured graph
+    cudaEvent_t ev[ST_COUNT + 1] = {};
+    float stageMs[ST_COUNT]      = {};
+    int lastN                    = 0;
+};
+
+//! a pipeline object for the coordinate and key widths (32 or 64 bits each)
+std::unique_ptr<PipelineBase> makePipeline(int coordBits, int keyBits, const cs_pipeline_config& cfg);
+
+//! device checksum of a neighbour result: the wrapping sum over particles i of a hash of (i, count, the first
+//! min(count, ngmax) stored indices); order-independent over particles, so equal results give equal sums
+uint64_t neighborChecksum(cudaStream_t s, const uint32_t* nb, const uint32_t* nc, size_t n, unsigned ngmax,
+                          uint64_t* scratchDev);
+
+} // namespace csg

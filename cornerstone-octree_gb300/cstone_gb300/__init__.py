@@ -496,6 +496,87 @@ class Batch:
         return out
 
 
+# ---------------------------------------------------------------------------------------------------------------
+# request server (cs_server_*)
+# ---------------------------------------------------------------------------------------------------------------
+
+REQ_BUILD, REQ_UPDATE = 0, 1
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("num_slots", C.c_int), ("hbm_budget_bytes", C.c_uint64), ("coord_bits", C.c_int),
+                ("key_bits", C.c_int), ("pipeline", PipelineConfig)]
+
+
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("tree", C.c_int32), ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("h", C.c_void_p), ("n", C.c_size_t), ("box", Box)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int), ("num_leaves", C.c_int32),
+                ("neighbor_checksum", C.c_uint64), ("queued_ms", C.c_double), ("run_ms", C.c_double),
+                ("latency_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_uint64), ("failed", C.c_uint64), ("particles", C.c_uint64),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("elapsed_s", C.c_double),
+                ("device_bytes", C.c_uint64), ("resident_trees", C.c_int)]
+
+
+class Server:
+    """continuous batching of build / update requests from host arrays (numpy) on the current GPU"""
+
+    def __init__(self, num_slots, budget_bytes, coord_bits=64, key_bits=64, kind=HILBERT, bucket=64, ngmax=200,
+                 search_ext=1.0):
+        pc = PipelineConfig(kind, bucket, 0xFFFFFFFF, ngmax, search_ext, 1.0, 0, 1)
+        self.cfg = ServerConfig(num_slots, int(budget_bytes), coord_bits, key_bits, pc)
+        self.handle = C.c_void_p()
+        _check(lib.cs_server_create(C.byref(self.handle), C.byref(self.cfg)))
+        self._inputs = {}  # keeps each request's host arrays alive until it is waited for
+
+    def submit(self, x, y, z, h, box, kind=REQ_BUILD, tree=-1):
+        import numpy as np
+
+        arrs = [np.ascontiguousarray(a) for a in (x, y, z, h)]
+        req = Request(kind, tree, *[a.ctypes.data for a in arrs], arrs[0].size, box)
+        rid = C.c_uint64()
+        _check(lib.cs_server_submit(self.handle, C.byref(req), C.byref(rid)))
+        self._inputs[rid.value] = arrs
+        return rid.value
+
+    def wait(self, rid, counts=True):
+        """(RequestResult, neighbour counts as a numpy array or None); raises on a failed request"""
+        import numpy as np
+
+        arrs = self._inputs.get(rid)
+        nc = np.empty(arrs[0].size, np.uint32) if counts and arrs is not None else None
+        res = RequestResult()
+        rc = lib.cs_server_wait(self.handle, C.c_uint64(rid), C.byref(res),
+                                nc.ctypes.data_as(C.c_void_p) if nc is not None else None)
+        self._inputs.pop(rid, None)
+        if rc != 0:
+            raise CsError(rc, f"request {rid} failed")
+        return res, nc
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib.cs_server_get_stats(self.handle, C.byref(st)))
+        return st
+
+    def release_tree(self, tree):
+        _check(lib.cs_server_release_tree(self.handle, tree))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib.cs_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        self.close()
+
+
 def _wrap(ptr, count, dtype):
     """non-owning torch view of device memory held by the library"""
     if count == 0 or not ptr:

@@ -419,6 +419,67 @@ int cs_batch_run(cs_batch b, cs_stream_t stream, const void* x, const void* y, c
 int cs_batch_get_outputs(cs_batch b, cs_batch_outputs* out);
 size_t cs_batch_device_bytes(cs_batch b);
 
+/* ---- request server --------------------------------------------------------------------------------------------
+ * No counterpart in the reference. Continuous batching of requests on one GPU: a BUILD request runs the whole path
+ * (keys -> neighbours, no halos) on a particle set from host arrays; with tree >= 0 the tree stays resident on the
+ * device, and an UPDATE request of that tree applies one updateOctree step to new positions of its particles
+ * (cs_pipeline_step). num_slots requests run at once, each on its own stream and host worker; a request is admitted
+ * when a slot is free and its device memory fits hbm_budget_bytes (idle resident trees are released least recently
+ * used first to make room); requests of one tree run in submission order. Every result depends only on its own
+ * inputs: the same alone and in any mix. The host arrays of a request must stay valid until it completes. */
+enum cs_request_kind
+{
+    CS_REQ_BUILD  = 0,
+    CS_REQ_UPDATE = 1
+};
+typedef struct cs_server_s* cs_server;
+typedef struct
+{
+    int num_slots;               /* requests on the device at once */
+    uint64_t hbm_budget_bytes;   /* device memory all requests and resident trees may hold */
+    int coord_bits;              /* 32 or 64 */
+    int key_bits;                /* 32 or 64 */
+    cs_pipeline_config pipeline; /* curve, bucket size, ngmax, search extent (halos are not run) */
+} cs_server_config;
+typedef struct
+{
+    int kind;     /* cs_request_kind */
+    int32_t tree; /* resident tree id (>= 0), or -1 for a one-off build */
+    const void *x, *y, *z, *h;
+    size_t n;
+    cs_box box;
+} cs_request;
+typedef struct
+{
+    uint64_t id;
+    int status;                 /* CS_OK or the failure (cs_last_error of the waiting thread has no detail) */
+    int32_t num_leaves;
+    uint64_t neighbor_checksum; /* order-independent hash of every particle's count and stored neighbour list */
+    double queued_ms;           /* submission -> start */
+    double run_ms;              /* start -> result on the host */
+    double latency_ms;          /* submission -> result on the host */
+} cs_request_result;
+typedef struct
+{
+    uint64_t completed;
+    uint64_t failed;
+    uint64_t particles; /* of the completed requests */
+    double p50_ms;      /* latency percentiles of the completed requests */
+    double p99_ms;
+    double elapsed_s;   /* first submission -> last completion */
+    uint64_t device_bytes;
+    int resident_trees;
+} cs_server_stats;
+int cs_server_create(cs_server* out, const cs_server_config* cfg);
+/* finishes the queued requests, then stops the workers and frees the device memory */
+int cs_server_destroy(cs_server s);
+int cs_server_submit(cs_server s, const cs_request* request, uint64_t* id);
+/* blocks until request id is done; copies its n neighbour counts into neighbor_counts_host (may be NULL); returns the
+ * request's status */
+int cs_server_wait(cs_server s, uint64_t id, cs_request_result* result, uint32_t* neighbor_counts_host);
+int cs_server_release_tree(cs_server s, int32_t tree);
+int cs_server_get_stats(cs_server s, cs_server_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif
