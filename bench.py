@@ -45,10 +45,13 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--n", type=int, default=None, help="particles (default 16M plummer, 64M incremental)")
     p.add_argument("--sets", type=int, default=4096, help="sets of the batched workload")
-    p.add_argument("--workload", default="plummer", choices=["plummer", "incremental", "batched"],
+    p.add_argument("--requests", type=int, default=600, help="requests of the served workload")
+    p.add_argument("--rate", type=float, default=2000.0, help="Poisson arrival rate (requests/s), served workload")
+    p.add_argument("--workload", default="plummer", choices=["plummer", "incremental", "batched", "served"],
                    help="plummer: the 16M keys->neighbours pass (default); incremental: 64M FP32 time steps with one "
                         "updateOctree step each, replayed from CUDA graphs; batched: 4096 uneven FP32 sets in "
-                        "one batched run per chunk against a per-set loop of the single-set pipeline")
+                        "one batched run per chunk against a per-set loop of the single-set pipeline; served: a "
+                        "Poisson stream of build and update requests through the request server")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=1 << 20, help="particles of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -394,6 +397,90 @@ def run_batched(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_served(args, world, rank, local):
+    """A Poisson stream of requests (rate 2000/s) through the request server: sizes log-uniform in [2^12, 2^22], FP64
+    uniform or Plummer (50/50), Hilbert64, bucket 64, per-request constant h for about 100 neighbours, 30 % of the
+    requests incremental updates (displacement 0.05 spacing) of resident trees, 150 GB admission budget, 4 slots.
+    Inputs come from a pool of pre-generated sets (the generation is not timed). Reports latency percentiles and the
+    particles/s of the completed requests."""
+    import numpy as np
+    import torch
+
+    import cstone_gb300 as cs
+    from cstone_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(args.seed + rank)
+    pool = []
+    for j in range(24):
+        n = int(2 ** (12 + 10 * rng.random()))
+        if j % 2:
+            x, y, z = W.uniform(n, 0.0, 1.0, args.seed * 100 + j)
+            lo, hi = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
+            h = 0.5 * (3 * 100 / (4 * np.pi * n)) ** (1 / 3)
+        else:
+            x, y, z = W.plummer(n, args.seed * 100 + j)
+            lo, hi = W.tight_box(x, y, z)
+            rhalf = 1.0 / np.sqrt(0.5 ** (-2.0 / 3.0) - 1.0)
+            h = 0.5 * (3 * 100 / (4 * np.pi * (n / 2) / (4 / 3 * np.pi * rhalf ** 3))) ** (1 / 3)
+        hh = np.full(n, h)
+        sp = (np.prod(np.array(hi) - np.array(lo)) / n) ** (1 / 3)
+        moved = [np.clip(a + rng.normal(0, 0.05 * sp, n), l, u) for a, l, u in zip((x, y, z), lo, hi)]
+        pool.append(dict(n=n, xyz=(x, y, z), moved=moved, h=hh, box=cs.make_box(lo, hi)))
+    trees = list(range(8))
+    srv = cs.Server(4, 150 * (1 << 30), 64, 64, cs.HILBERT, 64, 200, 1.0)
+    # resident trees for the update requests (not timed)
+    for t in trees:
+        p = pool[t]
+        srv.wait(srv.submit(*p["xyz"], p["h"], p["box"], cs.REQ_BUILD, t), counts=False)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
+    plan = []
+    flip = {t: 0 for t in trees}
+    for k in range(args.requests):
+        if rng.random() < 0.3:
+            t = int(rng.choice(trees))
+            flip[t] ^= 1
+            p = pool[t]
+            plan.append((t, p["moved"] if flip[t] else p["xyz"], p, cs.REQ_UPDATE))
+        else:
+            p = pool[int(rng.integers(len(pool)))]
+            plan.append((-1, p["xyz"], p, cs.REQ_BUILD))
+    ids = []
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for k, (t, xyz, p, kind) in enumerate(plan):
+            wait = t0 + arrivals[k] - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            ids.append((srv.submit(*xyz, p["h"], p["box"], kind, t), p["n"]))
+        lat, parts = [], 0
+        for rid, n in ids:
+            r, _ = srv.wait(rid, counts=False)
+            lat.append(r.latency_ms)
+            parts += n
+        elapsed = time.perf_counter() - t0  # first arrival -> last result (the warm-up builds are not counted)
+    st = srv.stats()
+    srv.close()
+    lat = np.sort(np.array(lat))
+    if rank == 0:
+        line = {"metric": "served requests: p50/p99 latency and Mparticles/s (Poisson 2000/s, 2^12..2^22 FP64)",
+                "value": round(parts / elapsed / 1e6, 3), "unit": "Mparticles/s", "n_gpus": world,
+                "steps": args.requests, "warmup": len(trees), "ms_per_step": round(elapsed * 1e3 / args.requests, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic",
+                "config": {"workload": "served-requests", "requests": args.requests, "rate_per_s": args.rate,
+                           "sizes": "log-uniform [2^12, 2^22]", "mix": "uniform / Plummer 50/50",
+                           "updates": "30 % of requests, one updateOctree step of a resident tree",
+                           "keys": "hilbert64", "bucket_size": 64, "ngmax": 200, "neighbours": "about 100",
+                           "slots": 4, "hbm_budget_gb": 150, "pool_sets": len(pool),
+                           "parallelism": f"replicas x{world}"},
+                "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                "completed": int(st.completed) - len(trees), "failed": int(st.failed), "particles": parts,
+                "offered_Mparticles_per_s": round(parts / arrivals[-1] / 1e6, 3),
+                "elapsed_s": round(elapsed, 3), "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
@@ -405,6 +492,9 @@ def main():
         return
     if args.workload == "batched":
         run_batched(args, world, rank, local)
+        return
+    if args.workload == "served":
+        run_served(args, world, rank, local)
         return
 
     import numpy as np
