@@ -472,6 +472,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
 
     __shared__ int sStack[NB_WARPS][NBG_STACK];
     __shared__ unsigned sMaskStack[NB_WARPS][NBG_STACK];
+    __shared__ int sC0Stack[NB_WARPS][NBG_STACK]; // child offset of each stacked node (<= 0: a leaf)
     __shared__ float4 sCand[NB_WARPS][32];
     // S == 1: the staged candidates as separate x, y, z rows, read four at a time (two float2 pairs)
     __shared__ __align__(16) float sCx[NB_WARPS][32], sCy[NB_WARPS][32], sCz[NB_WARPS][32];
@@ -557,6 +558,27 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     float gc[3], gh[3], gR2 = 0.f, rmax = 0.f;
     unsigned activeMask = 0;
     int rootNode        = 0;
+    // With one target per lane (S == 1) the bounds are those of the lane's sub-group of 8 consecutive targets (lanes
+    // 8g .. 8g + 7), so that a node is only carried for the sub-groups that can reach it; otherwise the whole warp's.
+    constexpr bool SUB = S == 1;
+    auto segMin = [&](float v) {
+        if constexpr (SUB)
+        {
+            for (int o = 4; o > 0; o >>= 1)
+                v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+            return v;
+        }
+        else return warpMinF(v);
+    };
+    auto segMax = [&](float v) {
+        if constexpr (SUB)
+        {
+            for (int o = 4; o > 0; o >>= 1)
+                v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+            return v;
+        }
+        else return warpMaxF(v);
+    };
     auto groupBounds = [&](bool inPass) {
         float rad = __fmul_ru(rr, 1.f + 64 * EPS);
 #pragma unroll
@@ -565,20 +587,20 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             float slack = __fmaf_ru(2 * EPS, fabsf(b[k]), delta);
             float lo    = inPass ? __fsub_rd(__fsub_rd(b[k], rad), slack) : INFINITY;
             float hi    = inPass ? __fadd_ru(__fadd_ru(b[k], rad), slack) : -INFINITY;
-            lo          = warpMinF(lo);
-            hi          = warpMaxF(hi);
+            lo          = segMin(lo);
+            hi          = segMax(hi);
             gc[k]       = 0.5f * (lo + hi);
             gh[k]       = __fmul_ru(__fsub_ru(hi, lo), 0.5f);
         }
-        // group bounding sphere around the box centre gc: every point of every lane's sphere is within gR of gc, so
-        // it cuts the corners of the box (which matter where the density rises steeply, e.g. towards a Plummer core)
+        // bounding sphere around the box centre gc: every point of every lane's sphere is within gR of gc, so it cuts
+        // the corners of the box (which matter where the density rises steeply, e.g. towards a Plummer core)
         activeMask = __ballot_sync(0xffffffffu, inPass);
-        rmax       = warpMaxF(inPass ? rr : 0.f);
+        rmax       = segMax(inPass ? rr : 0.f);
         float e0 = b[0] - gc[0], e1 = b[1] - gc[1], e2 = b[2] - gc[2];
         float dc = __fsqrt_ru(__fmaf_ru(e2, e2, __fmaf_ru(e1, e1, __fmul_ru(e0, e0))));
         float sl = __fmaf_ru(2 * EPS, fmaxf(fabsf(b[0]), fmaxf(fabsf(b[1]), fabsf(b[2]))), delta);
         float gr = inPass ? __fadd_ru(__fadd_ru(__fmul_ru(dc, 1.f + 8 * EPS), __fmul_ru(rr, 1.f + 64 * EPS)), sl) : 0.f;
-        gr       = warpMaxF(gr);
+        gr       = segMax(gr);
         gR2      = __fmul_ru(gr, gr);
     };
 
@@ -594,6 +616,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     // cost model of the candidate batches (lane 0): steps of the lane-per-target loop, needing lanes, the cheaper of
     // 11 instructions per step and 20 per needing lane, batches, cycles spent in the batches
     unsigned long long stSteps = 0, stNeed = 0, stMinCost = 0, stBatches = 0, stCandCyc = 0;
+    // cycles in leaf visits (box test, staging and batches) and leaf visits no lane needed
+    unsigned long long stLeafCyc = 0, stLeafIdle = 0;
 
     // node box in the warp frame: center cc = (chi - P) + clo, half size sz
     auto frameOf = [&](float4 ch, float4 cl, float4 s4, float cc[3], float sz[3]) {
@@ -943,13 +967,16 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     const bool inPass = active && (!a.numSets || mySet == passSet);
     groupBounds(inPass);
     rootNode   = a.numSets ? __ldg(a.setRoots + passSet) : 0;
-    loose      = __fsqrt_ru(gR2) > 3.f * rmax;
+    loose      = __any_sync(0xffffffffu, __fsqrt_ru(gR2) > 3.f * rmax);
     expansions = 0;
-    int top    = 0;
+    int* c0Stack = sC0Stack[warp];
+    int top      = 0;
+    const int rootC0 = __float_as_int(prep.nrec[3 * size_t(rootNode)].w);
     if (lane == 0)
     {
         stack[0]     = rootNode;
         maskStack[0] = activeMask;
+        c0Stack[0]   = rootC0;
     }
     top = activeMask ? 1 : 0;
     __syncwarp();
@@ -957,26 +984,41 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     {
         int node       = stack[top - 1];
         unsigned pmask = maskStack[top - 1];
+        int c0         = c0Stack[top - 1];
         --top;
-        const float4* rec = prep.nrec + 3 * size_t(node);
-        float4 recA = rec[0], recB = rec[1], recC = rec[2];
-        int c0      = __float_as_int(recA.w);
         if (c0 <= 0) // a leaf; -1: it holds particles outside its box
         {
+            const float4* rec = prep.nrec + 3 * size_t(node);
+            float4 recA = rec[0], recB = rec[1], recC = rec[2];
+            long long tl0 = Stats ? clock64() : 0;
+            unsigned long long before = stLeaves;
             processLeaf(node, pmask, recA, recB, recC, c0 < 0);
+            if constexpr (Stats)
+            {
+                stLeafCyc += (unsigned long long)(clock64() - tl0);
+                stLeafIdle += stLeaves == before;
+            }
             continue;
         }
         if constexpr (Stats) stNodes++;
         if (++expansions > LOOSE_AFTER) loose = true;
         bool ok         = false;
         unsigned cmask  = pmask; // lanes alive in the accepted child (this lane's child when lane < 8)
+        int childC0     = 0;     // child offset of this lane's child (lane < 8)
         if (!loose)
         {
-            if (lane < 8)
+            // lane l tests child l & 7 against its sub-group's bounds (every lane of one sub-group tests the 8
+            // children; S > 1: lanes 0-7 against the warp's bounds)
+            const int cidx = SUB ? (lane & 7) : lane;
+            bool hit       = false;
+            if (SUB || lane < 8)
             {
+                const float4* r = prep.nrec + 3 * size_t(c0 + cidx);
+                float4 rA = r[0], rB = r[1], rC = r[2];
                 float cc[3], sz[3];
-                nodeFrame(c0 + lane, cc, sz);
-                ok          = true;
+                frameOf(rA, rB, rC, cc, sz);
+                childC0     = __float_as_int(rA.w);
+                hit         = true;
                 float dist2 = 0.f;
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
@@ -984,12 +1026,20 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     float ad     = fabsf(cc[k] - gc[k]);
                     float margin = __fmaf_ru(4 * EPS, fabsf(cc[k]) + sz[k] + fabsf(gc[k]) + gh[k],
                                              __fmaf_ru(4 * EPS * EPS, C, delta));
-                    ok           = ok && (ad - sz[k] - gh[k] < margin);
+                    hit          = hit && (ad - sz[k] - gh[k] < margin);
                     float dk     = fmaxf(__fsub_rd(__fsub_rd(ad, sz[k]), margin), 0.f);
                     dist2        = __fmaf_rd(dk, dk, dist2);
                 }
-                ok = ok && dist2 <= gR2;
+                hit = hit && dist2 <= gR2;
             }
+            if constexpr (SUB)
+            {
+                // bit 8g + c: sub-group g may reach child c; the lanes of child c are those sub-groups' alive lanes
+                const unsigned m32 = __ballot_sync(0xffffffffu, hit);
+                cmask              = pmask & (((m32 >> cidx) & 0x01010101u) * 0xFFu);
+                ok                 = lane < 8 && cmask != 0;
+            }
+            else { ok = hit; }
         }
         else
         {
@@ -997,11 +1047,16 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
 #pragma unroll 1
             for (int c = 0; c < 8; ++c)
             {
-                unsigned m = __ballot_sync(0xffffffffu, alive && mayHit(c0 + c));
+                const float4* r = prep.nrec + 3 * size_t(c0 + c);
+                float4 rA = r[0], rB = r[1], rC = r[2];
+                float cc[3], sz[3];
+                frameOf(rA, rB, rC, cc, sz);
+                unsigned m = __ballot_sync(0xffffffffu, alive && mayHitBox(cc, sz));
                 if (lane == c)
                 {
-                    cmask = m;
-                    ok    = m != 0;
+                    cmask   = m;
+                    ok      = m != 0;
+                    childC0 = __float_as_int(rA.w);
                 }
             }
         }
@@ -1018,6 +1073,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             int pos        = top + __popc(m >> (lane + 1));
             stack[pos]     = c0 + lane;
             maskStack[pos] = cmask;
+            c0Stack[pos]   = childC0;
         }
         top += __popc(m);
         __syncwarp();
@@ -1046,6 +1102,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             atomicAdd(a.stats + 23, stBatches);
             atomicAdd(a.stats + 24, stCandCyc);
             atomicAdd(a.stats + 25, (unsigned long long)(clock64() - t0));
+            atomicAdd(a.stats + 26, stLeafCyc);
+            atomicAdd(a.stats + 27, stLeafIdle);
             atomicAdd(a.stats + 7, 1ull);
             // slowest warp: [8] cycles, [9] its expansions, [10] leaves, [11] candidates, [12] loose flag,
             // [13] its first target; [14] number of loose warps

@@ -583,6 +583,10 @@ struct Pipeline final : PipelineBase
                              "lanes %.1f, min-cost/step-cost %.3f | cycles in batches %.1f%% of warp cycles\n",
                              double(h[23]) / h[7], double(h[20]) / h[23], double(h[21]) / h[23],
                              double(h[22]) / (11.0 * double(h[20])), 100.0 * double(h[24]) / double(h[25]));
+                std::fprintf(stderr,
+                             "[cstone_gb300 neighbour stats] cycles in leaf visits %.1f%% | leaf visits no lane "
+                             "needed %.1f per warp\n",
+                             100.0 * double(h[26]) / double(h[25]), double(h[27]) / h[7]);
             }
         }
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_COUNT], s));
