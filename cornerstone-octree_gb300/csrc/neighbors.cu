@@ -707,6 +707,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         nb2[1] = make_float2(-float(yi), -float(yi));
         nb2[2] = make_float2(-float(zi), -float(zi));
     }
+    const float2 nTin2 = make_float2(-Tin, -Tin), nTup2 = make_float2(-Tup, -Tup);
     auto decideSlow = [&](uint32_t jj, int node, bool contained) -> bool {
         if constexpr (F64)
             return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
@@ -819,18 +820,19 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             {
                 if (need)
                 {
-                    // bit k of inM: candidate k passes the FP32 test outright; of ambM: its test is undecided in
-                    // FP32 (or, T = float, its root path must be checked); eight independent distance chains per
-                    // step, the staged points past the leaf's end never pass
+                    // Eight independent distance chains per step; the staged points past the leaf's end never pass.
+                    // Bit 31 - k of inM: candidate k passes the FP32 test outright; of ambM: it is below the upper
+                    // threshold. The sign of e - T (exact for the packed add) is the comparison e < T, and a funnel
+                    // shift appends it to the mask: candidate k ends at bit steps - 1 - k, then at 31 - k
                     unsigned inM = 0, ambM = 0;
-                    for (int k0 = 0; k0 < cnt; k0 += 8)
+                    int steps    = 0;
+                    for (int k0 = 0; k0 < cnt; k0 += 8, steps += 8)
                     {
                         // two candidates per instruction (packed FP32 pairs); the expressions are those of filter()
                         const float4* vx = reinterpret_cast<const float4*>(&sCx[warp][k0]);
                         const float4* vy = reinterpret_cast<const float4*>(&sCy[warp][k0]);
                         const float4* vz = reinterpret_cast<const float4*>(&sCz[warp][k0]);
                         float4 X[2] = {vx[0], vx[1]}, Y[2] = {vy[0], vy[1]}, Z[2] = {vz[0], vz[1]};
-                        unsigned mi = 0, ma = 0;
 #pragma unroll
                         for (int p = 0; p < 4; ++p)
                         {
@@ -854,18 +856,25 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                             {
                                 e = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
                             }
-                            mi |= (unsigned(e.x < Tin) | unsigned(e.y < Tin) << 1) << (2 * p);
-                            ma |= (unsigned(e.x < Tup) | unsigned(e.y < Tup) << 1) << (2 * p);
+                            const float2 ti = __fadd2_rn(e, nTin2), tu = __fadd2_rn(e, nTup2);
+                            inM  = __funnelshift_l(__float_as_uint(ti.x), inM, 1);
+                            inM  = __funnelshift_l(__float_as_uint(ti.y), inM, 1);
+                            ambM = __funnelshift_l(__float_as_uint(tu.x), ambM, 1);
+                            ambM = __funnelshift_l(__float_as_uint(tu.y), ambM, 1);
                         }
-                        inM |= mi << k0;
-                        ambM |= ma << k0;
+                    }
+                    if (steps < 32)
+                    {
+                        inM <<= 32 - steps;
+                        ambM <<= 32 - steps;
                     }
                     ambM &= ~inM;
+                    const unsigned outR = __brev(outB); // bit 31 - k: candidate k lies outside its leaf's box
                     // candidates outside their leaf's box: no path-safe shortcut; a neighbour iff within r and the
                     // lane's path to the leaf passes (T = float: e < Tup is exactly d2 < r2)
-                    unsigned flagged = (inM | ambM) & outB;
-                    inM &= ~outB;
-                    ambM &= ~outB;
+                    unsigned flagged = (inM | ambM) & outR;
+                    inM &= ~outR;
+                    ambM &= ~outR;
                     if (flagged && leafPass)
                     {
                         if constexpr (F64)
@@ -873,10 +882,10 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                             const PbcArgs open{}; // group warps have no periodic sphere
                             while (flagged)
                             {
-                                int k = __ffs(flagged) - 1;
-                                flagged &= flagged - 1;
+                                int k = __clz(flagged);
+                                flagged &= ~(0x80000000u >> k);
                                 if (pairExactF64(xi, yi, zi, false, r2, a.x, a.y, a.z, base + k, open))
-                                    inM |= 1u << k;
+                                    inM |= 0x80000000u >> k;
                             }
                         }
                         else { inM |= flagged; }
@@ -888,15 +897,15 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     }
                     while (ambM)
                     {
-                        int k = __ffs(ambM) - 1;
-                        ambM &= ambM - 1;
-                        if (decideSlow(base + k, node, true)) inM |= 1u << k;
+                        int k = __clz(ambM);
+                        ambM &= ~(0x80000000u >> k);
+                        if (decideSlow(base + k, node, true)) inM |= 0x80000000u >> k;
                     }
-                    if (i >= base && i - base < 32u) inM &= ~(1u << (i - base));
+                    if (i >= base && i - base < 32u) inM &= ~(0x80000000u >> (i - base));
                     while (inM)
                     {
-                        int k = __ffs(inM) - 1;
-                        inM &= inM - 1;
+                        int k = __clz(inM);
+                        inM &= ~(0x80000000u >> k);
                         if (nc < ngmax) myNb[nc] = base + k;
                         nc++;
                     }
