@@ -61,6 +61,10 @@ struct Pipeline final : PipelineBase
     // no capture is possible)
     cudaStream_t gstream = nullptr;
     cudaEvent_t joinEv   = nullptr;
+    // host inputs: the copy stream, one event per chunk copied, and the fork point
+    static constexpr int kCopyChunks = 4;
+    cudaStream_t copyStream          = nullptr;
+    cudaEvent_t copyEv[kCopyChunks + 1] = {};
     const void* outLeaves      = nullptr;
     const uint32_t* outCounts  = nullptr;
     // opt-in traversal statistics of the neighbour search, printed to stderr (CSTONE_GB300_NB_STATS=1)
@@ -81,6 +85,9 @@ struct Pipeline final : PipelineBase
         dropGraphs();
         if (gstream) cudaStreamDestroy(gstream);
         if (joinEv) cudaEventDestroy(joinEv);
+        if (copyStream) cudaStreamDestroy(copyStream);
+        for (auto& e : copyEv)
+            if (e) cudaEventDestroy(e);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
     }
@@ -385,6 +392,7 @@ struct Pipeline final : PipelineBase
     {
         n  = nIn;
         int rc;
+        const T* hostSrc[4] = {};
         constexpr int KB = 8 * sizeof(K);
         if (n == 0 || n >= (size_t(1) << 30))
         {
@@ -397,10 +405,15 @@ struct Pipeline final : PipelineBase
         {
             for (DevBuf* b : {&inX, &inY, &inZ, &inH})
                 if ((rc = b->ensure(n * sizeof(T)))) return rc;
-            CSG_CUDA_TRY(cudaMemcpyAsync(inX.p, x, n * sizeof(T), cudaMemcpyHostToDevice, s));
-            CSG_CUDA_TRY(cudaMemcpyAsync(inY.p, y, n * sizeof(T), cudaMemcpyHostToDevice, s));
-            CSG_CUDA_TRY(cudaMemcpyAsync(inZ.p, z, n * sizeof(T), cudaMemcpyHostToDevice, s));
-            CSG_CUDA_TRY(cudaMemcpyAsync(inH.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+            // the host arrays arrive in chunks on a copy stream, the keys of chunk c computed while chunk c + 1
+            // travels (the keys are per particle); concurrent copies would share the host link and gain nothing
+            if (!copyStream)
+            {
+                CSG_CUDA_TRY(cudaStreamCreateWithFlags(&copyStream, cudaStreamNonBlocking));
+                for (auto& e : copyEv)
+                    CSG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            }
+            hostSrc[0] = x, hostSrc[1] = y, hostSrc[2] = z, hostSrc[3] = h;
             x = inX.as<T>();
             y = inY.as<T>();
             z = inZ.as<T>();
@@ -428,9 +441,35 @@ struct Pipeline final : PipelineBase
         float* cmax   = reinterpret_cast<float*>(err + 8);
         CSG_CUDA_TRY(cudaMemsetAsync(err, 0, 64, s));
 
-        CSG_CUDA_TRY(cudaEventRecord(ev[ST_KEYS], s));
-        if ((rc = sfcKeysPacked<T, K>(s, x, y, z, h, keys.as<K>(), packed.as<PackedT<T>>(), n, box, cfg.sfc_kind)))
-            return rc;
+        if (hostIn)
+        {
+            // chunk c: four copies on the copy stream, then its keys on s; the keys stage of a host run begins when
+            // the first chunk has arrived and so includes the copies of the others
+            const size_t chunk = ((n + kCopyChunks - 1) / kCopyChunks + 255) & ~size_t(255);
+            CSG_CUDA_TRY(cudaEventRecord(copyEv[kCopyChunks], s));
+            CSG_CUDA_TRY(cudaStreamWaitEvent(copyStream, copyEv[kCopyChunks], 0));
+            T* dst[4] = {inX.as<T>(), inY.as<T>(), inZ.as<T>(), inH.as<T>()};
+            for (int c = 0; c < kCopyChunks && size_t(c) * chunk < n; ++c)
+            {
+                const size_t a = size_t(c) * chunk, m = std::min(chunk, n - a);
+                for (int k = 0; k < 4; ++k)
+                    CSG_CUDA_TRY(cudaMemcpyAsync(dst[k] + a, hostSrc[k] + a, m * sizeof(T), cudaMemcpyHostToDevice,
+                                                 copyStream));
+                CSG_CUDA_TRY(cudaEventRecord(copyEv[c], copyStream));
+                CSG_CUDA_TRY(cudaStreamWaitEvent(s, copyEv[c], 0));
+                if (c == 0) CSG_CUDA_TRY(cudaEventRecord(ev[ST_KEYS], s));
+                if ((rc = sfcKeysPacked<T, K>(s, x + a, y + a, z + a, h + a, keys.as<K>() + a,
+                                              packed.as<PackedT<T>>() + a, m, box, cfg.sfc_kind)))
+                    return rc;
+            }
+        }
+        else
+        {
+            CSG_CUDA_TRY(cudaEventRecord(ev[ST_KEYS], s));
+            if ((rc = sfcKeysPacked<T, K>(s, x, y, z, h, keys.as<K>(), packed.as<PackedT<T>>(), n, box,
+                                          cfg.sfc_kind)))
+                return rc;
+        }
 
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_SORT], s));
         bool inAlt = false;
