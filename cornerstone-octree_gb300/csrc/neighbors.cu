@@ -618,6 +618,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     unsigned long long stSteps = 0, stNeed = 0, stMinCost = 0, stBatches = 0, stCandCyc = 0;
     // cycles in leaf visits (box test, staging and batches) and leaf visits no lane needed
     unsigned long long stLeafCyc = 0, stLeafIdle = 0;
+    // output loop shapes per batch: the most hits of one lane, lanes with hits, rounds of 32 hits
+    unsigned long long stOutMax = 0, stOutLanes = 0, stOutRounds = 0;
+    unsigned long long stPathWalks = 0; // exact path walks to leaves holding particles outside their box
 
     // node box in the warp frame: center cc = (chi - P) + clo, half size sz
     auto frameOf = [&](float4 ch, float4 cl, float4 s4, float cc[3], float sz[3]) {
@@ -694,20 +697,20 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         Tup = float(r2);
     }
     // minus the target in the candidates' frame, as float pairs for the packed distance evaluation
-    float2 nb2[3];
+    float nbS[3];
     if constexpr (F64)
     {
-        nb2[0] = make_float2(-b[0], -b[0]);
-        nb2[1] = make_float2(-b[1], -b[1]);
-        nb2[2] = make_float2(-b[2], -b[2]);
+        nbS[0] = -b[0];
+        nbS[1] = -b[1];
+        nbS[2] = -b[2];
     }
     else
     {
-        nb2[0] = make_float2(-float(xi), -float(xi));
-        nb2[1] = make_float2(-float(yi), -float(yi));
-        nb2[2] = make_float2(-float(zi), -float(zi));
+        nbS[0] = -float(xi);
+        nbS[1] = -float(yi);
+        nbS[2] = -float(zi);
     }
-    const float2 nTin2 = make_float2(-Tin, -Tin), nTup2 = make_float2(-Tup, -Tup);
+    const float nTinS = -Tin, nTupS = -Tup;
     auto decideSlow = [&](uint32_t jj, int node, bool contained) -> bool {
         if constexpr (F64)
             return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
@@ -776,6 +779,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             }
             if (!(n2u < tsafe))
             {
+                if constexpr (Stats) stPathWalks++;
                 if constexpr (F64)
                     leafPass = pathExactF64(xi, yi, zi, cellR2, node, a.parents, a.centers, a.sizes, rootNode);
                 else
@@ -806,6 +810,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             __syncwarp();
             int cnt = int(min(32u, last - base));
             long long tc0 = 0;
+            unsigned hitsThis = 0;
             if constexpr (Stats)
             {
                 unsigned steps = (unsigned(cnt) + 7u) & ~7u;
@@ -818,50 +823,54 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             }
             if constexpr (S == 1)
             {
+                // Bit 31 - k of inM: candidate k passes the FP32 test outright; of ambM: it is below the upper
+                // threshold. The sign of e - T (exact for the packed add) is the comparison e < T, and a funnel shift
+                // appends it to the mask, so that the candidates of a run end in order below its first one.
+                unsigned inM = 0, ambM = 0;
+                // four candidates (two packed FP32 pairs) against the target -n (negated frame coordinates) with the
+                // negated thresholds nin, nup; the expressions are those of filter()
+                auto four = [&](const float4& x4, const float4& y4, const float4& z4, const float2 n[3], float2 nin,
+                                float2 nup, unsigned& mi, unsigned& ma) {
+#pragma unroll
+                    for (int p = 0; p < 2; ++p)
+                    {
+                        float2 cx = p ? make_float2(x4.z, x4.w) : make_float2(x4.x, x4.y);
+                        float2 cy = p ? make_float2(y4.z, y4.w) : make_float2(y4.x, y4.y);
+                        float2 cz = p ? make_float2(z4.z, z4.w) : make_float2(z4.x, z4.y);
+                        float2 dx = __fadd2_rn(cx, n[0]);
+                        float2 dy = __fadd2_rn(cy, n[1]);
+                        float2 dz = __fadd2_rn(cz, n[2]);
+                        float2 e;
+                        if constexpr (F64)
+                        {
+                            e = __fmul2_rn(dx, dx);
+                            e = __ffma2_rn(dy, dy, e);
+                            e = __ffma2_rn(dz, dz, e);
+                        }
+                        else { e = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz)); }
+                        const float2 ti = __fadd2_rn(e, nin), tu = __fadd2_rn(e, nup);
+                        mi = __funnelshift_l(__float_as_uint(ti.x), mi, 1);
+                        mi = __funnelshift_l(__float_as_uint(ti.y), mi, 1);
+                        ma = __funnelshift_l(__float_as_uint(tu.x), ma, 1);
+                        ma = __funnelshift_l(__float_as_uint(tu.y), ma, 1);
+                    }
+                };
+                const float4* vx = reinterpret_cast<const float4*>(sCx[warp]);
+                const float4* vy = reinterpret_cast<const float4*>(sCy[warp]);
+                const float4* vz = reinterpret_cast<const float4*>(sCz[warp]);
+                // the target as packed pairs (negated frame coordinates and thresholds), built per batch from scalars
+                const float2 n[3] = {make_float2(nbS[0], nbS[0]), make_float2(nbS[1], nbS[1]),
+                                     make_float2(nbS[2], nbS[2])};
+                const float2 nin = make_float2(nTinS, nTinS), nup = make_float2(nTupS, nTupS);
                 if (need)
                 {
-                    // Eight independent distance chains per step; the staged points past the leaf's end never pass.
-                    // Bit 31 - k of inM: candidate k passes the FP32 test outright; of ambM: it is below the upper
-                    // threshold. The sign of e - T (exact for the packed add) is the comparison e < T, and a funnel
-                    // shift appends it to the mask: candidate k ends at bit steps - 1 - k, then at 31 - k
-                    unsigned inM = 0, ambM = 0;
-                    int steps    = 0;
+                    // eight independent distance chains per step; the staged points past the leaf's end never pass
+                    int steps = 0;
                     for (int k0 = 0; k0 < cnt; k0 += 8, steps += 8)
                     {
-                        // two candidates per instruction (packed FP32 pairs); the expressions are those of filter()
-                        const float4* vx = reinterpret_cast<const float4*>(&sCx[warp][k0]);
-                        const float4* vy = reinterpret_cast<const float4*>(&sCy[warp][k0]);
-                        const float4* vz = reinterpret_cast<const float4*>(&sCz[warp][k0]);
-                        float4 X[2] = {vx[0], vx[1]}, Y[2] = {vy[0], vy[1]}, Z[2] = {vz[0], vz[1]};
-#pragma unroll
-                        for (int p = 0; p < 4; ++p)
-                        {
-                            const float4& x4 = X[p >> 1];
-                            const float4& y4 = Y[p >> 1];
-                            const float4& z4 = Z[p >> 1];
-                            float2 cx = (p & 1) ? make_float2(x4.z, x4.w) : make_float2(x4.x, x4.y);
-                            float2 cy = (p & 1) ? make_float2(y4.z, y4.w) : make_float2(y4.x, y4.y);
-                            float2 cz = (p & 1) ? make_float2(z4.z, z4.w) : make_float2(z4.x, z4.y);
-                            float2 dx = __fadd2_rn(cx, nb2[0]);
-                            float2 dy = __fadd2_rn(cy, nb2[1]);
-                            float2 dz = __fadd2_rn(cz, nb2[2]);
-                            float2 e;
-                            if constexpr (F64)
-                            {
-                                e = __fmul2_rn(dx, dx);
-                                e = __ffma2_rn(dy, dy, e);
-                                e = __ffma2_rn(dz, dz, e);
-                            }
-                            else
-                            {
-                                e = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz));
-                            }
-                            const float2 ti = __fadd2_rn(e, nTin2), tu = __fadd2_rn(e, nTup2);
-                            inM  = __funnelshift_l(__float_as_uint(ti.x), inM, 1);
-                            inM  = __funnelshift_l(__float_as_uint(ti.y), inM, 1);
-                            ambM = __funnelshift_l(__float_as_uint(tu.x), ambM, 1);
-                            ambM = __funnelshift_l(__float_as_uint(tu.y), ambM, 1);
-                        }
+                        const int v = k0 >> 2;
+                        four(vx[v], vy[v], vz[v], n, nin, nup, inM, ambM);
+                        four(vx[v + 1], vy[v + 1], vz[v + 1], n, nin, nup, inM, ambM);
                     }
                     if (steps < 32)
                     {
@@ -871,24 +880,27 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     ambM &= ~inM;
                     const unsigned outR = __brev(outB); // bit 31 - k: candidate k lies outside its leaf's box
                     // candidates outside their leaf's box: no path-safe shortcut; a neighbour iff within r and the
-                    // lane's path to the leaf passes (T = float: e < Tup is exactly d2 < r2)
-                    unsigned flagged = (inM | ambM) & outR;
+                    // lane's path to the leaf passes. Below Tin the FP32 bound already proves d2 < r2; the band
+                    // [Tin, Tup) is decided exactly (T = float: e < Tup is exactly d2 < r2)
+                    const unsigned fIn = inM & outR, fAmb = ambM & outR;
                     inM &= ~outR;
                     ambM &= ~outR;
-                    if (flagged && leafPass)
+                    if (leafPass)
                     {
+                        inM |= fIn;
                         if constexpr (F64)
                         {
                             const PbcArgs open{}; // group warps have no periodic sphere
-                            while (flagged)
+                            unsigned f = fAmb;
+                            while (f)
                             {
-                                int k = __clz(flagged);
-                                flagged &= ~(0x80000000u >> k);
+                                int k = __clz(f);
+                                f &= ~(0x80000000u >> k);
                                 if (pairExactF64(xi, yi, zi, false, r2, a.x, a.y, a.z, base + k, open))
                                     inM |= 0x80000000u >> k;
                             }
                         }
-                        else { inM |= flagged; }
+                        else { inM |= fAmb; }
                     }
                     if constexpr (Stats)
                     {
@@ -902,6 +914,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                         if (decideSlow(base + k, node, true)) inM |= 0x80000000u >> k;
                     }
                     if (i >= base && i - base < 32u) inM &= ~(0x80000000u >> (i - base));
+                    if constexpr (Stats) hitsThis = __popc(inM);
                     while (inM)
                     {
                         int k = __clz(inM);
@@ -939,6 +952,11 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             {
                 __syncwarp();
                 stCandCyc += (unsigned long long)(clock64() - tc0);
+                const unsigned mx  = __reduce_max_sync(0xffffffffu, hitsThis);
+                const unsigned tot = __reduce_add_sync(0xffffffffu, hitsThis);
+                stOutMax += mx;
+                stOutLanes += __popc(__ballot_sync(0xffffffffu, hitsThis != 0));
+                stOutRounds += (tot + 31) / 32;
             }
         }
     };
@@ -1092,6 +1110,12 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     if (active && s == 0) a.nc[i - a.first] = nc;
     if constexpr (Stats)
     {
+        {
+            unsigned long long x = stPathWalks;
+            for (int o = 16; o > 0; o >>= 1)
+                x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) atomicAdd(a.stats + 31, x);
+        }
         unsigned long long v[5] = {stPair, stExact, stLeaves, stCand, stNodes};
 #pragma unroll
         for (int k = 0; k < 5; ++k)
@@ -1113,6 +1137,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             atomicAdd(a.stats + 25, (unsigned long long)(clock64() - t0));
             atomicAdd(a.stats + 26, stLeafCyc);
             atomicAdd(a.stats + 27, stLeafIdle);
+            atomicAdd(a.stats + 28, stOutMax);
+            atomicAdd(a.stats + 29, stOutLanes);
+            atomicAdd(a.stats + 30, stOutRounds);
             atomicAdd(a.stats + 7, 1ull);
             // slowest warp: [8] cycles, [9] its expansions, [10] leaves, [11] candidates, [12] loose flag,
             // [13] its first target; [14] number of loose warps

@@ -626,6 +626,10 @@ struct Pipeline final : PipelineBase
                              "[cstone_gb300 neighbour stats] cycles in leaf visits %.1f%% | leaf visits no lane "
                              "needed %.1f per warp\n",
                              100.0 * double(h[26]) / double(h[25]), double(h[27]) / h[7]);
+                std::fprintf(stderr,
+                             "[cstone_gb300 neighbour stats] output per warp: sum of the most hits of a lane per "
+                             "batch %.1f, lanes with hits %.1f, rounds of 32 hits %.1f | exact path walks %.2f\n",
+                             double(h[28]) / h[7], double(h[29]) / h[7], double(h[30]) / h[7], double(h[31]) / h[7]);
             }
         }
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_COUNT], s));
