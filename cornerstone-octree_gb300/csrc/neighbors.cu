@@ -395,8 +395,10 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
 // per-lane test (lower bound of the distance from x_i to the leaf box) that decides which lanes scan it.
 // ---------------------------------------------------------------------------------------------------------------
 constexpr int NBG_STACK = 192;
+// resident blocks of 4 warps per SM: 64 registers per thread (a few spilled to the L1-cached stack); 7 and 9 measured
+// slower on the 16M Plummer search
 #ifndef NBG_MIN_BLOCKS
-#define NBG_MIN_BLOCKS 7
+#define NBG_MIN_BLOCKS 8
 #endif
 
 // exact decision of a pair in the ambiguous band (T = double): d2 < r2 and the reference's path condition
@@ -470,9 +472,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     constexpr float KAPPA_REL = F64 ? 32.f * 2.220446e-16f : 32.f * 1.1920929e-7f;
     constexpr float RHO       = F64 ? 9.5367432e-7f : 7.6293945e-6f; // 2^-20, 2^-17
 
-    __shared__ int sStack[NB_WARPS][NBG_STACK];
-    __shared__ unsigned sMaskStack[NB_WARPS][NBG_STACK];
-    __shared__ int sC0Stack[NB_WARPS][NBG_STACK]; // child offset of each stacked node (<= 0: a leaf)
+    // stack entries (code, lane mask): code > 0 is the child offset of an internal node; a leaf is -(2 node + out) - 1,
+    // out = 1 when it holds particles outside its box
+    __shared__ int2 sStack[NB_WARPS][NBG_STACK];
     __shared__ float4 sCand[NB_WARPS][32];
     // S == 1: the staged candidates as separate x, y, z rows, read four at a time (two float2 pairs)
     __shared__ __align__(16) float sCx[NB_WARPS][32], sCy[NB_WARPS][32], sCz[NB_WARPS][32];
@@ -971,8 +973,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     int expansions            = 0;
     long long t0              = Stats ? clock64() : 0;
     float rminW               = Stats ? warpMinF(active ? rr : INFINITY) : 0.f;
-    int* stack                = sStack[warp];
-    unsigned* maskStack       = sMaskStack[warp];
+    int2* stack               = sStack[warp];
+    auto entryCode            = [](int node, int c0) { return c0 > 0 ? c0 : -(2 * node + (c0 < 0 ? 1 : 0)) - 1; };
 
     // one pass per set among the warp's targets (batched trees; a single pass otherwise)
     int mySet = 0, passSet = 0, lastSet = 0;
@@ -996,30 +998,29 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     rootNode   = a.numSets ? __ldg(a.setRoots + passSet) : 0;
     loose      = __any_sync(0xffffffffu, __fsqrt_ru(gR2) > 3.f * rmax);
     expansions = 0;
-    int* c0Stack = sC0Stack[warp];
     int top      = 0;
     const int rootC0 = __float_as_int(prep.nrec[3 * size_t(rootNode)].w);
     if (lane == 0)
     {
-        stack[0]     = rootNode;
-        maskStack[0] = activeMask;
-        c0Stack[0]   = rootC0;
+        stack[0] = make_int2(entryCode(rootNode, rootC0), int(activeMask));
     }
     top = activeMask ? 1 : 0;
     __syncwarp();
     while (top > 0)
     {
-        int node       = stack[top - 1];
-        unsigned pmask = maskStack[top - 1];
-        int c0         = c0Stack[top - 1];
+        const int2 ent       = stack[top - 1];
+        const unsigned pmask = unsigned(ent.y);
+        const int c0         = ent.x;
         --top;
-        if (c0 <= 0) // a leaf; -1: it holds particles outside its box
+        if (c0 <= 0) // a leaf
         {
+            const int node = (-c0 - 1) >> 1;
+            const bool out = (-c0 - 1) & 1;
             const float4* rec = prep.nrec + 3 * size_t(node);
             float4 recA = rec[0], recB = rec[1], recC = rec[2];
             long long tl0 = Stats ? clock64() : 0;
             unsigned long long before = stLeaves;
-            processLeaf(node, pmask, recA, recB, recC, c0 < 0);
+            processLeaf(node, pmask, recA, recB, recC, out);
             if constexpr (Stats)
             {
                 stLeafCyc += (unsigned long long)(clock64() - tl0);
@@ -1098,9 +1099,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         if (ok)
         {
             int pos        = top + __popc(m >> (lane + 1));
-            stack[pos]     = c0 + lane;
-            maskStack[pos] = cmask;
-            c0Stack[pos]   = childC0;
+            stack[pos] = make_int2(entryCode(c0 + lane, childC0), int(cmask));
         }
         top += __popc(m);
         __syncwarp();
@@ -1437,6 +1436,38 @@ template int nbPrepare<double>(cudaStream_t, const double*, const double*, const
                                const double*, const int32_t*, const int32_t*, const uint32_t*, int, void*, size_t,
                                NbPrep*);
 
+// The smallest shared-memory carveout that keeps NBG_MIN_BLOCKS blocks of the kernel resident (1 KB per block is
+// reserved by the runtime), so that the rest of the unified L1 / shared storage caches node records and candidates.
+// Set once per kernel.
+template<auto Kernel>
+static void preferL1()
+{
+    static const bool done = [] {
+        cudaFuncAttributes fa{};
+        int dev = 0, smemSM = 0;
+        if (cudaFuncGetAttributes(&fa, Kernel) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+            smemSM <= 0)
+        {
+            (void)cudaGetLastError();
+            return false;
+        }
+        const size_t need = size_t(NBG_MIN_BLOCKS) * (fa.sharedSizeBytes + 1024);
+        const int pct     = int(std::min<size_t>(100, (need * 100 + size_t(smemSM) - 1) / size_t(smemSM) + 1));
+        if (cudaFuncSetAttribute(Kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct) != cudaSuccess)
+            (void)cudaGetLastError();
+        return true;
+    }();
+    (void)done;
+}
+
+template<class T, bool Stats, int G>
+static void launchGroup(unsigned gblk, cudaStream_t s, const NbArgs<T>& a, const NbPrep& prep)
+{
+    preferL1<findNeighborsGroupKernel<T, Stats, G>>();
+    findNeighborsGroupKernel<T, Stats, G><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+}
+
 template<class T>
 int findNeighbors(cudaStream_t s, const NbArgs<T>& a0, const NbPrep& prep)
 {
@@ -1451,18 +1482,18 @@ int findNeighbors(cudaStream_t s, const NbArgs<T>& a0, const NbPrep& prep)
     unsigned gblk  = unsigned((gwarps + NB_WARPS - 1) / NB_WARPS);
     if (G == 8)
     {
-        if (a.stats) findNeighborsGroupKernel<T, true, 8><<<gblk, NB_THREADS, 0, s>>>(a, prep);
-        else findNeighborsGroupKernel<T, false, 8><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+        if (a.stats) launchGroup<T, true, 8>(gblk, s, a, prep);
+        else launchGroup<T, false, 8>(gblk, s, a, prep);
     }
     else if (G == 16)
     {
-        if (a.stats) findNeighborsGroupKernel<T, true, 16><<<gblk, NB_THREADS, 0, s>>>(a, prep);
-        else findNeighborsGroupKernel<T, false, 16><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+        if (a.stats) launchGroup<T, true, 16>(gblk, s, a, prep);
+        else launchGroup<T, false, 16>(gblk, s, a, prep);
     }
     else
     {
-        if (a.stats) findNeighborsGroupKernel<T, true, 32><<<gblk, NB_THREADS, 0, s>>>(a, prep);
-        else findNeighborsGroupKernel<T, false, 32><<<gblk, NB_THREADS, 0, s>>>(a, prep);
+        if (a.stats) launchGroup<T, true, 32>(gblk, s, a, prep);
+        else launchGroup<T, false, 32>(gblk, s, a, prep);
     }
     CSG_CHECK_LAUNCH();
     if (a.anyPbc)
