@@ -138,7 +138,7 @@ __device__ __forceinline__ uint32_t blockExclusiveScan256(uint32_t v, uint32_t* 
 }
 
 template<class K, bool Iota>
-__global__ void __launch_bounds__(RS_THREADS) onesweepKernel(const K* __restrict__ keysIn,
+__global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restrict__ keysIn,
                                                              const uint32_t* __restrict__ valsIn,
                                                              K* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
                                                              size_t n, int shift, uint32_t mask,
@@ -224,13 +224,36 @@ __global__ void __launch_bounds__(RS_THREADS) onesweepKernel(const K* __restrict
     uint32_t prefix = 0;
     if (tile > 0)
     {
+        // four predecessors per round (independent loads), consumed in order down to the first inclusive entry;
+        // an unpublished entry ends the round and is read again. Below tile 0 reads as an empty inclusive entry.
+        constexpr int LB = 4;
         long t          = long(tile) - 1;
         uint32_t spins  = 0;
         bool timedOut   = false;
-        while (t >= 0)
+        while (true)
         {
-            uint32_t st = vstatus[size_t(t) * RS_BINS + dg];
-            if ((st & ST_FLAGS) == 0)
+            uint32_t st[LB];
+#pragma unroll
+            for (int u = 0; u < LB; ++u)
+                st[u] = t - u >= 0 ? uint32_t(vstatus[size_t(t - u) * RS_BINS + dg]) : uint32_t(ST_INC);
+            int used  = 0;
+            bool done = false, wait = false;
+#pragma unroll
+            for (int u = 0; u < LB; ++u)
+            {
+                if (done || wait) continue;
+                if ((st[u] & ST_FLAGS) == 0)
+                {
+                    wait = true;
+                    continue;
+                }
+                prefix += st[u] & ST_COUNT;
+                used++;
+                if (st[u] & ST_INC) done = true;
+            }
+            if (done) break;
+            t -= used;
+            if (wait)
             {
                 if (++spins > SPIN_LIMIT)
                 {
@@ -238,11 +261,7 @@ __global__ void __launch_bounds__(RS_THREADS) onesweepKernel(const K* __restrict
                     break;
                 }
                 __nanosleep(20);
-                continue;
             }
-            prefix += st & ST_COUNT;
-            if (st & ST_INC) break;
-            --t;
         }
         if (timedOut) atomicOr(errWord, ERRBIT_SORT_TIMEOUT);
         vstatus[myIdx] = ST_INC | (prefix + total);
