@@ -478,6 +478,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     __shared__ float4 sCand[NB_WARPS][32];
     // S == 1: the staged candidates as separate x, y, z rows, read four at a time (two float2 pairs)
     __shared__ __align__(16) float sCx[NB_WARPS][32], sCy[NB_WARPS][32], sCz[NB_WARPS][32];
+    // S == 1: each lane's target for the by-target loop: negated frame coordinates and -Tin, and -Tup
+    __shared__ float4 sTgtA[NB_WARPS][32];
+    __shared__ float sTgtB[NB_WARPS][32];
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int t = lane % G, s = lane / G;
@@ -713,6 +716,12 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         nbS[2] = -float(zi);
     }
     const float nTinS = -Tin, nTupS = -Tup;
+    if constexpr (S == 1)
+    {
+        sTgtA[warp][lane] = make_float4(nbS[0], nbS[1], nbS[2], nTinS);
+        sTgtB[warp][lane] = nTupS;
+        __syncwarp();
+    }
     auto decideSlow = [&](uint32_t jj, int node, bool contained) -> bool {
         if constexpr (F64)
             return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
@@ -801,16 +810,24 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             // candidates of this batch that lie outside their leaf's box (only in marked leaves)
             const unsigned outB =
                 anyOut ? __ballot_sync(0xffffffffu, base + lane < last && prep.pout[base + lane]) : 0u;
-            __syncwarp();
-            if constexpr (S == 1)
-            {
-                sCx[warp][lane] = q.x;
-                sCy[warp][lane] = q.y;
-                sCz[warp][lane] = q.z;
-            }
-            else { sCand[warp][lane] = q; }
-            __syncwarp();
             int cnt = int(min(32u, last - base));
+            // S == 1: few needing lanes against many candidates are cheaper with the roles swapped (lanes hold the
+            // candidates, the warp loops over the needing targets): about 19 instructions per needing target against
+            // about 7 per candidate step of the per-lane loop (steps of eight; the ratio measured best between 19
+            // and 24 on the 16M Plummer search)
+            const bool byTarget = S == 1 && 19 * __popc(mask) < 7 * ((cnt + 7) & ~7);
+            if (!byTarget)
+            {
+                __syncwarp();
+                if constexpr (S == 1)
+                {
+                    sCx[warp][lane] = q.x;
+                    sCy[warp][lane] = q.y;
+                    sCz[warp][lane] = q.z;
+                }
+                else { sCand[warp][lane] = q; }
+                __syncwarp();
+            }
             long long tc0 = 0;
             unsigned hitsThis = 0;
             if constexpr (Stats)
@@ -864,7 +881,33 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                 const float2 n[3] = {make_float2(nbS[0], nbS[0]), make_float2(nbS[1], nbS[1]),
                                      make_float2(nbS[2], nbS[2])};
                 const float2 nin = make_float2(nTinS, nTinS), nup = make_float2(nTupS, nTupS);
-                if (need)
+                if (byTarget)
+                {
+                    // lane k holds candidate k (past the leaf's end: a point at infinity); per needing target t the
+                    // same FP32 expressions as four(), and the two signs collected by ballots (bit k: candidate k)
+                    unsigned mm = mask, bi = 0, ba = 0;
+                    while (mm)
+                    {
+                        const int t = __ffs(mm) - 1;
+                        mm &= mm - 1;
+                        const float4 tg = sTgtA[warp][t];
+                        const float tup = sTgtB[warp][t];
+                        const float dx = __fadd_rn(q.x, tg.x), dy = __fadd_rn(q.y, tg.y), dz = __fadd_rn(q.z, tg.z);
+                        float e;
+                        if constexpr (F64) e = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                        else e = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        const unsigned mi = __ballot_sync(0xffffffffu, __float_as_int(__fadd_rn(e, tg.w)) < 0);
+                        const unsigned ma = __ballot_sync(0xffffffffu, __float_as_int(__fadd_rn(e, tup)) < 0);
+                        if (lane == t)
+                        {
+                            bi = mi;
+                            ba = ma;
+                        }
+                    }
+                    inM  = __brev(bi);
+                    ambM = __brev(ba);
+                }
+                else if (need)
                 {
                     // eight independent distance chains per step; the staged points past the leaf's end never pass
                     int steps = 0;
@@ -879,6 +922,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                         inM <<= 32 - steps;
                         ambM <<= 32 - steps;
                     }
+                }
+                if (need)
+                {
                     ambM &= ~inM;
                     const unsigned outR = __brev(outB); // bit 31 - k: candidate k lies outside its leaf's box
                     // candidates outside their leaf's box: no path-safe shortcut; a neighbour iff within r and the
