@@ -453,6 +453,65 @@ __device__ __noinline__ bool pathCheckF32(float xi, float yi, float zi, float ce
     }
 }
 
+// The group traversal's rare exact decisions reload the target (coordinates, h; r2 and cellR2 recomputed with the
+// expressions of the kernel's start) instead of keeping them in registers through the whole traversal.
+template<class T>
+struct TargetRef
+{
+    const T *x, *y, *z, *h;
+    float ext;
+    uint32_t i;
+};
+
+template<class T>
+__device__ __forceinline__ void loadTarget(const TargetRef<T>& t, T& xi, T& yi, T& zi, T& r2, T& cellR2)
+{
+    xi       = t.x[t.i];
+    yi       = t.y[t.i];
+    zi       = t.z[t.i];
+    T hi     = t.h[t.i];
+    r2       = RN<T>::mul(RN<T>::mul(T(4.0), hi), hi);
+    cellR2   = RN<T>::mul(RN<T>::mul(r2, T(t.ext)), T(t.ext));
+}
+
+// a candidate in the FP32 band (T = double) or past Tsafe (T = float): the pair and path decision
+template<class T>
+__device__ __noinline__ bool slowPairAt(TargetRef<T> t, float kappa, uint32_t j, int leafNode, const int32_t* parents,
+                                        const T* centers, const T* sizes, bool contained, int rootNode)
+{
+    T xi, yi, zi, r2, cellR2;
+    loadTarget(t, xi, yi, zi, r2, cellR2);
+    if constexpr (std::is_same_v<T, double>)
+        return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), t.x, t.y, t.z, j, leafNode, parents, centers,
+                             sizes, contained, rootNode);
+    else
+        return pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), leafNode, parents,
+                            reinterpret_cast<const float*>(centers), reinterpret_cast<const float*>(sizes), rootNode);
+}
+
+// the path condition to a leaf (its candidates outside its box have no path-safe shortcut)
+template<class T>
+__device__ __noinline__ bool leafPathAt(TargetRef<T> t, int leafNode, const int32_t* parents, const T* centers,
+                                        const T* sizes, int rootNode)
+{
+    T xi, yi, zi, r2, cellR2;
+    loadTarget(t, xi, yi, zi, r2, cellR2);
+    if constexpr (std::is_same_v<T, double>)
+        return pathExactF64(xi, yi, zi, cellR2, leafNode, parents, centers, sizes, rootNode);
+    else
+        return pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), leafNode, parents,
+                            reinterpret_cast<const float*>(centers), reinterpret_cast<const float*>(sizes), rootNode);
+}
+
+// exact d2 < r2 of a pair (T = double, no periodic axis)
+__device__ __noinline__ bool pairWithinAt(TargetRef<double> t, uint32_t j)
+{
+    double xi, yi, zi, r2, cellR2;
+    loadTarget(t, xi, yi, zi, r2, cellR2);
+    const PbcArgs open{};
+    return pairExactF64(xi, yi, zi, false, r2, t.x, t.y, t.z, j, open);
+}
+
 __device__ __forceinline__ float warpMinF(float v)
 {
     for (int o = 16; o > 0; o >>= 1)
@@ -722,13 +781,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         sTgtB[warp][lane] = nTupS;
         __syncwarp();
     }
+    const TargetRef<T> tref{a.x, a.y, a.z, a.h, a.ext, i};
     auto decideSlow = [&](uint32_t jj, int node, bool contained) -> bool {
-        if constexpr (F64)
-            return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), a.x, a.y, a.z, jj, node, a.parents,
-                                 a.centers, a.sizes, contained, rootNode);
-        else
-            return pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
-                                reinterpret_cast<const float*>(a.centers), reinterpret_cast<const float*>(a.sizes), rootNode);
+        return slowPairAt<T>(tref, kappa, jj, node, a.parents, a.centers, a.sizes, contained, rootNode);
     };
     // first filter: FP32 distance of the staged candidate; returns d2 and whether it can be a neighbour
     auto filter = [&](float4 c, float& d2) -> bool {
@@ -791,12 +846,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             if (!(n2u < tsafe))
             {
                 if constexpr (Stats) stPathWalks++;
-                if constexpr (F64)
-                    leafPass = pathExactF64(xi, yi, zi, cellR2, node, a.parents, a.centers, a.sizes, rootNode);
-                else
-                    leafPass = pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), node, a.parents,
-                                            reinterpret_cast<const float*>(a.centers),
-                                            reinterpret_cast<const float*>(a.sizes), rootNode);
+                leafPass = leafPathAt<T>(tref, node, a.parents, a.centers, a.sizes, rootNode);
             }
         }
         if constexpr (Stats)
@@ -938,14 +988,13 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                         inM |= fIn;
                         if constexpr (F64)
                         {
-                            const PbcArgs open{}; // group warps have no periodic sphere
+                            // group warps have no periodic sphere
                             unsigned f = fAmb;
                             while (f)
                             {
                                 int k = __clz(f);
                                 f &= ~(0x80000000u >> k);
-                                if (pairExactF64(xi, yi, zi, false, r2, a.x, a.y, a.z, base + k, open))
-                                    inM |= 0x80000000u >> k;
+                                if (pairWithinAt(tref, base + k)) inM |= 0x80000000u >> k;
                             }
                         }
                         else { inM |= fAmb; }
