@@ -912,11 +912,21 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                         float2 e;
                         if constexpr (F64)
                         {
+                            // an FP32 filter with proven margins: any rounding of these FMAs stays inside them
                             e = __fmul2_rn(dx, dx);
                             e = __ffma2_rn(dy, dy, e);
                             e = __ffma2_rn(dz, dz, e);
                         }
-                        else { e = __fadd2_rn(__fadd2_rn(__fmul2_rn(dx, dx), __fmul2_rn(dy, dy)), __fmul2_rn(dz, dz)); }
+                        else
+                        {
+                            // the reference's FP32 distance itself, so no product may be fused into the next add:
+                            // scalar __fmul_rn / __fadd_rn (a packed multiply followed by a packed add was measured to
+                            // round once, as a fused multiply-add, even with explicit rounding modifiers)
+                            auto d2 = [](float a, float b, float c) {
+                                return __fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c));
+                            };
+                            e = make_float2(d2(dx.x, dy.x, dz.x), d2(dx.y, dy.y, dz.y));
+                        }
                         const float2 ti = __fadd2_rn(e, nin), tu = __fadd2_rn(e, nup);
                         mi = __funnelshift_l(__float_as_uint(ti.x), mi, 1);
                         mi = __funnelshift_l(__float_as_uint(ti.y), mi, 1);

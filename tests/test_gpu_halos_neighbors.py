@@ -160,3 +160,28 @@ def test_neighbors_particles_outside_their_leaf_box(cs, O, bits):
     if bits == 32:
         _, counts = brute_force_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], lo, hi, False)
         assert (counts != rnc).any()  # the case is exercised: the reference drops a pair within the radius
+
+
+def test_fp32_pair_at_the_radius_is_not_a_neighbour(cs, O):
+    """FP32 coordinates: a candidate whose squared distance RN(RN(RN(dx dx) + RN(dy dy)) + RN(dz dz)) equals r2 exactly
+    is not a neighbour (d2 < r2 is false), although the same sum with the first product fused into the add lies one
+    ulp below r2. Forty coincident targets make every lane of the warp need the candidate's leaf, so the per-lane
+    candidate loop decides it (the pair came from a 783k-particle uniform set of the batched workload)."""
+    f = np.float32
+    xi = (float.fromhex("0x1.f91c64p-3"), float.fromhex("0x1.388148p-5"), float.fromhex("0x1.2841eap-1"))
+    xc = (float.fromhex("0x1.423806p-2"), float.fromhex("0x1.b76b46p-5"), float.fromhex("0x1.26c99cp-1"))
+    hv = f(float.fromhex("0x1.1e079p-5"))
+    d = [f(f(a) - f(b)) for a, b in zip(xc, xi)]
+    assert f(f(f(d[0] * d[0]) + f(d[1] * d[1])) + f(d[2] * d[2])) == f(f(f(4) * hv) * hv)  # exactly at the radius
+    rng = np.random.default_rng(23)
+    fill = rng.random((3, 3000)).astype(f)
+    x, y, z = (np.concatenate([np.full(40, a, f), [f(b)], fill[k]]) for k, (a, b) in enumerate(zip(xi, xc)))
+    n = x.size
+    h = np.full(n, hv, f)
+    ngmax = 100
+    ref, obox, box, o, layout, c, s, (tx, ty, tz, th) = _setup(O, cs, x, y, z, h, 0.0, 1.0, 0, 16, 0, 32)
+    rnb, rnc = O.find_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], 0, n, obox, ref["tree"], ref["layout"],
+                                ref["centers"], ref["sizes"], ngmax)
+    nb, nc = cs.find_neighbors(tx, ty, tz, th, 0, n, box, o, layout, c, s, ngmax)
+    torch.cuda.synchronize()
+    neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)
