@@ -64,6 +64,7 @@ __global__ void setRootsKernel(const uint64_t* __restrict__ prefixes, const int3
 struct BatchBase
 {
     cs_batch_config cfg{};
+    cs_tuning tuning{32, 7};
     virtual ~BatchBase() = default;
     virtual int run(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, const uint32_t* off,
                     int S, const cs_box* boxes, const uint32_t* buckets, cs_batch_result* res) = 0;
@@ -285,8 +286,10 @@ struct Batch final : BatchBase
                           layout.as<uint32_t>(), centers.p, sizes.p, cfg.search_ext};
             NbArgs<T> a  = makeNbArgs<T>(xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), 0, uint32_t(n), open, nv,
                                          cfg.ngmax, nb.as<uint32_t>(), nc.as<uint32_t>());
-            a.errWord    = err + 3;
-            a.setOffsets = setOff.as<uint32_t>();
+            a.errWord      = err + 3;
+            a.groupSize    = tuning.nb_group;
+            a.byTargetCost = tuning.nb_by_target_cost;
+            a.setOffsets   = setOff.as<uint32_t>();
             a.setRoots   = roots.as<int32_t>();
             a.numSets    = S;
             if ((rc = findNeighbors<T>(s, a, prep))) return rc;
@@ -368,6 +371,18 @@ extern "C" int cs_batch_create(cs_batch* out, const cs_batch_config* cfg)
 extern "C" int cs_batch_destroy(cs_batch b)
 {
     delete b;
+    return CS_OK;
+}
+
+extern "C" int cs_batch_set_tuning(cs_batch b, const cs_tuning* t)
+{
+    if (!b || !t || !(t->nb_group == 8 || t->nb_group == 16 || t->nb_group == 32) || t->nb_by_target_cost < 0 ||
+        t->nb_by_target_cost > 64)
+    {
+        setLastError("batch set tuning: nb_group must be 8, 16 or 32 and nb_by_target_cost in [0, 64]");
+        return CS_ERR_INVALID;
+    }
+    b->impl->tuning = *t;
     return CS_OK;
 }
 

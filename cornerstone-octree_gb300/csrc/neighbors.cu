@@ -863,9 +863,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             int cnt = int(min(32u, last - base));
             // S == 1: few needing lanes against many candidates are cheaper with the roles swapped (lanes hold the
             // candidates, the warp loops over the needing targets): about 19 instructions per needing target against
-            // about 7 per candidate step of the per-lane loop (steps of eight; the ratio measured best between 19
-            // and 24 on the 16M Plummer search)
-            const bool byTarget = S == 1 && 19 * __popc(mask) < 7 * ((cnt + 7) & ~7);
+            // about byTargetCost (default 7) per candidate step of the per-lane loop (steps of eight; on the 16M
+            // Plummer search the ratio 19 : 7 measured as good as any between 19 : 9 and 24 : 7)
+            const bool byTarget = S == 1 && 19 * __popc(mask) < a.byTargetCost * ((cnt + 7) & ~7);
             if (!byTarget)
             {
                 __syncwarp();
@@ -1582,7 +1582,6 @@ int findNeighbors(cudaStream_t s, const NbArgs<T>& a0, const NbPrep& prep)
     NbArgs<T> a   = a0;
     a.pathOnlyPbcWarps = 0;
     int G = a.groupSize == 8 || a.groupSize == 16 || a.groupSize == 32 ? a.groupSize : 32;
-    if (const char* env = std::getenv("CSTONE_GB300_NB_GROUP")) G = std::atoi(env) == 8 ? 8 : std::atoi(env) == 32 ? 32 : 16;
     size_t gwarps  = (size_t(a.last - a.first) + G - 1) / G;
     unsigned gblk  = unsigned((gwarps + NB_WARPS - 1) / NB_WARPS);
     if (G == 8)

@@ -32,6 +32,9 @@ struct NbArgs
     uint32_t* errWord = nullptr;
     //! targets per warp of the group traversal (8, 16 or 32)
     int groupSize = 32;
+    //! one target per lane (groupSize 32): a candidate batch runs the by-target loop when 19 x (needing lanes) is
+    //! below byTargetCost x (candidate steps of the per-lane loop); 0 never. Speed only, results do not change
+    int byTargetCost = 7;
     //! many independent sets in one tree (may be null): the sorted particles of set s are [setOffsets[s],
     //! setOffsets[s + 1]) and its traversal starts at node setRoots[s] instead of the root
     const uint32_t* setOffsets = nullptr;

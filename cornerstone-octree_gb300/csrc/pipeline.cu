@@ -108,6 +108,62 @@ struct Pipeline final : PipelineBase
         incCur = -1;
     }
 
+    const void* lastIn[4] = {};
+    size_t lastNIn        = 0;
+    cs_box lastBox{};
+    uint64_t lastF0 = 0, lastF1 = 0;
+
+    // Each candidate reruns the last run's inputs (device arrays, or the device copies of host inputs) reps times and
+    // is scored by the mean device time of the neighbour stage. The results do not depend on the tuning.
+    int autotune(cudaStream_t s, int reps, cs_tuning* best, cs_tuning* tried, float* ms, int capacity,
+                 int* count) override
+    {
+        if (!lastNIn || !cfg.do_neighbors)
+        {
+            setLastError("autotune: needs a previous run with neighbours");
+            return CS_ERR_INVALID;
+        }
+        static constexpr cs_tuning candidates[] = {{32, 7}, {32, 0}, {32, 5}, {32, 10}, {16, 7}, {8, 7}};
+        const void* in[4] = {lastIn[0], lastIn[1], lastIn[2], lastIn[3]};
+        const size_t n0   = lastNIn;
+        const cs_box box0 = lastBox;
+        const uint64_t f0 = lastF0, f1 = lastF1;
+        const cs_tuning keep = tuning;
+        cs_tuning win        = keep;
+        float winMs          = 0.f;
+        int k                = 0;
+        for (const cs_tuning& c : candidates)
+        {
+            tuning    = c;
+            float acc = 0.f;
+            for (int r = 0; r < std::max(1, reps); ++r)
+            {
+                int rc = run(s, in[0], in[1], in[2], in[3], n0, box0, f0, f1, nullptr, false);
+                if (rc)
+                {
+                    tuning = keep;
+                    return rc;
+                }
+                float t = 0.f;
+                CSG_CUDA_TRY(cudaEventSynchronize(ev[ST_COUNT]));
+                CSG_CUDA_TRY(cudaEventElapsedTime(&t, ev[ST_NEIGHBORS], ev[ST_COUNT]));
+                acc += t;
+            }
+            acc /= float(std::max(1, reps));
+            if (k < capacity)
+            {
+                if (tried) tried[k] = c;
+                if (ms) ms[k] = acc;
+            }
+            ++k;
+            if (k == 1 || acc < winMs) win = c, winMs = acc;
+        }
+        tuning = win;
+        if (best) *best = win;
+        if (count) *count = k;
+        return CS_OK;
+    }
+
     // grow a buffer keeping its first keep bytes (stream-ordered copy, then the old buffer is released)
     static int growKeep(DevBuf& b, size_t need, size_t keep, cudaStream_t s)
     {
@@ -251,6 +307,8 @@ struct Pipeline final : PipelineBase
             NbArgs<T> a = makeNbArgs<T>(xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), 0, uint32_t(nIn), box, nv,
                                         cfg.ngmax, nb.as<uint32_t>(), nc.as<uint32_t>());
             a.errWord   = err + 3;
+            a.groupSize    = tuning.nb_group;
+            a.byTargetCost = tuning.nb_by_target_cost;
             if ((rc = findNeighbors<T>(s, a, prep))) return rc;
         }
         CSG_CUDA_TRY(rec(ev[ST_COUNT]));
@@ -419,6 +477,9 @@ struct Pipeline final : PipelineBase
             z = inZ.as<T>();
             h = inH.as<T>();
         }
+        // device inputs of this run (the copies of host inputs), for autotune
+        lastIn[0] = x, lastIn[1] = y, lastIn[2] = z, lastIn[3] = h;
+        lastNIn = n, lastBox = box, lastF0 = f0, lastF1 = f1;
         for (DevBuf* b : {&keys, &keysAlt})
             if ((rc = b->ensure(n * sizeof(K)))) return rc;
         for (DevBuf* b : {&order, &orderAlt})
@@ -585,6 +646,8 @@ struct Pipeline final : PipelineBase
             NbArgs<T> a = makeNbArgs<T>(xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), 0, uint32_t(n), box, nv,
                                         cfg.ngmax, nb.as<uint32_t>(), nc.as<uint32_t>());
             a.errWord   = err + 3;
+            a.groupSize    = tuning.nb_group;
+            a.byTargetCost = tuning.nb_by_target_cost;
             if (statsOn)
             {
                 if ((rc = nbStats.ensure(32 * sizeof(unsigned long long)))) return rc;
@@ -807,6 +870,41 @@ extern "C" int cs_pipeline_run_host(cs_pipeline p, cs_stream_t stream, const voi
     int rc = p->impl->run(cudaStream_t(stream), x, y, z, h, n, *box, f0, f1, res, true);
     if (rc) return rc;
     return p->impl->copyBack(cudaStream_t(stream), ncHost, flagsHost, flagsCap);
+}
+
+extern "C" int cs_pipeline_set_tuning(cs_pipeline p, const cs_tuning* t)
+{
+    if (!p || !t || !(t->nb_group == 8 || t->nb_group == 16 || t->nb_group == 32) || t->nb_by_target_cost < 0 ||
+        t->nb_by_target_cost > 64)
+    {
+        setLastError("set tuning: nb_group must be 8, 16 or 32 and nb_by_target_cost in [0, 64]");
+        return CS_ERR_INVALID;
+    }
+    p->impl->tuning = *t;
+    p->impl->resetSteps(); // captured step graphs hold the old launch arguments
+    return CS_OK;
+}
+
+extern "C" int cs_pipeline_get_tuning(cs_pipeline p, cs_tuning* t)
+{
+    if (!p || !t)
+    {
+        setLastError("get tuning: null argument");
+        return CS_ERR_INVALID;
+    }
+    *t = p->impl->tuning;
+    return CS_OK;
+}
+
+extern "C" int cs_pipeline_autotune(cs_pipeline p, cs_stream_t stream, int reps, cs_tuning* best, cs_tuning* tried,
+                                    float* ms, int capacity, int* count)
+{
+    if (!p || reps < 1 || capacity < 0)
+    {
+        setLastError("autotune: invalid argument");
+        return CS_ERR_INVALID;
+    }
+    return p->impl->autotune(cudaStream_t(stream), reps, best, tried, ms, capacity, count);
 }
 
 extern "C" int cs_pipeline_step(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,

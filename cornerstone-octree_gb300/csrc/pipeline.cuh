@@ -33,7 +33,11 @@ struct PipelineBase
     virtual int step(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, size_t n,
                      const cs_box& box, bool useGraph, cs_pipeline_result* res) = 0;
     virtual void resetSteps() = 0;
+    //! times the neighbour search of the last run's inputs for each candidate tuning and keeps the fastest
+    virtual int autotune(cudaStream_t s, int reps, cs_tuning* best, cs_tuning* tried, float* ms, int capacity,
+                         int* count) = 0;
     int graphReplays = 0; // steps of the last step sequence that were replayed from a captured graph
+    cs_tuning tuning{32, 7};
     cudaEvent_t ev[ST_COUNT + 1] = {};
     float stageMs[ST_COUNT]      = {};
     int lastN                    = 0;

@@ -340,6 +340,19 @@ class PipelineOutputs(C.Structure):
 lib.cs_pipeline_device_bytes.restype = C.c_size_t
 lib.cs_pipeline_device_bytes.argtypes = [C.c_void_p]
 
+
+class Tuning(C.Structure):
+    """speed knobs of the neighbour traversal (results do not depend on them): targets per warp (32, 16, 8) and the
+    by-target switch cost (0: never)"""
+    _fields_ = [("nb_group", C.c_int), ("nb_by_target_cost", C.c_int)]
+
+    def as_dict(self):
+        return {"nb_group": self.nb_group, "nb_by_target_cost": self.nb_by_target_cost}
+
+
+lib.cs_pipeline_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                     C.c_void_p]
+
 STAGES = ("keys", "sort", "gather", "build", "link", "geometry", "nbprep", "halos", "neighbors")
 
 
@@ -392,6 +405,24 @@ class Pipeline:
         ms = (C.c_float * len(STAGES))()
         _check(lib.cs_pipeline_stage_times(self.handle, ms, len(STAGES)))
         return dict(zip(STAGES, list(ms)))
+
+    def set_tuning(self, nb_group=32, nb_by_target_cost=7):
+        t = Tuning(nb_group, nb_by_target_cost)
+        _check(lib.cs_pipeline_set_tuning(self.handle, C.byref(t)))
+
+    def get_tuning(self):
+        t = Tuning()
+        _check(lib.cs_pipeline_get_tuning(self.handle, C.byref(t)))
+        return t.as_dict()
+
+    def autotune(self, reps=2):
+        """times the neighbour stage of the last run's inputs for each candidate tuning and keeps the fastest;
+        returns {"best": tuning, "tried": [(tuning, ms), ...]}"""
+        cap = 16
+        best, tried, ms, count = Tuning(), (Tuning * cap)(), (C.c_float * cap)(), C.c_int()
+        _check(lib.cs_pipeline_autotune(self.handle, _stream(), int(reps), C.byref(best), tried, ms, cap,
+                                        C.byref(count)))
+        return {"best": best.as_dict(), "tried": [(tried[k].as_dict(), float(ms[k])) for k in range(count.value)]}
 
     def device_bytes(self):
         return lib.cs_pipeline_device_bytes(self.handle)
@@ -462,6 +493,10 @@ class Batch:
         if getattr(self, "handle", None):
             lib.cs_batch_destroy(self.handle)
             self.handle = None
+
+    def set_tuning(self, nb_group=32, nb_by_target_cost=7):
+        t = Tuning(nb_group, nb_by_target_cost)
+        _check(lib.cs_batch_set_tuning(self.handle, C.byref(t)))
 
     def run(self, x, y, z, h, offsets, boxes, buckets):
         """x..h: device tensors of all sets concatenated; offsets: S + 1 ints; boxes: S cs_box; buckets: S ints"""

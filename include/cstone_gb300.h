@@ -364,6 +364,29 @@ int cs_pipeline_reset_steps(cs_pipeline p);
 /* steps of the current sequence that were replayed from a captured graph */
 int cs_pipeline_graph_replays(cs_pipeline p);
 
+/* ---- tuning: knobs that change the speed of a pipeline, never its results -----------------------------------------
+ * nb_group: targets per warp of the neighbour traversal (32, 16 or 8; 1, 2 or 4 lanes per target).
+ * nb_by_target_cost: with one target per lane, a candidate batch that few lanes need runs the by-target loop (lanes
+ * hold the candidates, the warp loops over the needing targets) when 19 x (needing lanes) < nb_by_target_cost x (the
+ * per-lane loop's candidate steps); 0 never. Default {32, 7}. Setting a tuning ends a step sequence (the next
+ * cs_pipeline_step builds from the root). The reference has no counterpart: its traversal shape is the compile-time
+ * TravConfig (traversal/find_neighbors.cuh:29-58). */
+typedef struct
+{
+    int nb_group;
+    int nb_by_target_cost;
+} cs_tuning;
+
+int cs_pipeline_set_tuning(cs_pipeline p, const cs_tuning* tuning);
+int cs_pipeline_get_tuning(cs_pipeline p, cs_tuning* tuning);
+/* Autotuner: reruns the inputs of the last cs_pipeline_run / cs_pipeline_run_host (device input arrays must still be
+ * valid) reps times for each candidate tuning ({32, 7}, {32, 0}, {32, 5}, {32, 10}, {16, 7}, {8, 7}), scores each by
+ * the mean device time of the neighbour stage, and keeps the fastest as the pipeline's tuning. Writes the best, and
+ * up to capacity candidates with their mean ms (tried / ms may be NULL); *count = candidates run. The outputs
+ * afterwards are those of the last candidate's run (identical for every tuning). */
+int cs_pipeline_autotune(cs_pipeline p, cs_stream_t stream, int reps, cs_tuning* best, cs_tuning* tried, float* ms,
+                         int capacity, int* count);
+
 /* device time in ms of each stage of the last run: keys, sort, gather, build, link, geometry, float node boxes
  * (node preparation of the halo and neighbour searches), halos, neighbours (count <= 9 values); waits for the last
  * run to finish */
@@ -413,6 +436,8 @@ typedef struct
 } cs_batch_outputs;
 int cs_batch_create(cs_batch* out, const cs_batch_config* cfg);
 int cs_batch_destroy(cs_batch b);
+/* the neighbour traversal's tuning for later runs (as cs_pipeline_set_tuning; results do not change) */
+int cs_batch_set_tuning(cs_batch b, const cs_tuning* tuning);
 int cs_batch_run(cs_batch b, cs_stream_t stream, const void* x, const void* y, const void* z, const void* h,
                  const uint32_t* set_offsets_host, int32_t num_sets, const cs_box* boxes_host,
                  const uint32_t* buckets_host, cs_batch_result* result);
