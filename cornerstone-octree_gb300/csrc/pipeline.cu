@@ -26,7 +26,9 @@ namespace csg
 template<class T, class K>
 struct Pipeline final : PipelineBase
 {
-    DevBuf inX, inY, inZ, inH;
+    // device copies of host inputs: two sets used in turn, so that a run's input copies overlap the previous run
+    DevBuf inBuf[2][4];
+    int inSet = 0;
     DevBuf keys, keysAlt, order, orderAlt;
     DevBuf xs, ys, zs, hs;
     DevBuf packed, shadowHi, shadowLo; // x,y,z,h records of the keys pass; float shadows made by the gather
@@ -64,7 +66,16 @@ struct Pipeline final : PipelineBase
     // host inputs: the copy stream, one event per chunk copied, and the fork point
     static constexpr int kCopyChunks = 4;
     cudaStream_t copyStream          = nullptr;
-    cudaEvent_t copyEv[kCopyChunks + 1] = {};
+    cudaEvent_t copyEv[kCopyChunks]  = {};
+    cudaEvent_t inUsed[2]            = {}; // on the compute stream after the keys of the last run that read the set
+    bool inUsedRec[2]                = {false, false};
+    // results to host: a stream of their own; the error words first (errCopied), then counts and flags (outDone)
+    cudaStream_t d2hStream = nullptr;
+    cudaEvent_t outReady = nullptr, errCopied = nullptr, outDone = nullptr;
+    uint32_t* herrHost   = nullptr; // pinned, the last copied error words
+    bool outPending      = false;   // a copy-back whose errors are not yet reported
+    int stickyRc         = CS_OK;   // an earlier run's device error, reported by the next wait
+    char stickyMsg[160]  = {};
     const void* outLeaves      = nullptr;
     const uint32_t* outCounts  = nullptr;
     // opt-in traversal statistics of the neighbour search, printed to stderr (CSTONE_GB300_NB_STATS=1)
@@ -88,6 +99,12 @@ struct Pipeline final : PipelineBase
         if (copyStream) cudaStreamDestroy(copyStream);
         for (auto& e : copyEv)
             if (e) cudaEventDestroy(e);
+        for (auto& e : inUsed)
+            if (e) cudaEventDestroy(e);
+        if (d2hStream) cudaStreamDestroy(d2hStream);
+        for (cudaEvent_t e : {outReady, errCopied, outDone})
+            if (e) cudaEventDestroy(e);
+        if (herrHost) cudaFreeHost(herrHost);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
     }
@@ -319,6 +336,7 @@ struct Pipeline final : PipelineBase
              const cs_box& box, bool useGraph, cs_pipeline_result* res) override
     {
         int rc;
+        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, outDone, 0)); // a copy-back still reads the outputs
         if (incCur < 0 || nIn != incN)
         {
             // the first step of a sequence builds from the root and becomes the current tree; the step buffers are
@@ -436,7 +454,8 @@ struct Pipeline final : PipelineBase
     size_t deviceBytes() const override
     {
         size_t t = 0;
-        for (const DevBuf* b : {&inX, &inY, &inZ, &inH, &keys, &keysAlt, &order, &orderAlt, &xs, &ys, &zs, &hs,
+        for (const DevBuf* b : {&inBuf[0][0], &inBuf[0][1], &inBuf[0][2], &inBuf[0][3], &inBuf[1][0], &inBuf[1][1],
+                                &inBuf[1][2], &inBuf[1][3], &keys, &keysAlt, &order, &orderAlt, &xs, &ys, &zs, &hs,
                                 &packed, &shadowHi, &shadowLo, &pout, &sortWs, &errWords, &buildWs, &leaves, &counts,
                                 &layout, &prefixes, &childOffsets,
                                 &parents, &levelRange, &i2l, &l2i, &linkWs, &centers, &sizes, &sc, &ss, &flags,
@@ -461,8 +480,8 @@ struct Pipeline final : PipelineBase
                 *h = static_cast<const T*>(hv);
         if (hostIn)
         {
-            for (DevBuf* b : {&inX, &inY, &inZ, &inH})
-                if ((rc = b->ensure(n * sizeof(T)))) return rc;
+            for (DevBuf& b : inBuf[inSet])
+                if ((rc = b.ensure(n * sizeof(T)))) return rc;
             // the host arrays arrive in chunks on a copy stream, the keys of chunk c computed while chunk c + 1
             // travels (the keys are per particle); concurrent copies would share the host link and gain nothing
             if (!copyStream)
@@ -470,12 +489,14 @@ struct Pipeline final : PipelineBase
                 CSG_CUDA_TRY(cudaStreamCreateWithFlags(&copyStream, cudaStreamNonBlocking));
                 for (auto& e : copyEv)
                     CSG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                for (auto& e : inUsed)
+                    CSG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             }
             hostSrc[0] = x, hostSrc[1] = y, hostSrc[2] = z, hostSrc[3] = h;
-            x = inX.as<T>();
-            y = inY.as<T>();
-            z = inZ.as<T>();
-            h = inH.as<T>();
+            x = inBuf[inSet][0].as<T>();
+            y = inBuf[inSet][1].as<T>();
+            z = inBuf[inSet][2].as<T>();
+            h = inBuf[inSet][3].as<T>();
         }
         // device inputs of this run (the copies of host inputs), for autotune
         lastIn[0] = x, lastIn[1] = y, lastIn[2] = z, lastIn[3] = h;
@@ -500,16 +521,19 @@ struct Pipeline final : PipelineBase
         // coordinate bound (float, atomic max from 0)
         uint32_t* err = errWords.as<uint32_t>();
         float* cmax   = reinterpret_cast<float*>(err + 8);
+        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, errCopied, 0)); // the previous copy-back read them
         CSG_CUDA_TRY(cudaMemsetAsync(err, 0, 64, s));
 
         if (hostIn)
         {
             // chunk c: four copies on the copy stream, then its keys on s; the keys stage of a host run begins when
             // the first chunk has arrived and so includes the copies of the others
+            // the copies wait only for the last reader of this input set (the keys of the run before the previous
+            // one), so that they overlap the previous run's computation
             const size_t chunk = ((n + kCopyChunks - 1) / kCopyChunks + 255) & ~size_t(255);
-            CSG_CUDA_TRY(cudaEventRecord(copyEv[kCopyChunks], s));
-            CSG_CUDA_TRY(cudaStreamWaitEvent(copyStream, copyEv[kCopyChunks], 0));
-            T* dst[4] = {inX.as<T>(), inY.as<T>(), inZ.as<T>(), inH.as<T>()};
+            if (inUsedRec[inSet]) CSG_CUDA_TRY(cudaStreamWaitEvent(copyStream, inUsed[inSet], 0));
+            T* dst[4] = {inBuf[inSet][0].as<T>(), inBuf[inSet][1].as<T>(), inBuf[inSet][2].as<T>(),
+                         inBuf[inSet][3].as<T>()};
             for (int c = 0; c < kCopyChunks && size_t(c) * chunk < n; ++c)
             {
                 const size_t a = size_t(c) * chunk, m = std::min(chunk, n - a);
@@ -523,6 +547,9 @@ struct Pipeline final : PipelineBase
                                               packed.as<PackedT<T>>() + a, m, box, cfg.sfc_kind)))
                     return rc;
             }
+            CSG_CUDA_TRY(cudaEventRecord(inUsed[inSet], s));
+            inUsedRec[inSet] = true;
+            inSet ^= 1;
         }
         else
         {
@@ -619,6 +646,7 @@ struct Pipeline final : PipelineBase
         // ---- halos for the focus leaves ----
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_HALOS], s));
         if ((rc = flags.ensure(size_t(N)))) return rc;
+        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, outDone, 0)); // the previous copy-back of flags, counts
         CSG_CUDA_TRY(cudaMemsetAsync(flags.p, 0, size_t(N), s));
         if (cfg.do_halos && br.focusLast > br.focusFirst)
         {
@@ -706,21 +734,9 @@ struct Pipeline final : PipelineBase
         return CS_OK;
     }
 
-    int copyBack(cudaStream_t s, uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap) override
+    // the error words of a finished copy-back as a status (and message)
+    static int deviceErrors(const uint32_t* herr)
     {
-        if (ncHost) CSG_CUDA_TRY(cudaMemcpyAsync(ncHost, nc.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-        if (flagsHost)
-        {
-            if (flagsCap < size_t(last.num_nodes))
-            {
-                setLastError("pipeline: halo flag buffer holds %zu, %d needed", flagsCap, last.num_nodes);
-                return CS_ERR_CAPACITY;
-            }
-            CSG_CUDA_TRY(cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, s));
-        }
-        uint32_t herr[4] = {0, 0, 0, 0};
-        CSG_CUDA_TRY(cudaMemcpyAsync(herr, errWords.p, sizeof(herr), cudaMemcpyDeviceToHost, s));
-        CSG_CUDA_TRY(cudaStreamSynchronize(s));
         if (herr[0] | herr[1])
         {
             setLastError("pipeline: a bounded device wait timed out (sort look-back)");
@@ -737,6 +753,65 @@ struct Pipeline final : PipelineBase
             return CS_ERR_DEVICE;
         }
         return CS_OK;
+    }
+
+    // Enqueue the copy of the last run's results to host memory on the copy-back stream, after the run's work.
+    int copyBackAsync(cudaStream_t s, uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap) override
+    {
+        if (flagsHost && flagsCap < size_t(last.num_nodes))
+        {
+            setLastError("pipeline: halo flag buffer holds %zu, %d needed", flagsCap, last.num_nodes);
+            return CS_ERR_CAPACITY;
+        }
+        if (!d2hStream)
+        {
+            CSG_CUDA_TRY(cudaStreamCreateWithFlags(&d2hStream, cudaStreamNonBlocking));
+            for (cudaEvent_t* e : {&outReady, &errCopied, &outDone})
+                CSG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+            CSG_CUDA_TRY(cudaHostAlloc(&herrHost, 4 * sizeof(uint32_t), cudaHostAllocDefault));
+        }
+        if (outPending)
+        {
+            // the previous copy-back's error words (copied long ago) before they are overwritten
+            CSG_CUDA_TRY(cudaEventSynchronize(errCopied));
+            int rc = deviceErrors(herrHost);
+            if (rc && stickyRc == CS_OK)
+            {
+                stickyRc = rc;
+                std::snprintf(stickyMsg, sizeof(stickyMsg), "%s", cs_last_error());
+            }
+        }
+        CSG_CUDA_TRY(cudaEventRecord(outReady, s));
+        CSG_CUDA_TRY(cudaStreamWaitEvent(d2hStream, outReady, 0));
+        CSG_CUDA_TRY(cudaMemcpyAsync(herrHost, errWords.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d2hStream));
+        CSG_CUDA_TRY(cudaEventRecord(errCopied, d2hStream));
+        if (ncHost)
+            CSG_CUDA_TRY(cudaMemcpyAsync(ncHost, nc.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, d2hStream));
+        if (flagsHost)
+            CSG_CUDA_TRY(
+                cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, d2hStream));
+        CSG_CUDA_TRY(cudaEventRecord(outDone, d2hStream));
+        outPending = true;
+        return CS_OK;
+    }
+
+    // Wait for the last copy-back; report the first device error of the runs since the previous wait.
+    int wait() override
+    {
+        int rc = CS_OK;
+        if (outPending)
+        {
+            CSG_CUDA_TRY(cudaEventSynchronize(outDone));
+            outPending = false;
+            rc         = deviceErrors(herrHost);
+        }
+        if (stickyRc != CS_OK)
+        {
+            rc = stickyRc;
+            setLastError("%s", stickyMsg);
+            stickyRc = CS_OK;
+        }
+        return rc;
     }
 
     int outputs(cs_pipeline_outputs* o) override
@@ -869,7 +944,33 @@ extern "C" int cs_pipeline_run_host(cs_pipeline p, cs_stream_t stream, const voi
     }
     int rc = p->impl->run(cudaStream_t(stream), x, y, z, h, n, *box, f0, f1, res, true);
     if (rc) return rc;
-    return p->impl->copyBack(cudaStream_t(stream), ncHost, flagsHost, flagsCap);
+    if ((rc = p->impl->copyBackAsync(cudaStream_t(stream), ncHost, flagsHost, flagsCap))) return rc;
+    return p->impl->wait();
+}
+
+extern "C" int cs_pipeline_run_host_async(cs_pipeline p, cs_stream_t stream, const void* x, const void* y,
+                                          const void* z, const void* h, size_t n, const cs_box* box, uint64_t f0,
+                                          uint64_t f1, uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap,
+                                          cs_pipeline_result* res)
+{
+    if (!p || !box || !x || !y || !z || !h)
+    {
+        setLastError("pipeline run: null argument");
+        return CS_ERR_INVALID;
+    }
+    int rc = p->impl->run(cudaStream_t(stream), x, y, z, h, n, *box, f0, f1, res, true);
+    if (rc) return rc;
+    return p->impl->copyBackAsync(cudaStream_t(stream), ncHost, flagsHost, flagsCap);
+}
+
+extern "C" int cs_pipeline_wait(cs_pipeline p)
+{
+    if (!p)
+    {
+        setLastError("pipeline wait: null argument");
+        return CS_ERR_INVALID;
+    }
+    return p->impl->wait();
 }
 
 extern "C" int cs_pipeline_set_tuning(cs_pipeline p, const cs_tuning* t)

@@ -388,6 +388,20 @@ class Pipeline:
                                         _p(flags_out), C.c_size_t(fcap), C.byref(self.result)))
         return self.result
 
+    def run_host_async(self, x, y, z, h, box, focus=(0, 0), nc_out=None, flags_out=None):
+        """as run_host, returning once enqueued; the next call's input copies overlap this run. Keep x..h unchanged
+        and nc_out / flags_out unread until wait()."""
+        fcap = flags_out.numel() if flags_out is not None else 0
+        self._n = x.numel()
+        _check(lib.cs_pipeline_run_host_async(self.handle, _stream(), _p(x), _p(y), _p(z), _p(h),
+                                              C.c_size_t(x.numel()), C.byref(box), C.c_uint64(focus[0]),
+                                              C.c_uint64(focus[1]), _p(nc_out), _p(flags_out), C.c_size_t(fcap),
+                                              C.byref(self.result)))
+        return self.result
+
+    def wait(self):
+        _check(lib.cs_pipeline_wait(self.handle))
+
     def step(self, x, y, z, h, box, use_graph=True):
         """one incremental time step (the first of a sequence builds from the root); device tensors"""
         self._n = x.numel()

@@ -344,6 +344,18 @@ int cs_pipeline_run_host(cs_pipeline p, cs_stream_t stream, const void* x, const
                          const void* h, size_t n, const cs_box* box, uint64_t focus_start, uint64_t focus_end,
                          uint32_t* neighbor_counts_host, uint8_t* halo_flags_host, size_t halo_flags_capacity,
                          cs_pipeline_result* result);
+/* Pipelined form of cs_pipeline_run_host: returns once the run and the copy of its results are enqueued. Input copies go
+ * to one of two device input sets in turn and wait only for the last reader of that set, so the next call's input
+ * copies overlap this run's computation; results travel back on a stream of their own. The host arrays of a call must
+ * stay unchanged, and its outputs unread, until cs_pipeline_wait returns; the device outputs of cs_pipeline_get_outputs
+ * are those of the last call. */
+int cs_pipeline_run_host_async(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
+                               const void* h, size_t n, const cs_box* box, uint64_t focus_start, uint64_t focus_end,
+                               uint32_t* neighbor_counts_host, uint8_t* halo_flags_host, size_t halo_flags_capacity,
+                               cs_pipeline_result* result);
+/* waits for the results of the last cs_pipeline_run_host_async; returns the first device error (sort look-back
+ * timeout, traversal stack overflow) of the runs since the previous wait */
+int cs_pipeline_wait(cs_pipeline p);
 int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out);
 /* bytes of device memory the pipeline holds */
 size_t cs_pipeline_device_bytes(cs_pipeline p);

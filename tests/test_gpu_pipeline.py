@@ -81,6 +81,40 @@ def test_pipeline_host_call_matches_device_call(cs, O):
     assert torch.equal(flags_host, flags_dev.cpu())
 
 
+def test_pipeline_host_calls_pipelined(cs, O):
+    """cs_pipeline_run_host_async: successive calls on different inputs (the two device input sets in turn, each
+    call's copies overlapping the previous call's computation), one wait at the end; every call's counts and flags
+    equal those of a device-input run on the same inputs, and so does a synchronous call after them"""
+    n = 1 << 15
+    box_lo, box_hi = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0)
+    box = cs.make_box(box_lo, box_hi)
+    focus = (0, 1 << 61)
+    inputs = []
+    for seed in (11, 12, 13):
+        x, y, z = (O.philox_uniform(seed, a, n, -1.0, 1.0) for a in range(3))
+        inputs.append((x, y, z, np.full(n, 0.03 + 0.01 * (seed - 11))))
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, 64, 100, 1.0, 1.0, True, True)
+    ref = []
+    for x, y, z, h in inputs:
+        pipe.run(*to_dev(x, y, z, h), box, focus)
+        o = pipe.outputs()
+        ref.append((o["neighbor_counts"].cpu().clone(), o["halo_flags"].cpu().clone()))
+    hosts = [tuple(torch.from_numpy(a).pin_memory() for a in t) for t in inputs]
+    order = [0, 1, 2, 0, 1]
+    fcap = max(r[1].numel() for r in ref)
+    outs = [(torch.empty(n, dtype=torch.int32).pin_memory(), torch.empty(fcap, dtype=torch.uint8).pin_memory())
+            for k in order]
+    for k, (nc_h, fl_h) in zip(order, outs):
+        pipe.run_host_async(*hosts[k], box, focus, nc_h, fl_h)
+    pipe.wait()
+    for k, (nc_h, fl_h) in zip(order, outs):
+        assert torch.equal(nc_h, ref[k][0]), k
+        assert torch.equal(fl_h[:ref[k][1].numel()], ref[k][1]), k
+    nc_h, fl_h = outs[0]
+    pipe.run_host(*hosts[2], box, focus, nc_h, fl_h)
+    assert torch.equal(nc_h, ref[2][0])
+
+
 def test_pipeline_repeated_runs_reuse_buffers(cs, O):
     """a second run on different inputs (smaller, then larger) gives the same results as fresh objects"""
     pipe = cs.Pipeline(64, 64, cs.HILBERT, 32, 64, 1.0, 1.0, False, True)
