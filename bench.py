@@ -48,11 +48,13 @@ def parse():
     p.add_argument("--sets", type=int, default=4096, help="sets of the batched workload")
     p.add_argument("--requests", type=int, default=600, help="requests of the served workload")
     p.add_argument("--rate", type=float, default=2000.0, help="Poisson arrival rate (requests/s), served workload")
-    p.add_argument("--workload", default="plummer", choices=["plummer", "incremental", "batched", "served"],
+    p.add_argument("--workload", default="plummer",
+                   choices=["plummer", "incremental", "batched", "served", "sort"],
                    help="plummer: the 16M keys->neighbours pass (default); incremental: 64M FP32 time steps with one "
                         "updateOctree step each, replayed from CUDA graphs; batched: 4096 uneven FP32 sets in "
                         "one batched run per chunk against a per-set loop of the single-set pipeline; served: a "
-                        "Poisson stream of build and update requests through the request server")
+                        "Poisson stream of build and update requests through the request server; sort: the stable "
+                        "key sort of the 16M Plummer workload's Hilbert keys alone, with its HBM fraction")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=1 << 20, help="particles of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -400,6 +402,59 @@ def run_batched(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_sort(args, world, rank, local):
+    """The stable (key, index) sort of the 16M Plummer workload's 64-bit Hilbert keys (63 significant bits: a
+    histogram pass and 8 onesweep passes of 8 bits), inputs resident; each timed sort starts from the unsorted keys
+    (restored by a copy outside the timed events). Algorithmic bytes per sort: the histogram pass reads the keys (8 B
+    per key) and every onesweep pass reads and writes key and index (24 B per key; the first pass reads no index)."""
+    import torch
+
+    import cstone_gb300 as cs
+    from cstone_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.n or 16 * 1024 * 1024
+    x, y, z = W.plummer(n, args.seed + rank)
+    lo, hi = W.tight_box(x, y, z)
+    box = cs.make_box(lo, hi)
+    tx, ty, tz = (torch.from_numpy(a).to(dev) for a in (x, y, z))
+    k0 = cs.sfc_keys(tx, ty, tz, box, cs.HILBERT, 64)
+    keys = torch.empty_like(k0)
+    ws = torch.empty(cs.lib.cs_sort_pairs_workspace_bytes(n, 64), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    acc = 0.0
+    with ClockSampler(local) as clocks:
+        for it in range(args.warmup + args.steps):
+            keys.copy_(k0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            kk, _ = cs.sort_pairs(keys, end_bit=63, workspace=ws)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if it >= args.warmup:
+                acc += e0.elapsed_time(e1)
+    ms = max_over_ranks(acc / args.steps, world)
+    ok = bool((kk[1:] >= kk[:-1]).all())
+    passes = 8
+    algo = n * (8 + 20 + (passes - 1) * 24)
+    peak, peak_kind = measured_hbm_peak()
+    achieved = algo / (ms * 1e-3) / 1e9
+    if rank == 0:
+        line = {"metric": "Mkeys/s stable sort (16M Hilbert64 keys of the Plummer workload)",
+                "value": round(world * n / (ms * 1e-3) / 1e6, 3), "unit": "Mkeys/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+                "config": {"workload": "sort-hilbert64-keys", "n_keys": n, "bits": 63, "passes": passes,
+                           "values": "indices (first pass: generated)", "parallelism": f"replicas x{world}"},
+                "sorted": ok,
+                "roofline": {"kernel": "histogram + onesweep passes", "bound": "hbm", "achieved": round(achieved, 1),
+                             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                             "algorithmic_bytes": algo},
+                "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+
+
 def run_served(args, world, rank, local):
     """A Poisson stream of requests (rate 2000/s) through the request server: sizes log-uniform in [2^12, 2^22], FP64
     uniform or Plummer (50/50), Hilbert64, bucket 64, per-request constant h for about 100 neighbours, 30 % of the
@@ -498,6 +553,9 @@ def main():
         return
     if args.workload == "served":
         run_served(args, world, rank, local)
+        return
+    if args.workload == "sort":
+        run_sort(args, world, rank, local)
         return
 
     import numpy as np
