@@ -36,6 +36,33 @@ def test_keys(cs, O, dtype, kind, bits, boxspec):
 
 
 @pytest.mark.parametrize("bits", [32, 64])
+@pytest.mark.parametrize("lo,width", [(1000.25, 0.5), (-3.5, 7.0), (123456.789, 1e-3), (-1e-4, 3e-4), (7.0, 1.0),
+                                      (0.1, 2.0 / 3.0)])
+def test_keys_fp64_offsets_and_cell_boundaries(cs, O, bits, lo, width):
+    """FP64 quantisation int(floor(x * m) - xmin * m) with boxes whose xmin * m has integer, near-integer and
+    arbitrary fractions and large or negative offsets; points on the cell boundaries (x = (floor(xmin m) + j) / m),
+    just beside them, and outside the box, against the oracle"""
+    rng = np.random.default_rng(int(abs(lo) * 1000) % 1000 + bits)
+    L = 10 if bits == 32 else 21
+    m = float(1 << L) * (1.0 / width)
+    o = lo * m
+    j = rng.integers(-3, (1 << L) + 4, 30000)
+    on = (np.floor(o) + j) / m
+    pts = np.concatenate([on, np.nextafter(on, np.inf), np.nextafter(on, -np.inf),
+                          lo + width * rng.random(30000), lo + width * (3 * rng.random(3000) - 1)])
+    x = pts
+    y = rng.permutation(pts)
+    z = rng.permutation(pts)
+    box = ((lo, lo, lo), (lo + width, lo + width, lo + width))
+    for kind in (0, 1):
+        ref = O.sfc_keys(x, y, z, O.make_box(*box), kind, bits)
+        tx, ty, tz = to_dev(x, y, z)
+        k = cs.sfc_keys(tx, ty, tz, cs.make_box(*box), kind, bits)
+        torch.cuda.synchronize()
+        assert np.array_equal(keys_u(k), ref), kind
+
+
+@pytest.mark.parametrize("bits", [32, 64])
 def test_keys_respect_remove_key(cs, O, bits):
     n = 5000
     x, y, z = uniform(O, 3, n, -1.0, 1.0)
