@@ -217,6 +217,66 @@ __host__ __device__ __forceinline__ K iHilbert(unsigned px, unsigned py, unsigne
     return key;
 }
 
+// The same curve by a state table. Every level of iHilbert complements some axes of the remaining bits and permutes
+// the axes, so its running transform is a state: for each transformed axis, the original axis it reads (one of six
+// permutations) and whether it is complemented (3 bits), 48 states of which 24 are reached from the identity (state
+// 0). Entry [state * 8 + octant of the original bits at a level] = digit | next state << 3, generated from the level
+// rule above.
+struct HilbertTable
+{
+    uint16_t e[384];
+};
+
+constexpr HilbertTable makeHilbertTable()
+{
+    HilbertTable t{};
+    constexpr int perms[6][3]  = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    constexpr unsigned m2h[8] = {0, 1, 3, 2, 7, 6, 4, 5};
+    for (int st = 0; st < 48; ++st)
+    {
+        const int s[3]      = {perms[st / 8][0], perms[st / 8][1], perms[st / 8][2]};
+        const unsigned f[3] = {(unsigned(st) >> 2) & 1u, (unsigned(st) >> 1) & 1u, unsigned(st) & 1u};
+        for (unsigned o = 0; o < 8; ++o)
+        {
+            const unsigned ob[3] = {(o >> 2) & 1u, (o >> 1) & 1u, o & 1u};
+            const unsigned xi = ob[s[0]] ^ f[0], yi = ob[s[1]] ^ f[1], zi = ob[s[2]] ^ f[2];
+            const unsigned nyi = yi ^ 1u, nzi = zi ^ 1u;
+            const unsigned g[3] = {f[0] ^ (xi & (nyi | zi)), f[1] ^ ((xi & (yi | zi)) | (yi & nzi)),
+                                   f[2] ^ ((xi & nyi & nzi) | (yi & nzi))};
+            // zi: (x, y, z) <- (y, z, x); !zi && !yi: swap x and z
+            const int from[3] = {zi ? 1 : (yi ? 0 : 2), zi ? 2 : 1, zi ? 0 : (yi ? 2 : 0)};
+            const int ns[3]   = {s[from[0]], s[from[1]], s[from[2]]};
+            int pi            = 0;
+            for (int q = 0; q < 6; ++q)
+                if (perms[q][0] == ns[0] && perms[q][1] == ns[1] && perms[q][2] == ns[2]) pi = q;
+            const unsigned next = unsigned(pi) * 8u + (g[from[0]] << 2 | g[from[1]] << 1 | g[from[2]]);
+            t.e[st * 8 + int(o)] = uint16_t(m2h[xi << 2 | yi << 1 | zi] | (next << 3));
+        }
+    }
+    return t;
+}
+
+// iHilbert through the state table T (in shared memory): the octants of all levels from one Morton interleave, then
+// one lookup per level
+template<class K>
+__host__ __device__ __forceinline__ K iHilbertByTable(unsigned px, unsigned py, unsigned pz, const uint16_t* T)
+{
+    constexpr int L = KeyTraits<K>::maxLevel;
+    uint64_t m;
+    if constexpr (L == 21) m = (spreadBits21(px) << 2) | (spreadBits21(py) << 1) | spreadBits21(pz);
+    else m = (spreadBits10(px) << 2) | (spreadBits10(py) << 1) | spreadBits10(pz);
+    K key       = 0;
+    unsigned st = 0;
+#pragma unroll
+    for (int level = L - 1; level >= 0; --level)
+    {
+        const unsigned e = T[st * 8u + (unsigned(m >> (3 * level)) & 7u)];
+        key              = (key << 3) | K(e & 7u);
+        st               = e >> 3;
+    }
+    return key;
+}
+
 template<class K>
 __host__ __device__ __forceinline__ void decodeHilbert(K key, unsigned& ox, unsigned& oy, unsigned& oz)
 {
@@ -334,8 +394,9 @@ inline KeyParams<T, K> makeKeyParams(const BoxParams<T>& b)
     return p;
 }
 
+// htab: the Hilbert state table in shared memory (iHilbertByTable), or null for the per-level encoder; same keys
 template<class T, class K>
-__device__ __forceinline__ K sfc3D(T x, T y, T z, const KeyParams<T, K>& p, int kind)
+__device__ __forceinline__ K sfc3D(T x, T y, T z, const KeyParams<T, K>& p, int kind, const uint16_t* htab = nullptr)
 {
     constexpr int mcoord = (1 << KeyTraits<K>::maxLevel) - 1;
     int ix = RN<T>::toIntRz(RN<T>::sub(RN<T>::floor_(RN<T>::mul(x, p.m[0])), p.o[0]));
@@ -344,6 +405,7 @@ __device__ __forceinline__ K sfc3D(T x, T y, T z, const KeyParams<T, K>& p, int 
     ix     = min(ix, mcoord);
     iy     = min(iy, mcoord);
     iz     = min(iz, mcoord);
+    if (kind == CS_HILBERT && htab) return iHilbertByTable<K>(unsigned(ix), unsigned(iy), unsigned(iz), htab);
     return iSfc<K>(unsigned(ix), unsigned(iy), unsigned(iz), kind);
 }
 

@@ -1,7 +1,8 @@
 // SFC key encoding and permutation gathers.
 //
 // Keys: one pass over x, y, z (SoA), 4 particles per thread with 16-byte vector loads where the arrays are aligned,
-// sfc3D quantisation with unfused arithmetic (sfc/sfc.hpp:142-179), Hilbert or Morton interleave, 16-byte stores.
+// sfc3D quantisation with unfused arithmetic (sfc/sfc.hpp:142-179), Hilbert keys through the state table in shared
+// memory (one lookup per level) or Morton interleave, 16-byte stores.
 // HBM-bound: 3*sizeof(T) + sizeof(K) bytes per particle (+ sizeof(K) when removeKey entries are respected).
 #include "cs_common.cuh"
 #include "sfc_keys.cuh"
@@ -11,11 +12,29 @@
 namespace csg
 {
 
+// the Hilbert state table (iHilbertByTable), staged into shared memory by the key kernels of the Hilbert curve
+__device__ const HilbertTable kHilbertTable = makeHilbertTable();
+
+template<int Kind>
+__device__ __forceinline__ const uint16_t* stageHilbertTable(uint16_t* sH)
+{
+    if constexpr (Kind == CS_HILBERT)
+    {
+        for (int i = threadIdx.x; i < 384; i += blockDim.x)
+            sH[i] = kHilbertTable.e[i];
+        __syncthreads();
+        return sH;
+    }
+    else { return nullptr; }
+}
+
 template<class T, class K, int Kind, bool RespectRemove>
 __global__ void __launch_bounds__(256) sfcKeysKernel(const T* __restrict__ x, const T* __restrict__ y,
                                                      const T* __restrict__ z, K* __restrict__ keys, size_t n,
                                                      KeyParams<T, K> p)
 {
+    __shared__ uint16_t sH[384];
+    const uint16_t* ht = stageHilbertTable<Kind>(sH);
     constexpr int V = 4;
     size_t stride   = size_t(gridDim.x) * blockDim.x;
     for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) * V; base < n; base += stride * V)
@@ -34,7 +53,7 @@ __global__ void __launch_bounds__(256) sfcKeysKernel(const T* __restrict__ x, co
 #pragma unroll
             for (int v = 0; v < V; ++v)
             {
-                K k = sfc3D<T, K>(xs[v], ys[v], zs[v], p, Kind);
+                K k = sfc3D<T, K>(xs[v], ys[v], zs[v], p, Kind, ht);
                 if constexpr (RespectRemove)
                 {
                     K old = keys[base + v];
@@ -50,7 +69,7 @@ __global__ void __launch_bounds__(256) sfcKeysKernel(const T* __restrict__ x, co
         {
             for (size_t i = base; i < n; ++i)
             {
-                K k = sfc3D<T, K>(x[i], y[i], z[i], p, Kind);
+                K k = sfc3D<T, K>(x[i], y[i], z[i], p, Kind, ht);
                 if constexpr (RespectRemove)
                 {
                     if (keys[i] == removeKey<K>()) continue;
@@ -105,6 +124,8 @@ __global__ void __launch_bounds__(256) sfcKeysPackKernel(const T* __restrict__ x
                                                          K* __restrict__ keys, PackedT<T>* __restrict__ packed,
                                                          size_t n, KeyParams<T, K> p)
 {
+    __shared__ uint16_t sH[384];
+    const uint16_t* ht = stageHilbertTable<Kind>(sH);
     constexpr int V = 4;
     size_t stride   = size_t(gridDim.x) * blockDim.x;
     for (size_t base = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) * V; base < n; base += stride * V)
@@ -127,7 +148,7 @@ __global__ void __launch_bounds__(256) sfcKeysPackKernel(const T* __restrict__ x
         {
             if (v < m)
             {
-                keys[base + v]   = sfc3D<T, K>(xs[v], ys[v], zs[v], p, Kind);
+                keys[base + v]   = sfc3D<T, K>(xs[v], ys[v], zs[v], p, Kind, ht);
                 PackedT<T> r;
                 r.x              = xs[v];
                 r.y              = ys[v];
@@ -173,6 +194,8 @@ __global__ void __launch_bounds__(256)
                        const KeyParams<T, uint32_t>* __restrict__ kps, uint64_t* __restrict__ keys,
                        PackedT<T>* __restrict__ packed)
 {
+    __shared__ uint16_t sH[384];
+    const uint16_t* ht = stageHilbertTable<Kind>(sH);
     size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
     {
@@ -185,7 +208,7 @@ __global__ void __launch_bounds__(256)
             else hi = mid;
         }
         T px = __ldcs(x + i), py = __ldcs(y + i), pz = __ldcs(z + i), ph = __ldcs(h + i);
-        uint32_t k = sfc3D<T, uint32_t>(px, py, pz, kps[lo], Kind);
+        uint32_t k = sfc3D<T, uint32_t>(px, py, pz, kps[lo], Kind, ht);
         keys[i]    = (uint64_t(lo) << 30) | uint64_t(k);
         PackedT<T> r;
         r.x       = px;
