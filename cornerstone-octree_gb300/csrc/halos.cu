@@ -52,17 +52,35 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
         for (int k = 0; k < 3; ++k)
             mn[k] = mx[k] = ordKey(init[k]);
         uint32_t first = layout[leaf], last = layout[leaf + 1];
-        for (uint32_t i = first + sub; i < last; i += TPL)
+        // four particles per lane and round, loaded before any is used (leaves hold about 20 particles)
+        constexpr int U = 4;
+        for (uint32_t i0 = first + sub; i0 < last; i0 += U * TPL)
         {
-            T r    = RN<T>::mul(h[i], scale);
-            T p[3] = {x[i], y[i], z[i]};
+            T ph[U], px[U], py[U], pz[U];
 #pragma unroll
-            for (int k = 0; k < 3; ++k)
+            for (int u = 0; u < U; ++u)
             {
-                I lo  = ordKey(RN<T>::sub(p[k], r));
-                I hi  = ordKey(RN<T>::add(p[k], r));
-                mn[k] = lo < mn[k] ? lo : mn[k];
-                mx[k] = mx[k] < hi ? hi : mx[k];
+                const uint32_t i = i0 + u * TPL;
+                const bool ok    = i < last;
+                ph[u]            = ok ? h[i] : T(0);
+                px[u]            = ok ? x[i] : T(0);
+                py[u]            = ok ? y[i] : T(0);
+                pz[u]            = ok ? z[i] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+            {
+                if (i0 + u * TPL >= last) continue;
+                T r    = RN<T>::mul(ph[u], scale);
+                T p[3] = {px[u], py[u], pz[u]};
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                {
+                    I lo  = ordKey(RN<T>::sub(p[k], r));
+                    I hi  = ordKey(RN<T>::add(p[k], r));
+                    mn[k] = lo < mn[k] ? lo : mn[k];
+                    mx[k] = mx[k] < hi ? hi : mx[k];
+                }
             }
         }
     }
