@@ -44,6 +44,16 @@ def test_pipeline_uniform_cube(cs, O):
     assert res.num_leaves > 0
 
 
+def test_pipeline_uniform_cube_full_size(cs, O):
+    """the CPU-runnable plain build at its full size: N = 2^20 FP64 U[-1,1]^3, h = 0.028, Hilbert64, stable sort,
+    bucket 64 from the root to convergence, link, neighbours with ngmax 150; everything bit-exact against the oracle"""
+    n = 1 << 20
+    x, y, z = (O.philox_uniform(20, s, n, -1.0, 1.0) for s in range(3))
+    h = np.full(n, 0.028)
+    res = _check_against_oracle(cs, O, x, y, z, h, -1.0, 1.0, 0, 64, 150, (0, 0))
+    assert res.num_leaves > 0
+
+
 def test_pipeline_plummer(cs, O):
     """the 16M Plummer workload at reduced size: Plummer, tight box, adaptive h (~100 neighbours), halos in the first
     quarter of the key space, ngmax 200"""
