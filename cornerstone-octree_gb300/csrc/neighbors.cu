@@ -7,12 +7,16 @@
 // stored neighbours are the first ngmax in ascending j among those on leaves whose whole root path passed the test.
 //
 // Main kernel (findNeighborsGroupKernel): one warp serves 32 consecutive targets and walks the tree ONCE for all of
-// them, depth first with an explicit stack of (node, lane mask) in shared memory, lowest child first. A child is
-// pushed when it can hold a neighbour of some lane: normally tested against the bounding box and bounding sphere of
-// the warp's 32 search spheres by lanes 0-7 (one child each); a warp whose targets are spread far apart, or that has
-// already expanded many nodes, tests each child per lane instead and carries the alive lanes on the stack. At a leaf,
-// each lane whose conservative test says the leaf may hold a neighbour stages the leaf's candidates 32 at a time in
-// shared memory and tests them in order. Visiting superset leaves is harmless as long as the final decision equals the
+// them, depth first with an explicit stack of (child offset or leaf code, lane mask) in shared memory, lowest child
+// first. A child is pushed when it can hold a neighbour of some lane: lane l tests child l % 8 against the bounding
+// box and bounding sphere of its sub-group of 8 targets (l / 8), and a child carries the lanes of the sub-groups that
+// may reach it; a warp whose targets are spread far apart, or that has already expanded many nodes, tests each child
+// per lane instead. At a leaf, each lane decides with a conservative box test whether it needs the leaf; the leaf's
+// candidates come 32 at a time, and a batch is tested either per lane (each needing lane against all staged
+// candidates, two per packed FP32 instruction, comparison signs appended to bit masks) or, when few lanes need it,
+// per target (lanes hold the candidates, the warp loops over the needing targets with two ballots each); both give
+// the same masks. The targets per warp (32, 16, 8) and the switch between the two loops are runtime tuning
+// (NbArgs::groupSize, byTargetCost). Visiting superset leaves is harmless as long as the final decision equals the
 // reference's, which depends on the whole root path (next paragraph).
 //
 // Path safety. A candidate at distance^2 d2 < r2 is counted by the reference only if each ancestor of its leaf passed

@@ -3,6 +3,9 @@
 // them, so repeated runs (time steps, requests) allocate nothing once sized. The only host synchronisation per run
 // is the one that returns the leaf count of the build (the reference's updateOctreeGpu synchronises three times per
 // rebalance iteration; here the whole rebalance loop is one cooperative launch).
+// Host inputs are copied in chunks on a copy stream into one of two device input sets in turn, so a run's copies
+// overlap the previous run; results go back on a stream of their own (run_host_async / wait). The neighbour
+// traversal's tuning is set per object and can be chosen by timing candidates on the last run's inputs (autotune).
 #include "cs_common.cuh"
 #include "halos.cuh"
 #include "pipeline.cuh"
