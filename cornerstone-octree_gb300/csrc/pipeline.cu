@@ -340,6 +340,7 @@ struct Pipeline final : PipelineBase
     {
         int rc;
         if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, outDone, 0)); // a copy-back still reads the outputs
+        lastNIn = 0; // autotune reruns plain runs only (a step's inputs need not outlive it)
         if (incCur < 0 || nIn != incN)
         {
             // the first step of a sequence builds from the root and becomes the current tree; the step buffers are

@@ -391,8 +391,8 @@ typedef struct
 
 int cs_pipeline_set_tuning(cs_pipeline p, const cs_tuning* tuning);
 int cs_pipeline_get_tuning(cs_pipeline p, cs_tuning* tuning);
-/* Autotuner: reruns the inputs of the last cs_pipeline_run / cs_pipeline_run_host (device input arrays must still be
- * valid) reps times for each candidate tuning ({32, 7}, {32, 0}, {32, 5}, {32, 10}, {16, 7}, {8, 7}), scores each by
+/* Autotuner: reruns the inputs of the last cs_pipeline_run / cs_pipeline_run_host, when no cs_pipeline_step came
+ * after it (device input arrays must still be valid), reps times for each candidate tuning ({32, 7}, {32, 0}, {32, 5}, {32, 10}, {16, 7}, {8, 7}), scores each by
  * the mean device time of the neighbour stage, and keeps the fastest as the pipeline's tuning. Writes the best, and
  * up to capacity candidates with their mean ms (tried / ms may be NULL); *count = candidates run. The outputs
  * afterwards are those of the last candidate's run (identical for every tuning). */
