@@ -228,7 +228,7 @@ struct Batch final : BatchBase
             br = BuildResult{};
             rc = octreeBuild<uint64_t>(s, sortedKeys, n, 64, 0xffffffffu, nullptr, nullptr, 0, leaves.as<uint64_t>(),
                                        counts.as<uint32_t>(), layout.as<uint32_t>(), capacity, buildWs.p,
-                                       buildWs.bytes, &br, true, FocusQuery<uint64_t>{}, nullptr, &bt);
+                                       buildWs.bytes, &br, true, FocusQuery<uint64_t>{}, nullptr, &bt, err);
             if (rc == CS_ERR_CAPACITY)
             {
                 capacity = std::max(2 * capacity, br.needed + br.needed / 4);

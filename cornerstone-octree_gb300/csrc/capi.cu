@@ -1,6 +1,7 @@
 // Error reporting, device queries and version of the C ABI.
 #include "cs_common.cuh"
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 
@@ -19,9 +20,9 @@ void setLastError(const char* fmt, ...)
 
 int smCount()
 {
-    static int cachedDevice = -1;
-    static int cachedCount  = 0;
-    int dev                 = 0;
+    static thread_local int cachedDevice = -1;
+    static thread_local int cachedCount  = 0;
+    int dev                              = 0;
     cudaGetDevice(&dev);
     if (dev != cachedDevice)
     {
@@ -33,8 +34,35 @@ int smCount()
     return cachedCount;
 }
 
+static std::atomic<uint32_t> gSortSpins{WaitLimits{}.sortSpins};
+static std::atomic<uint32_t> gBarrierSpins{WaitLimits{}.barrierSpins};
+static std::atomic<int> gStall{0};
+
+WaitLimits waitLimits()
+{
+    WaitLimits w;
+    w.sortSpins    = gSortSpins.load();
+    w.barrierSpins = gBarrierSpins.load();
+    w.stall        = gStall.load();
+    return w;
+}
+
 } // namespace csg
 
 extern "C" const char* cs_last_error(void) { return csg::tlsError; }
 
 extern "C" int cs_version(void) { return 100; }
+
+extern "C" int cs_set_wait_limits(uint32_t sort_spins, uint32_t barrier_spins, int stall)
+{
+    if (stall < 0 || stall > (CS_WAIT_STALL_SORT | CS_WAIT_STALL_BARRIER))
+    {
+        csg::setLastError("wait limits: unknown stall mode %d", stall);
+        return CS_ERR_INVALID;
+    }
+    const csg::WaitLimits d;
+    csg::gSortSpins.store(sort_spins ? sort_spins : d.sortSpins);
+    csg::gBarrierSpins.store(barrier_spins ? barrier_spins : d.barrierSpins);
+    csg::gStall.store(stall);
+    return CS_OK;
+}

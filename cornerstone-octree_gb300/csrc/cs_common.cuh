@@ -432,6 +432,17 @@ inline unsigned iceil(size_t a, size_t b) { return unsigned((a + b - 1) / b); }
 // number of SMs of the current device (cached per device)
 int smCount();
 
+// Bounds of the device-side waits, read by the host at each launch and passed as kernel arguments. The defaults
+// give up after about a second; cs_set_wait_limits lowers them and can make one wait stall on purpose (a flag that
+// nothing sets), so that tests reach the timeout path on ordinary inputs.
+struct WaitLimits
+{
+    uint32_t sortSpins    = 1u << 22; // look-back rounds of the onesweep passes
+    uint32_t barrierSpins = 1u << 24; // polls of the build's grid barrier
+    int stall             = 0;        // CS_WAIT_STALL_* of include/cstone_gb300.h
+};
+WaitLimits waitLimits();
+
 // bump allocator over a caller workspace; `size` only accumulates when base == nullptr (size query)
 struct Arena
 {

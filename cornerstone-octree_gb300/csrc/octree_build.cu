@@ -16,13 +16,13 @@
 #include "octree_build.cuh"
 
 #include <algorithm>
+#include <atomic>
 
 namespace csg
 {
 
 constexpr int BUILD_THREADS   = 256;
 constexpr int BUILD_MAX_ITERS = 256;
-constexpr unsigned BARRIER_SPIN_LIMIT = 1u << 24;
 
 struct BuildState
 {
@@ -39,12 +39,18 @@ struct BuildState
     int changed[BUILD_MAX_ITERS];
 };
 
-// grid-wide barrier for a cooperative launch; returns false if the wait gave up
-__device__ bool gridBarrier(BuildState* st, unsigned nblocks)
+// grid-wide barrier for a cooperative launch; returns false if the wait gave up. With `stall` set (test mode, first
+// barrier only) block 0 does not arrive and gives up at once, so that every other block's wait runs out.
+__device__ bool gridBarrier(BuildState* st, unsigned nblocks, unsigned spinLimit, bool stall = false)
 {
     __shared__ int sFail;
     __syncthreads();
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0 && stall && blockIdx.x == 0)
+    {
+        atomicOr(&st->err, ERRBIT_BARRIER_TIMEOUT);
+        sFail = 1;
+    }
+    else if (threadIdx.x == 0)
     {
         sFail                  = 0;
         volatile unsigned* gen = &st->barGen;
@@ -62,7 +68,7 @@ __device__ bool gridBarrier(BuildState* st, unsigned nblocks)
             unsigned spins = 0;
             while (*gen == g)
             {
-                if (++spins > BARRIER_SPIN_LIMIT)
+                if (++spins > spinLimit)
                 {
                     atomicOr(&st->err, ERRBIT_BARRIER_TIMEOUT);
                     sFail = 1;
@@ -246,6 +252,9 @@ struct BuildArgs
     uint32_t* layoutOut;
     BuildState* st;
     FocusQuery<K> focus;
+    const uint32_t* upstreamErr; // the key sort's error word (may be null): set means the keys may be unordered
+    unsigned spinLimit;    // polls of a grid barrier before it gives up
+    int stallFirstBarrier; // test mode: block 0 never arrives at the first barrier
 };
 
 template<class K>
@@ -258,6 +267,14 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
     const unsigned tid = threadIdx.x;
     BuildState* st     = a.st;
 
+    // keys from a sort whose look-back gave up may be unordered: every block leaves before touching them (all blocks
+    // read the same word, written before this launch, so none waits at a barrier for the others)
+    if (a.upstreamErr && *a.upstreamErr)
+    {
+        if (b == 0 && tid == 0) atomicOr(&st->err, ERRBIT_UPSTREAM);
+        return;
+    }
+
     int L   = a.updateMode ? (a.LinDev ? *a.LinDev : a.Lin) : (a.initL ? a.initL : 1);
     int cur = 0;
     if (!a.updateMode && !a.initL && b == 0 && tid == 0)
@@ -267,7 +284,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
         a.off[0][0]  = 0;
         a.off[0][1]  = uint32_t(a.n);
     }
-    if (!gridBarrier(st, G)) return;
+    if (!gridBarrier(st, G, a.spinLimit, a.stallFirstBarrier != 0)) return;
 
     int iter = 0;
     bool converged = false;
@@ -338,7 +355,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
             a.blockSums[b] = bsum;
             if (a.updateMode) a.blockCnt[b] = bcnt;
         }
-        if (!gridBarrier(st, G)) return;
+        if (!gridBarrier(st, G, a.spinLimit)) return;
 
         if (!a.updateMode && ldcg(&st->changed[iter]) == 0)
         {
@@ -426,7 +443,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
             a.ops[L] = tot;
             if (a.updateMode) a.gscan[L] = (long long)a.n;
         }
-        if (!gridBarrier(st, G)) return;
+        if (!gridBarrier(st, G, a.spinLimit)) return;
 
         // ---------------- phase D: emit new leaves ----------------
         const int newL = tot;
@@ -473,7 +490,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
                 nof[j] = o;
             }
         }
-        if (!gridBarrier(st, G)) return;
+        if (!gridBarrier(st, G, a.spinLimit)) return;
         L   = newL;
         cur ^= 1;
     }
@@ -488,7 +505,7 @@ __global__ void __launch_bounds__(BUILD_THREADS) octreeBuildKernel(BuildArgs<K> 
             long long g = j < L ? ldcg(a.gscan + size_t(a.capacity) + 1 + j) : (long long)a.n;
             of[j]       = uint32_t(guessedLowerBound<K>(a.keys, a.n, g, ldcg(tr + j)));
         }
-        if (!gridBarrier(st, G)) return;
+        if (!gridBarrier(st, G, a.spinLimit)) return;
         converged = ldcg(&st->changed[0]) == 0;
     }
     else if (!converged)
@@ -552,17 +569,23 @@ struct BuildLayout
     BuildState* st;
 };
 
+// blocks of the cooperative build on the current device: all resident at once (at most 4 per SM), computed once per
+// device ordinal since devices may differ in SM count
 static int buildGridSize()
 {
-    static int cached = -1;
-    if (cached > 0) return cached;
+    constexpr int MAX_DEVICES = 64;
+    static std::atomic<int> cached[MAX_DEVICES];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < MAX_DEVICES && cached[dev].load() > 0) return cached[dev].load();
     int perSm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, octreeBuildKernel<uint64_t>, BUILD_THREADS, 0);
     int perSm32 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm32, octreeBuildKernel<uint32_t>, BUILD_THREADS, 0);
-    perSm  = std::max(1, std::min(std::min(perSm, perSm32), 4));
-    cached = perSm * smCount();
-    return cached;
+    perSm     = std::max(1, std::min(std::min(perSm, perSm32), 4));
+    const int g = perSm * smCount();
+    if (dev >= 0 && dev < MAX_DEVICES) cached[dev].store(g);
+    return g;
 }
 
 template<class K>
@@ -600,7 +623,7 @@ template<class K>
 int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32_t maxCount, const K* treeIn,
                 const uint32_t* countsIn, int Lin, K* treeOut, uint32_t* countsOut, uint32_t* layoutOut, int capacity,
                 void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus, const int* LinDev,
-                const BatchTree<K>* batch)
+                const BatchTree<K>* batch, const uint32_t* upstreamErr)
 {
     bool update = treeIn != nullptr;
     if (batch && (update || batch->initL < 1 || batch->initL > capacity || !batch->initTree || !batch->initOff))
@@ -676,6 +699,10 @@ int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32
     a.layoutOut  = layoutOut;
     a.st         = l.st;
     a.focus      = focus;
+    a.upstreamErr = upstreamErr;
+    const WaitLimits wl = waitLimits();
+    a.spinLimit         = wl.barrierSpins;
+    a.stallFirstBarrier = (wl.stall & CS_WAIT_STALL_BARRIER) ? 1 : 0;
     void* params[] = {&a};
     CSG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)octreeBuildKernel<K>, dim3(G), dim3(BUILD_THREADS), params,
                                              0, s));
@@ -706,6 +733,11 @@ int octreeBuildFinish(cudaStream_t s, void* ws, size_t wsBytes, int capacity, bo
         res->maxDepth   = h.maxDepth;
         res->focusFirst = h.focusFirst;
         res->focusLast  = h.focusLast;
+    }
+    if (h.err & ERRBIT_UPSTREAM)
+    {
+        setLastError("octree: the key sort's look-back timed out; the build did not run");
+        return CS_ERR_TIMEOUT;
     }
     if (h.err & ERRBIT_BARRIER_TIMEOUT)
     {
@@ -756,10 +788,12 @@ template size_t octreeBuildWorkspaceBytes<uint32_t>(int, bool);
 template size_t octreeBuildWorkspaceBytes<uint64_t>(int, bool);
 template int octreeBuild<uint32_t>(cudaStream_t, const uint32_t*, size_t, unsigned, uint32_t, const uint32_t*,
                                    const uint32_t*, int, uint32_t*, uint32_t*, uint32_t*, int, void*, size_t,
-                                   BuildResult*, bool, FocusQuery<uint32_t>, const int*, const BatchTree<uint32_t>*);
+                                   BuildResult*, bool, FocusQuery<uint32_t>, const int*, const BatchTree<uint32_t>*,
+                                   const uint32_t*);
 template int octreeBuild<uint64_t>(cudaStream_t, const uint64_t*, size_t, unsigned, uint32_t, const uint64_t*,
                                    const uint32_t*, int, uint64_t*, uint32_t*, uint32_t*, int, void*, size_t,
-                                   BuildResult*, bool, FocusQuery<uint64_t>, const int*, const BatchTree<uint64_t>*);
+                                   BuildResult*, bool, FocusQuery<uint64_t>, const int*, const BatchTree<uint64_t>*,
+                                   const uint32_t*);
 
 // ---------------------------------------------------------------------------------------------------------------
 // standalone counts and decisions

@@ -10,6 +10,7 @@ namespace csg
 constexpr uint32_t ERRBIT_BARRIER_TIMEOUT = 2u;
 constexpr uint32_t ERRBIT_CAPACITY        = 4u;
 constexpr uint32_t ERRBIT_NO_CONVERGENCE  = 8u;
+constexpr uint32_t ERRBIT_UPSTREAM        = 16u; // the key sort before the build reported a timeout
 
 struct BuildResult
 {
@@ -36,7 +37,9 @@ template<class K>
 size_t octreeBuildWorkspaceBytes(int capacity, bool update);
 
 /*! Build (treeIn == nullptr: computeOctree from the root) or update (one updateOctree step from treeIn/countsIn).
- *  With sync == false the call only enqueues work; the state block (see BuildResult::stateDev) holds the outcome. */
+ *  With sync == false the call only enqueues work; the state block (see BuildResult::stateDev) holds the outcome.
+ *  upstreamErr (device, may be null): the error word of the sort that produced `keys`; if it is set when the build
+ *  starts, the build does nothing and reports CS_ERR_TIMEOUT (keys from a sort that gave up may be unordered). */
 //! many independent sets in one tree: set s owns the key range [s << setShift, (s + 1) << setShift) (an aligned
 //! subtree rooted at level minMergeLevel), uses bucket size setBucket[s], and no node at or above minMergeLevel is
 //! merged; the build starts from initTree (set roots and empty filler nodes, initL leaves) with particle offsets
@@ -57,7 +60,8 @@ template<class K>
 int octreeBuild(cudaStream_t s, const K* keys, size_t n, unsigned bucket, uint32_t maxCount, const K* treeIn,
                 const uint32_t* countsIn, int Lin, K* treeOut, uint32_t* countsOut, uint32_t* layoutOut, int capacity,
                 void* ws, size_t wsBytes, BuildResult* res, bool sync, FocusQuery<K> focus = FocusQuery<K>{},
-                const int* LinDev = nullptr, const BatchTree<K>* batch = nullptr);
+                const int* LinDev = nullptr, const BatchTree<K>* batch = nullptr,
+                const uint32_t* upstreamErr = nullptr);
 
 /*! after an octreeBuild with sync = false (e.g. replayed from a CUDA graph): read its state block from the same
  *  workspace, synchronise, fill res and map the device error bits to a status, as the sync path does */

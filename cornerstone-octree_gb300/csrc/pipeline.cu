@@ -287,7 +287,8 @@ struct Pipeline final : PipelineBase
         BuildResult br;
         rc = octreeBuild<K>(s, sortedKeys, nIn, cfg.bucket_size, cfg.max_count, incLeaves[cur].as<K>(),
                             incCounts[cur].as<uint32_t>(), 0, incLeaves[nxt].as<K>(), incCounts[nxt].as<uint32_t>(),
-                            layout.as<uint32_t>(), cap, buildWs.p, buildWs.bytes, &br, false, FocusQuery<K>{}, Ldev);
+                            layout.as<uint32_t>(), cap, buildWs.p, buildWs.bytes, &br, false, FocusQuery<K>{}, Ldev,
+                            nullptr, err);
         if (rc) return rc;
         if ((rc = commitLeafCount<K>(s, buildWs.p, buildWs.bytes, cap, Ldev))) return rc;
 
@@ -590,7 +591,7 @@ struct Pipeline final : PipelineBase
             br = BuildResult{};
             rc = octreeBuild<K>(s, sortedKeys, n, cfg.bucket_size, cfg.max_count, nullptr, nullptr, 0, leaves.as<K>(),
                                 counts.as<uint32_t>(), layout.as<uint32_t>(), capacity, buildWs.p, buildWs.bytes, &br,
-                                true, FocusQuery<K>{K(f0), K(f1), cfg.do_halos != 0});
+                                true, FocusQuery<K>{K(f0), K(f1), cfg.do_halos != 0}, nullptr, nullptr, err);
             if (rc == CS_ERR_CAPACITY)
             {
                 capacity = std::max(2 * capacity, br.needed + br.needed / 4);

@@ -27,7 +27,6 @@ constexpr uint32_t ST_INC   = 2u << 30;
 constexpr uint32_t ST_FLAGS = 3u << 30;
 constexpr uint32_t ST_COUNT = (1u << 30) - 1;
 
-constexpr uint32_t SPIN_LIMIT = 1u << 22;
 
 struct SortLayout
 {
@@ -144,7 +143,7 @@ __global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restr
                                                              size_t n, int shift, uint32_t mask,
                                                              const uint32_t* __restrict__ passHist,
                                                              uint32_t* status, uint32_t* tileCounter,
-                                                             uint32_t* errWord)
+                                                             uint32_t* errWord, uint32_t spinLimit, int stallTile1)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     K* sKeys        = reinterpret_cast<K*>(smem);
@@ -236,6 +235,8 @@ __global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restr
 #pragma unroll
             for (int u = 0; u < LB; ++u)
                 st[u] = t - u >= 0 ? uint32_t(vstatus[size_t(t - u) * RS_BINS + dg]) : uint32_t(ST_INC);
+            // test mode: tile 1 waits for an entry that is never published, until the spin limit
+            if (stallTile1 && tile == 1) st[0] = 0;
             int used  = 0;
             bool done = false, wait = false;
 #pragma unroll
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restr
             t -= used;
             if (wait)
             {
-                if (++spins > SPIN_LIMIT)
+                if (++spins > spinLimit)
                 {
                     timedOut = true;
                     break;
@@ -372,6 +373,8 @@ int radixSortPairs(cudaStream_t s, K* keys, uint32_t* vals, K* keysAlt, uint32_t
     CSG_CUDA_TRY(cudaFuncSetAttribute(onesweepKernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       int(smemBytes)));
 
+    const WaitLimits wl = waitLimits();
+    const int stall     = (wl.stall & CS_WAIT_STALL_SORT) ? 1 : 0;
     K* kin        = keys;
     uint32_t* vin = vals;
     K* kout       = keysAlt;
@@ -384,10 +387,12 @@ int radixSortPairs(cudaStream_t s, K* keys, uint32_t* vals, K* keysAlt, uint32_t
         uint32_t* st  = L.status + size_t(p) * L.tiles * RS_BINS;
         if (p == 0 && iota)
             onesweepKernel<K, true><<<unsigned(L.tiles), RS_THREADS, smemBytes, s>>>(
-                kin, vin, kout, vout, n, shift, mask, L.hist + p * RS_BINS, st, L.tileCounter + p, err);
+                kin, vin, kout, vout, n, shift, mask, L.hist + p * RS_BINS, st, L.tileCounter + p, err, wl.sortSpins,
+                stall);
         else
             onesweepKernel<K, false><<<unsigned(L.tiles), RS_THREADS, smemBytes, s>>>(
-                kin, vin, kout, vout, n, shift, mask, L.hist + p * RS_BINS, st, L.tileCounter + p, err);
+                kin, vin, kout, vout, n, shift, mask, L.hist + p * RS_BINS, st, L.tileCounter + p, err, wl.sortSpins,
+                stall);
         CSG_CHECK_LAUNCH();
         std::swap(kin, kout);
         std::swap(vin, vout);
@@ -402,6 +407,20 @@ int radixSortPairs(cudaStream_t s, K* keys, uint32_t* vals, K* keysAlt, uint32_t
     return CS_OK;
 }
 
+template<class K>
+int radixSortPreload()
+{
+    cudaFuncAttributes fa;
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, radixHistogramKernel<K>));
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, histScanKernel));
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, iotaKernel));
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, onesweepKernel<K, true>));
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, onesweepKernel<K, false>));
+    return CS_OK;
+}
+
+template int radixSortPreload<uint32_t>();
+template int radixSortPreload<uint64_t>();
 template size_t radixSortWorkspaceBytes<uint32_t>(size_t, int, int);
 template size_t radixSortWorkspaceBytes<uint64_t>(size_t, int, int);
 template int radixSortPairs<uint32_t>(cudaStream_t, uint32_t*, uint32_t*, uint32_t*, uint32_t*, size_t, int, int, bool,

@@ -20,4 +20,9 @@ template<class K>
 int radixSortPairs(cudaStream_t s, K* keys, uint32_t* vals, K* keysAlt, uint32_t* valsAlt, size_t n, int beginBit,
                    int endBit, bool iota, void* ws, size_t wsBytes, uint32_t* errWord, bool* resultInAlt);
 
+/*! Loads the sort's kernels on the current device (cudaFuncGetAttributes), so that with lazy module loading the
+ *  first sort does not load them. */
+template<class K>
+int radixSortPreload();
+
 } // namespace csg

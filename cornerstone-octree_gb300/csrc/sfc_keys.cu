@@ -252,7 +252,8 @@ __global__ void __launch_bounds__(256) gatherPackedKernel(const uint32_t* __rest
     float m       = 0.f;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
     {
-        PackedT<T> r = packed[__ldcs(perm + i)];
+        // an index past the end (a permutation from a sort that gave up) is clamped, so nothing is read out of range
+        PackedT<T> r = packed[min(__ldcs(perm + i), uint32_t(n - 1))];
         __stcs(xs + i, r.x);
         __stcs(ys + i, r.y);
         __stcs(zs + i, r.z);

@@ -12,13 +12,17 @@
 //  - at most CS_SORT_NOALLOC_MAX_N keys per call; larger calls are rejected with CS_ERR_INVALID;
 //  - every call uses the same array, so two calls that overlap on the GPU (different streams, or different host
 //    threads on the same device) race and corrupt each other: serialise them;
-//  - the first call on a device looks up the array's device address (cudaGetSymbolAddress) with that device
-//    current and caches it; make that first call before capturing any stream into a graph;
+//  - CUDA loads modules lazily by default (CUDA_MODULE_LOADING=LAZY): the array and the sort kernels come into
+//    device memory on first use. A call with n = 0 does that set-up (looks the array up with cudaGetSymbolAddress
+//    and loads the kernels) without sorting; make it once per device, with that device current, before reserving
+//    the memory pool. CUDA_MODULE_LOADING=EAGER loads everything when the library is loaded instead;
+//  - each call reads the sort's error word back and synchronises its stream before returning, so it cannot be
+//    recorded into a CUDA graph: a call made while its stream is being captured is refused with CS_ERR_INVALID;
+//  - the array's address is looked up on every call (cheap next to the sort), so a device reset or a new context
+//    needs nothing special;
 //  - the parts of the array that must start at zero are cleared by every call with cudaMemsetAsync.
 #include "cs_common.cuh"
 #include "radix_sort.cuh"
-
-#include <mutex>
 
 namespace csg
 {
@@ -32,33 +36,18 @@ constexpr size_t NOALLOC_SCRATCH_BYTES = NOALLOC_MAX_N * (sizeof(uint64_t) + siz
 
 static __device__ __align__(256) unsigned char g_sortScratch[NOALLOC_SCRATCH_BYTES];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-static void* g_scratchAddr[NOALLOC_MAX_DEVICES] = {};
-static std::mutex g_scratchMutex;
-
-// device address of g_sortScratch on the current device (looked up once per device)
+// device address of g_sortScratch on the current device. In host code the name g_sortScratch is a host-side
+// stand-in; only the address from cudaGetSymbolAddress may be passed to kernels.
 int scratchAddress(void** out)
 {
-    int dev = 0;
-    CSG_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+    void* p          = nullptr;
+    cudaError_t err_ = cudaGetSymbolAddress(&p, g_sortScratch);
+    if (err_ != cudaSuccess || p == nullptr)
     {
-        setLastError("sort (no-alloc): device ordinal %d not supported", dev);
-        return CS_ERR_INVALID;
+        setLastError("sort (no-alloc): cudaGetSymbolAddress failed: %s", cudaGetErrorString(err_));
+        return CS_ERR_CUDA;
     }
-    std::lock_guard<std::mutex> lock(g_scratchMutex);
-    if (!g_scratchAddr[dev])
-    {
-        void* p          = nullptr;
-        cudaError_t err_ = cudaGetSymbolAddress(&p, g_sortScratch);
-        if (err_ != cudaSuccess || p == nullptr)
-        {
-            setLastError("sort (no-alloc): cudaGetSymbolAddress failed: %s", cudaGetErrorString(err_));
-            return CS_ERR_CUDA;
-        }
-        g_scratchAddr[dev] = p;
-    }
-    *out = g_scratchAddr[dev];
+    *out = p;
     return CS_OK;
 }
 
@@ -75,16 +64,28 @@ extern "C" int cs_sort_pairs_noalloc_u64(cs_stream_t stream, uint64_t* keys, uin
         setLastError("sort (no-alloc): n = %zu exceeds the fixed scratch limit of %zu keys", n, NOALLOC_MAX_N);
         return CS_ERR_INVALID;
     }
+    cudaStream_t s = cudaStream_t(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CSG_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone)
+    {
+        setLastError("sort (no-alloc): the stream is being captured; this call synchronises its stream and cannot be "
+                     "part of a CUDA graph");
+        return CS_ERR_INVALID;
+    }
+    // set-up on every call, including n == 0 (the warm-up call): the array's address, which loads this file's
+    // module and so the array itself, and the sort kernels
+    void* base = nullptr;
+    int rc     = scratchAddress(&base);
+    if (rc) return rc;
+    rc = radixSortPreload<uint64_t>();
+    if (rc) return rc;
     if (n == 0) return CS_OK;
     if (!keys || !values)
     {
         setLastError("sort (no-alloc): null pointer");
         return CS_ERR_INVALID;
     }
-    cudaStream_t s = cudaStream_t(stream);
-    void* base     = nullptr;
-    int rc         = scratchAddress(&base);
-    if (rc) return rc;
 
     Arena a{static_cast<char*>(base), 0, NOALLOC_SCRATCH_BYTES};
     uint64_t* keysAlt   = a.take<uint64_t>(n);

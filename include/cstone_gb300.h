@@ -97,6 +97,19 @@ typedef struct
 const char* cs_last_error(void);
 int cs_version(void);
 
+/* ---- bounded device-side waits --------------------------------------------------------------------------------
+ * No counterpart in the reference (its CUB look-back and host-synchronised build loop never give up). The sort's
+ * decoupled look-back and the cooperative build's grid barrier spin on flags that other blocks publish; each wait
+ * gives up after a bounded number of polls, sets an error bit, and the call returns CS_ERR_TIMEOUT without writing
+ * outside its buffers (the results of that call are then unspecified). cs_set_wait_limits sets the bounds for the
+ * whole process (0 = default: 2^22 look-back rounds, 2^24 barrier polls) and, for tests, makes one wait stall on a
+ * flag that nothing sets: CS_WAIT_STALL_SORT (tile 1 of every sort pass waits for its predecessor),
+ * CS_WAIT_STALL_BARRIER (block 0 of every cooperative build never arrives at the first barrier). Kernels read the
+ * values when they are launched; CUDA graphs keep the values they were captured with. */
+#define CS_WAIT_STALL_SORT 1
+#define CS_WAIT_STALL_BARRIER 2
+int cs_set_wait_limits(uint32_t sort_spins, uint32_t barrier_spins, int stall);
+
 /* ---- SFC keys ----------------------------------------------------------------------------------------------
  * replaces computeSfcKeys(execution::Gpu, x, y, z, keys, n, box) (sfc/sfc_gpu.h:24-26, kernel sfc/sfc_gpu.cu:23-44).
  * respect_remove_key = 1 keeps keys that equal removeKey (2^30 / 2^63) untouched, as the reference kernel does;
@@ -137,9 +150,11 @@ int cs_sort_pairs_u64(cs_stream_t stream, uint64_t* keys, uint32_t* values, size
  * cannot afford cudaMalloc/cudaFree's implicit device synchronisation). Every temporary lives in one fixed
  * file-scope device array, held by each device that loads the library until the process exits; the caller passes
  * only keys and values, sorted in place. At most CS_SORT_NOALLOC_MAX_N keys (larger n: CS_ERR_INVALID). All calls
- * share that array: calls that overlap on the GPU race, so serialise them. The first call on a device looks up the
- * array's address with that device current; make it before any stream capture. Synchronises the stream on return,
- * like cs_sort_pairs_u64. */
+ * share that array: calls that overlap on the GPU race, so serialise them. CUDA loads modules lazily by default, so
+ * the array and the sort kernels reach device memory on first use: call once with n = 0 per device, with that device
+ * current, before reserving the pool (or run with CUDA_MODULE_LOADING=EAGER). Every call reads the sort's error word
+ * back and synchronises the stream before it returns, so it cannot be recorded into a CUDA graph; a call on a stream
+ * that is being captured returns CS_ERR_INVALID. */
 #define CS_SORT_NOALLOC_MAX_N 262144
 int cs_sort_pairs_noalloc_u64(cs_stream_t stream, uint64_t* keys, uint32_t* values, size_t n, int begin_bit,
                               int end_bit, int values_are_iota);

@@ -41,6 +41,45 @@ def test_noalloc_sort_matches_allocating_sort_twice(cs, iota):
         assert torch.equal(v2, ref_v), f"values differ on call {call}"
 
 
+def test_noalloc_sort_allocates_no_device_memory(cs):
+    """After warm-up calls (n = 0, which loads the fixed array and the sort kernels, then one full-size sort, which
+    also settles the kernels' per-thread stack reservation), a second full-size call on new inputs leaves the device's
+    free memory unchanged."""
+    assert _noalloc_sort(cs, torch.empty(0, dtype=torch.int64, device="cuda"),
+                         torch.empty(0, dtype=torch.int32, device="cuda"), True) == 0, cs.lib.cs_last_error().decode()
+    rng = np.random.default_rng(7)
+    n = 262144
+    wk = torch.from_numpy(rng.integers(0, 1 << 63, size=n, dtype=np.uint64).view(np.int64)).cuda()
+    wv = torch.empty(n, dtype=torch.int32, device="cuda")
+    assert _noalloc_sort(cs, wk, wv, True) == 0, cs.lib.cs_last_error().decode()
+    keys = rng.integers(0, 1 << 63, size=n, dtype=np.uint64)
+    dk = torch.from_numpy(keys.view(np.int64)).cuda()
+    dv = torch.empty(n, dtype=torch.int32, device="cuda")
+    ref_k = torch.from_numpy(np.sort(keys).view(np.int64)).cuda()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    rc = _noalloc_sort(cs, dk, dv, True)
+    assert rc == 0, cs.lib.cs_last_error().decode()
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, f"device free memory changed by {free_before - free_after} bytes"
+    assert torch.equal(dk, ref_k)
+
+
+def test_noalloc_sort_refuses_a_capturing_stream(cs):
+    n = 1024
+    k = torch.zeros(n, dtype=torch.int64, device="cuda")
+    v = torch.zeros(n, dtype=torch.int32, device="cuda")
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    rc = None
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            rc = _noalloc_sort(cs, k, v, True)
+    assert rc == cs.CS_ERR_INVALID
+    assert "captured" in cs.lib.cs_last_error().decode()
+
+
 def test_noalloc_sort_rejects_sizes_beyond_limit(cs):
     n = 262144 + 1
     k = torch.zeros(n, dtype=torch.int64, device="cuda")
