@@ -44,7 +44,8 @@ def parse():
     p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--n", type=int, default=None, help="particles (default 16M plummer, 64M incremental)")
+    p.add_argument("--n", "--particles", dest="n", type=int, default=None,
+                   help="particles (default 16M plummer, 64M incremental)")
     p.add_argument("--sets", type=int, default=4096, help="sets of the batched workload")
     p.add_argument("--requests", type=int, default=600, help="requests of the served workload")
     p.add_argument("--rate", type=float, default=2000.0, help="Poisson arrival rate (requests/s), served workload")
@@ -164,34 +165,59 @@ def measured_hbm_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(n):
-    """DRAM bytes per neighbour-search launch from the committed ncu summary, scaled to n particles, or None"""
+def profile_figures(n):
+    """per-launch DRAM bytes and warp instructions of the neighbour search, from the committed ncu summary of a
+    smaller capture of the same workload, scaled to n particles by particle count (None where absent)"""
     path = os.path.join(ROOT, "profiles", "neighbors_plummer.md")
+    fig = {}
     try:
         with open(path) as f:
             for line in f:
                 if line.startswith("traffic_bytes_per_particle:"):
-                    return float(line.split(":")[1]) * n
+                    fig["traffic"] = float(line.split(":")[1]) * n
+                elif line.startswith("warp_instructions_per_particle:"):
+                    fig["warp_instructions"] = float(line.split(":")[1]) * n
+                elif line.startswith("capture_particles:"):
+                    fig["source"] = (f"ncu capture of the {int(line.split(':')[1])}-particle case "
+                                     f"(profiles/neighbors_plummer.md), scaled by particle count")
     except OSError:
         pass
-    return None
+    return fig
 
 
 # ---------------------------------------------------------------------------------------------------------------
 # CPU side (oracle): bounded sample of the workload
 # ---------------------------------------------------------------------------------------------------------------
 
-def cpu_sample(n_sample, seed):
+def cpu_sample(n_sample, seed, tol=0.1):
+    """the workload's inputs for the CPU oracle: the same numpy generator as the GPU arm (cstone_synth, which loads no
+    CUDA library), h by per-particle bisection with the oracle's own neighbour counts to within tol of k"""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    from cstone_gb300 import workloads as W
+    import cstone_synth as S
 
-    x, y, z = W.plummer(n_sample, seed)
-    lo, hi = W.tight_box(x, y, z)
+    x, y, z = S.plummer(n_sample, seed)
+    lo, hi = S.tight_box(x, y, z)
     box = O.make_box(lo, hi)
-    h = O.h_for_k_neighbors_cpu(x, y, z, box, K_NEIGHBORS)
+    h = O.h_for_k_neighbors_cpu(x, y, z, box, K_NEIGHBORS, tol=tol)
     return O, x, y, z, h, box
+
+
+def host_cpu():
+    """model and logical CPU count of the host (lscpu), for the CPU baseline's record"""
+    info = {"model": None, "cpus": os.cpu_count()}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() == "Model name" and info["model"] is None:
+                info["model"] = v.strip()
+            elif k.strip() == "CPU(s)":
+                info["cpus"] = int(v.strip())
+    except (OSError, ValueError, subprocess.SubprocessError):
+        pass
+    return info
 
 
 def cpu_time(O, x, y, z, h, box):
@@ -200,9 +226,16 @@ def cpu_time(O, x, y, z, h, box):
 
 
 def run_reference(args, world, rank):
+    """The reference's CPU path (the oracle port, OpenMP on all host cores, serial stable sort as std::stable_sort)
+    on the GPU arm's workload: the same 16M Plummer particles (same generator and seed), tight box, Hilbert64, bucket
+    64, focus [0, 2^61), ngmax 200; h such that each particle has 100 +- 2 neighbours within 2h, prepared once with
+    the oracle (not timed). Loads only oracle/ libraries, never the CUDA library."""
     if rank != 0:
         return
-    O, x, y, z, h, box = cpu_sample(args.cpu_sample, args.seed)
+    n = args.n or 16 * 1024 * 1024
+    t0 = time.perf_counter()
+    O, x, y, z, h, box = cpu_sample(n, args.seed, tol=0.02)
+    prep_s = time.perf_counter() - t0
     for _ in range(args.warmup):
         cpu_time(O, x, y, z, h, box)
     t0 = time.perf_counter()
@@ -210,17 +243,19 @@ def run_reference(args, world, rank):
     for _ in range(args.steps):
         stages.append(cpu_time(O, x, y, z, h, box))
     dt = (time.perf_counter() - t0) / args.steps
-    value = args.cpu_sample / dt / 1e6
+    value = n / dt / 1e6
     cores = O.num_threads()
-    sample = (f"{args.cpu_sample} particles of the same Plummer workload (k=100 neighbours, h within 10% of the "
-              f"k-distance), full path per step")
+    sample = (f"the whole workload every step: {n} particles of the Plummer sphere (seed {args.seed}), h for "
+              f"{K_NEIGHBORS} +- 2 neighbours prepared by the oracle in {prep_s:.0f} s")
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "plummer-keys-to-neighbors", "n_particles": args.cpu_sample, "ngmax": NGMAX,
-                       "bucket_size": BUCKET, "keys": "hilbert64", "focus": "[0, 2^61)"},
+            "config": {"workload": "plummer-keys-to-neighbors", "n_particles_per_gpu": n, "ngmax": NGMAX,
+                       "bucket_size": BUCKET, "keys": "hilbert64", "focus": "[0, 2^61)",
+                       "neighbours_target": K_NEIGHBORS, "l2": "inputs (512 MB) larger than L2",
+                       "parallelism": "replicas x1"},
             "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "host_cpu": host_cpu()},
             "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "stage_seconds": {k: round(statistics.mean(s[k] for s in stages), 4) for k in stages[0]}}
     print(json.dumps(line), flush=True)
@@ -325,19 +360,10 @@ def run_batched(args, world, rank, local):
     sets = W.batched_sets(args.sets, args.seed + rank, dev)
     total = sum(st["n"] for st in sets)
     chunk_cap = 64 * 1024 * 1024
-    chunks, cur, acc = [], [], 0
-    for st in sets:
-        if cur and acc + st["n"] > chunk_cap:
-            chunks.append(cur)
-            cur, acc = [], 0
-        cur.append(st)
-        acc += st["n"]
-    chunks.append(cur)
-    packed = []
-    for ch in chunks:
-        offs = np.concatenate([[0], np.cumsum([st["n"] for st in ch])])
-        xyzh = [torch.cat([st[c] for st in ch]) for c in "xyzh"]
-        packed.append((offs, xyzh, [cs.make_box(st["lo"], st["hi"]) for st in ch], [st["bucket"] for st in ch]))
+    packed = [(offs, xyzh, [cs.make_box(sets[s]["lo"], sets[s]["hi"]) for s in ch], [sets[s]["bucket"] for s in ch])
+              for ch, offs, xyzh in W.chunk_sets(sets, chunk_cap)]
+    chunks = packed
+    del sets
     torch.cuda.synchronize()
 
     batch = cs.Batch(32, cs.MORTON, ngmax)
@@ -349,11 +375,14 @@ def run_batched(args, world, rank, local):
     pipes = {b: cs.Pipeline(32, 32, cs.MORTON, b, ngmax, 1.0, 1.0, False, True) for b in (16, 32, 64)}
 
     def per_set_pass(check=False):
+        """the per-set loop; with check, every set's neighbour counts and stored lists against the batched run's
+        (batched lists hold chunk-global indices: shifted by the set's offset)"""
         bad = 0
         for ci, (offs, (x, y, z, h), boxes, buckets) in enumerate(packed):
             if check:
                 batch.run(x, y, z, h, offs, boxes, buckets)
-                bnc = batch.outputs()["neighbor_counts"]
+                bo = batch.outputs()
+                bnc, bnb = bo["neighbor_counts"], bo["neighbors"]
             for j in range(len(buckets)):
                 a, e = int(offs[j]), int(offs[j + 1])
                 if e == a:
@@ -361,8 +390,12 @@ def run_batched(args, world, rank, local):
                 pipe = pipes[buckets[j]]
                 pipe.run(x[a:e], y[a:e], z[a:e], h[a:e], boxes[j])
                 if check:
-                    pnc = pipe.outputs()["neighbor_counts"]
-                    bad += int(not torch.equal(pnc, bnc[a:e]))
+                    po = pipe.outputs()
+                    pnc, pnb = po["neighbor_counts"], po["neighbors"]
+                    stored = torch.arange(ngmax, device=dev)[None, :] < pnc.clamp(max=ngmax)[:, None]
+                    same = torch.equal(pnc, bnc[a:e]) and torch.equal(torch.where(stored, pnb, 0),
+                                                                       torch.where(stored, bnb[a:e] - a, 0))
+                    bad += int(not same)
         return bad
 
     steps = max(1, min(args.steps, 3))
@@ -397,7 +430,8 @@ def run_batched(args, world, rank, local):
                 "particles_per_s": round(total / tb / 1e6, 3),
                 "per_set_loop": {"sets_per_s": round(args.sets / tp, 3), "ms_per_pass": round(tp * 1e3, 3),
                                  "particles_per_s_M": round(total / tp / 1e6, 3)},
-                "identical_neighbor_counts": mismatched == 0, "mismatched_sets": mismatched,
+                "identical_neighbor_lists": mismatched == 0, "mismatched_sets": mismatched,
+                "check": "every set's neighbour counts and stored lists, batched run against the per-set loop",
                 "clocks": clocks.summary()}
         print(json.dumps(line), flush=True)
 
@@ -612,51 +646,89 @@ def main():
     mean_nc = float(nc.double().mean())
     stored = float(nc.clamp(max=NGMAX).double().sum())
 
-    # ---- end to end through the host-buffer call ----
+    # ---- end to end through the host-buffer calls ----
+    # headline e2e: pinned host inputs in, neighbour counts, halo flags and the stored neighbour lists (CSR, written
+    # straight into pinned host memory) out, every step; the same without the lists beside it
     e2e = None
     if not args.no_e2e:
         hx, hy, hz, hh = (t.cpu().pin_memory() for t in (tx, ty, tz, th))
         nc_host = torch.empty(n, dtype=torch.int32).pin_memory()
         flags_host = torch.empty(res.num_nodes * 2 + 1024, dtype=torch.uint8).pin_memory()
-        for _ in range(max(1, args.warmup)):
-            pipe.run_host(hx, hy, hz, hh, box, FOCUS, nc_host, flags_host)
-        # one call per step and a wait for each step's results (synchronous calls)
-        barrier(world)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            pipe.run_host(hx, hy, hz, hh, box, FOCUS, nc_host, flags_host)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        sync_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
-        # pipelined calls: step k + 1's input copies overlap step k's computation, results copied back every step
-        barrier(world)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e0.record(stream)
-        for _ in range(args.steps):
-            pipe.run_host_async(hx, hy, hz, hh, box, FOCUS, nc_host, flags_host)
-        pipe.wait()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        barrier(world)
-        e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world)
-        e2e = {"value": round(world * n / (e2e_ms * 1e-3) / 1e6, 3), "unit": UNIT,
-               "h2d_bytes_per_step": 4 * n * 8, "d2h_bytes_per_step": n * 4 + pipe.result.num_nodes,
-               "ms_per_step": round(e2e_ms, 3),
-               "wall_ms_per_step": round((time.perf_counter() - t0) * 1e3 / args.steps, 3),
-               "api": "cs_pipeline_run_host_async per step, cs_pipeline_wait at the end",
-               "synchronous_calls": {"value": round(world * n / (sync_ms * 1e-3) / 1e6, 3),
-                                     "ms_per_step": round(sync_ms, 3), "api": "cs_pipeline_run_host per step"}}
+        total = int(stored)
+        off_host = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+        list_host = torch.empty(total + total // 8 + 1024, dtype=torch.int32).pin_memory()
+        del nc
+        torch.cuda.empty_cache()
 
-    # ---- roofline of the dominant kernel (neighbour search) ----
+        def timed_e2e(call, sync_each):
+            for _ in range(max(1, args.warmup)):
+                call()
+                if sync_each:
+                    pipe.wait()
+            pipe.wait()
+            barrier(world)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e0.record(stream)
+            for _ in range(args.steps):
+                call()
+                if sync_each:
+                    pipe.wait()
+            pipe.wait()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            wall = (time.perf_counter() - t0) * 1e3 / args.steps
+            barrier(world)
+            return max_over_ranks(e0.elapsed_time(e1) / args.steps, world), wall
+
+        lists_ms, lists_wall = timed_e2e(
+            lambda: pipe.run_host_csr(hx, hy, hz, hh, box, FOCUS, off_host, list_host, nc_out=nc_host,
+                                      flags_out=flags_host, asynchronous=True), False)
+        lists_ok = int(off_host[-1]) == total
+        lists_sync_ms, _ = timed_e2e(
+            lambda: pipe.run_host_csr(hx, hy, hz, hh, box, FOCUS, off_host, list_host, nc_out=nc_host,
+                                      flags_out=flags_host), False)
+        dev_ms, dev_wall = timed_e2e(
+            lambda: pipe.run_host_async(hx, hy, hz, hh, box, FOCUS, nc_host, flags_host), False)
+        d2h_small = n * 4 + res.num_nodes
+        e2e = {"value": round(world * n / (lists_ms * 1e-3) / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": 4 * n * 8,
+               "d2h_bytes_per_step": d2h_small + 8 * (n + 1) + 4 * total,
+               "ms_per_step": round(lists_ms, 3), "wall_ms_per_step": round(lists_wall, 3),
+               "returns": "neighbour counts, halo flags and the stored neighbour lists (CSR: u64 offsets + u32 "
+                          "indices, the first min(nc, ngmax) per particle)",
+               "lists_total": total, "lists_complete": lists_ok,
+               "api": "cs_pipeline_run_host_csr_async per step, cs_pipeline_wait at the end",
+               "synchronous_calls": {"value": round(world * n / (lists_sync_ms * 1e-3) / 1e6, 3),
+                                     "ms_per_step": round(lists_sync_ms, 3), "api": "cs_pipeline_run_host_csr"},
+               "lists_on_device": {"value": round(world * n / (dev_ms * 1e-3) / 1e6, 3),
+                                   "ms_per_step": round(dev_ms, 3), "wall_ms_per_step": round(dev_wall, 3),
+                                   "d2h_bytes_per_step": d2h_small,
+                                   "returns": "neighbour counts and halo flags; lists stay in device memory",
+                                   "api": "cs_pipeline_run_host_async per step, cs_pipeline_wait at the end"}}
+
+    # ---- roofline of the dominant kernel (neighbour search): HBM bytes and issued instructions ----
     peak, peak_kind = measured_hbm_peak()
     nb_bytes = n * (4 * 8 + 4) + 4.0 * stored  # x,y,z,h read + count written + stored neighbour indices
     nb_ms = stages["neighbors"]
     achieved = nb_bytes / (nb_ms * 1e-3) / 1e9
-    roofline = {"kernel": "findNeighborsGroupKernel<double>", "bound": "hbm", "achieved": round(achieved, 1),
+    prof = profile_figures(n)
+    sm_mhz = clocks.summary().get("sm_mhz") or 2070.0
+    roofline = {"kernel": "findNeighborsGroupKernel<double>", "bound": "issue", "achieved": round(achieved, 1),
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": profiled_traffic(n), "algorithmic_bytes": nb_bytes, "ms": round(nb_ms, 4)}
+                "traffic": prof.get("traffic"), "algorithmic_bytes": nb_bytes, "ms": round(nb_ms, 4),
+                "traffic_source": prof.get("source"),
+                "note": "the hbm fraction above is algorithmic bytes / event time / measured copy bandwidth; the "
+                        "kernel is bound by instruction issue, whose fraction is below"}
+    if prof.get("warp_instructions"):
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        issue_peak = sms * 4 * sm_mhz * 1e6 / 1e9  # warp instructions per ns = G/s
+        issue_ach = prof["warp_instructions"] / (nb_ms * 1e-3) / 1e9
+        roofline["issue"] = {"achieved": round(issue_ach, 1), "peak": round(issue_peak, 1),
+                             "unit": "G warp-instructions/s", "frac": round(issue_ach / issue_peak, 4),
+                             "warp_instructions": prof["warp_instructions"],
+                             "peak_basis": f"{sms} SMs x 4 issue slots/clk x {sm_mhz:.0f} MHz (sampled)",
+                             "source": prof.get("source")}
 
     # ---- CPU baseline on a bounded sample ----
     cpu = None

@@ -9,6 +9,7 @@
 #include "cs_common.cuh"
 #include "halos.cuh"
 #include "pipeline.cuh"
+#include "neighbor_csr.cuh"
 #include "neighbors.cuh"
 #include "octree_build.cuh"
 #include "octree_link.cuh"
@@ -76,6 +77,8 @@ struct Pipeline final : PipelineBase
     cudaStream_t d2hStream = nullptr;
     cudaEvent_t outReady = nullptr, errCopied = nullptr, outDone = nullptr;
     uint32_t* herrHost   = nullptr; // pinned, the last copied error words
+    uint32_t* listOverflowHost = nullptr; // pinned, set by the list compaction when a list buffer was too small
+    DevBuf csrWs;
     bool outPending      = false;   // a copy-back whose errors are not yet reported
     int stickyRc         = CS_OK;   // an earlier run's device error, reported by the next wait
     char stickyMsg[160]  = {};
@@ -108,6 +111,7 @@ struct Pipeline final : PipelineBase
         for (cudaEvent_t e : {outReady, errCopied, outDone})
             if (e) cudaEventDestroy(e);
         if (herrHost) cudaFreeHost(herrHost);
+        if (listOverflowHost) cudaFreeHost(listOverflowHost);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
     }
@@ -761,12 +765,18 @@ struct Pipeline final : PipelineBase
     }
 
     // Enqueue the copy of the last run's results to host memory on the copy-back stream, after the run's work.
-    int copyBackAsync(cudaStream_t s, uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap) override
+    int copyBackAsync(cudaStream_t s, uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap, uint64_t* listOffsets,
+                      uint32_t* listHost, size_t listCap) override
     {
         if (flagsHost && flagsCap < size_t(last.num_nodes))
         {
             setLastError("pipeline: halo flag buffer holds %zu, %d needed", flagsCap, last.num_nodes);
             return CS_ERR_CAPACITY;
+        }
+        if (listOffsets && !cfg.do_neighbors)
+        {
+            setLastError("pipeline: neighbour lists requested from a pipeline without neighbour search");
+            return CS_ERR_INVALID;
         }
         if (!d2hStream)
         {
@@ -774,6 +784,8 @@ struct Pipeline final : PipelineBase
             for (cudaEvent_t* e : {&outReady, &errCopied, &outDone})
                 CSG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
             CSG_CUDA_TRY(cudaHostAlloc(&herrHost, 4 * sizeof(uint32_t), cudaHostAllocDefault));
+            CSG_CUDA_TRY(cudaHostAlloc(&listOverflowHost, sizeof(uint32_t), cudaHostAllocMapped));
+            *listOverflowHost = 0;
         }
         if (outPending)
         {
@@ -795,6 +807,17 @@ struct Pipeline final : PipelineBase
         if (flagsHost)
             CSG_CUDA_TRY(
                 cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, d2hStream));
+        if (listOffsets)
+        {
+            // the stored neighbour indices, compacted straight into the caller's pinned buffers over the host link
+            int rc = csrWs.ensure(neighborCsrWorkspaceBytes(n));
+            if (rc) return rc;
+            uint32_t* flag = nullptr;
+            CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&flag), listOverflowHost, 0));
+            if ((rc = neighborCsr(d2hStream, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax, listOffsets,
+                                  listHost, listHost ? listCap : 0, csrWs.p, csrWs.bytes, flag)))
+                return rc;
+        }
         CSG_CUDA_TRY(cudaEventRecord(outDone, d2hStream));
         outPending = true;
         return CS_OK;
@@ -809,6 +832,12 @@ struct Pipeline final : PipelineBase
             CSG_CUDA_TRY(cudaEventSynchronize(outDone));
             outPending = false;
             rc         = deviceErrors(herrHost);
+            if (rc == CS_OK && listOverflowHost && *listOverflowHost)
+            {
+                setLastError("pipeline: a neighbour list buffer was too small (offsets[n] holds the entries needed)");
+                rc = CS_ERR_CAPACITY;
+            }
+            if (listOverflowHost) *listOverflowHost = 0;
         }
         if (stickyRc != CS_OK)
         {
@@ -966,6 +995,33 @@ extern "C" int cs_pipeline_run_host_async(cs_pipeline p, cs_stream_t stream, con
     int rc = p->impl->run(cudaStream_t(stream), x, y, z, h, n, *box, f0, f1, res, true);
     if (rc) return rc;
     return p->impl->copyBackAsync(cudaStream_t(stream), ncHost, flagsHost, flagsCap);
+}
+
+extern "C" int cs_pipeline_run_host_csr_async(cs_pipeline p, cs_stream_t stream, const void* x, const void* y,
+                                              const void* z, const void* h, size_t n, const cs_box* box, uint64_t f0,
+                                              uint64_t f1, uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap,
+                                              uint64_t* offsetsHost, uint32_t* listHost, size_t listCap,
+                                              cs_pipeline_result* res)
+{
+    if (!p || !box || !x || !y || !z || !h || !offsetsHost || (!listHost && listCap))
+    {
+        setLastError("pipeline run: null argument");
+        return CS_ERR_INVALID;
+    }
+    int rc = p->impl->run(cudaStream_t(stream), x, y, z, h, n, *box, f0, f1, res, true);
+    if (rc) return rc;
+    return p->impl->copyBackAsync(cudaStream_t(stream), ncHost, flagsHost, flagsCap, offsetsHost, listHost, listCap);
+}
+
+extern "C" int cs_pipeline_run_host_csr(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
+                                        const void* h, size_t n, const cs_box* box, uint64_t f0, uint64_t f1,
+                                        uint32_t* ncHost, uint8_t* flagsHost, size_t flagsCap, uint64_t* offsetsHost,
+                                        uint32_t* listHost, size_t listCap, cs_pipeline_result* res)
+{
+    int rc = cs_pipeline_run_host_csr_async(p, stream, x, y, z, h, n, box, f0, f1, ncHost, flagsHost, flagsCap,
+                                            offsetsHost, listHost, listCap, res);
+    if (rc) return rc;
+    return p->impl->wait();
 }
 
 extern "C" int cs_pipeline_wait(cs_pipeline p)

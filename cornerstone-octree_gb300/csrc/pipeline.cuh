@@ -29,8 +29,10 @@ struct PipelineBase
                     const cs_box& box, uint64_t f0, uint64_t f1, cs_pipeline_result* res, bool hostIn) = 0;
     virtual int outputs(cs_pipeline_outputs* o) = 0;
     virtual size_t deviceBytes() const          = 0;
-    //! enqueue the copy of the last run's counts and halo flags (either may be null) to host memory
-    virtual int copyBackAsync(cudaStream_t s, uint32_t* nc, uint8_t* flags, size_t flagsCap) = 0;
+    //! enqueue the copy of the last run's counts and halo flags (either may be null) to host memory, and optionally
+    //! its neighbour lists as CSR (listOffsets: n + 1 entries; list: listCap entries; both pinned host memory)
+    virtual int copyBackAsync(cudaStream_t s, uint32_t* nc, uint8_t* flags, size_t flagsCap,
+                              uint64_t* listOffsets = nullptr, uint32_t* list = nullptr, size_t listCap = 0) = 0;
     //! wait for the last copy-back; the first device error of the runs since the previous wait
     virtual int wait() = 0;
     virtual int step(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, size_t n,

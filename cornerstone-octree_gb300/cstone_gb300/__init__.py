@@ -135,6 +135,20 @@ def gather4(perm, a, b, c, d):
     return outs
 
 
+def neighbors_csr(nb, nc, ngmax, offsets=None, lst=None):
+    """compacts ngmax-strided neighbour rows (nb: n x ngmax, nc: n) into (offsets[n + 1] int64, list int32)"""
+    n = nc.numel()
+    if offsets is None:
+        offsets = torch.empty(n + 1, dtype=torch.int64, device=nc.device)
+    if lst is None:
+        total = int(nc.clamp(max=ngmax).sum()) if n else 0
+        lst = torch.empty(max(total, 1), dtype=torch.int32, device=nc.device)
+    lib.cs_neighbors_csr_workspace_bytes.restype = C.c_size_t
+    _check(lib.cs_neighbors_csr(_stream(), _p(nb), _p(nc), C.c_size_t(n), C.c_uint(ngmax), _p(offsets), _p(lst),
+                                C.c_size_t(lst.numel()), None, C.c_size_t(0)))
+    return offsets, lst
+
+
 # ---------------------------------------------------------------------------------------------------------------
 # cornerstone leaf array
 # ---------------------------------------------------------------------------------------------------------------
@@ -397,6 +411,18 @@ class Pipeline:
                                               C.c_size_t(x.numel()), C.byref(box), C.c_uint64(focus[0]),
                                               C.c_uint64(focus[1]), _p(nc_out), _p(flags_out), C.c_size_t(fcap),
                                               C.byref(self.result)))
+        return self.result
+
+    def run_host_csr(self, x, y, z, h, box, focus, offsets_out, list_out, nc_out=None, flags_out=None,
+                     asynchronous=False):
+        """as run_host / run_host_async, with the neighbour lists returned as CSR into pinned host tensors:
+        offsets_out (int64, n + 1), list_out (int32, capacity); row i = list_out[offsets_out[i]:offsets_out[i+1]]"""
+        fcap = flags_out.numel() if flags_out is not None else 0
+        self._n = x.numel()
+        fn = lib.cs_pipeline_run_host_csr_async if asynchronous else lib.cs_pipeline_run_host_csr
+        _check(fn(self.handle, _stream(), _p(x), _p(y), _p(z), _p(h), C.c_size_t(x.numel()), C.byref(box),
+                  C.c_uint64(focus[0]), C.c_uint64(focus[1]), _p(nc_out), _p(flags_out), C.c_size_t(fcap),
+                  _p(offsets_out), _p(list_out), C.c_size_t(list_out.numel()), C.byref(self.result)))
         return self.result
 
     def wait(self):

@@ -1,12 +1,13 @@
 """Seeded synthetic inputs for the benchmark configurations (no dataset is involved).
 
-- uniform(n, lo, hi, seed): i.i.d. uniform coordinates in a box.
-- plummer(n, seed): Plummer sphere with scale radius 1 truncated at r = 100 (R = (u^(-2/3) - 1)^(-1/2),
-  z = (1 - 2u) R, phi = 2 pi u), shifted to its centre of mass.
+- uniform, plummer, tight_box: the numpy generators of cstone_synth (re-exported).
+- batched_sets(...): the batched workload's sets, generated on the device.
 - h_for_k_neighbors(...): per-particle smoothing length such that exactly k other particles lie within 2h
   (the k-th nearest-neighbour distance, up to the gap to the (k+1)-th), found by per-particle bisection on
   neighbour counts computed with this library's own GPU search. This is input preparation, not part of the path.
 """
+import os
+import sys
 import types
 
 import numpy as np
@@ -14,35 +15,8 @@ import torch
 
 from . import HILBERT, Pipeline, find_neighbors
 
-
-def uniform(n, lo, hi, seed, dtype=np.float64):
-    rng = np.random.default_rng(seed)
-    return [rng.uniform(lo, hi, n).astype(dtype) for _ in range(3)]
-
-
-def plummer(n, seed, rmax=100.0):
-    rng = np.random.default_rng(seed)
-    xs, ys, zs = [], [], []
-    need = n
-    while need > 0:
-        m = int(need * 1.01) + 64
-        u0 = rng.random(m)
-        u1 = rng.random(m)
-        u2 = rng.random(m)
-        ok = u0 > 0
-        r = np.full(m, np.inf)
-        r[ok] = 1.0 / np.sqrt(u0[ok] ** (-2.0 / 3.0) - 1.0)
-        keep = r < rmax
-        r, u1, u2 = r[keep][:need], u1[keep][:need], u2[keep][:need]
-        zz = (1.0 - 2.0 * u1) * r
-        phi = 2.0 * np.pi * u2
-        rho = np.sqrt(r * r - zz * zz)
-        xs.append(rho * np.cos(phi))
-        ys.append(rho * np.sin(phi))
-        zs.append(zz)
-        need -= r.size
-    x, y, z = (np.concatenate(a) for a in (xs, ys, zs))
-    return x - x.mean(), y - y.mean(), z - z.mean()
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+from cstone_synth import plummer, tight_box, uniform  # noqa: E402  (numpy-only generators, shared with the CPU arm)
 
 
 def batched_sets(num_sets, seed, device, lo_exp=10, hi_exp=20, k=60):
@@ -88,10 +62,6 @@ def batched_sets(num_sets, seed, device, lo_exp=10, hi_exp=20, k=60):
     return sets
 
 
-def tight_box(x, y, z):
-    return (float(x.min()), float(y.min()), float(z.min())), (float(x.max()), float(y.max()), float(z.max()))
-
-
 def h_for_k_neighbors(x, y, z, box, k=100, bucket=64, key_bits=64, kind=HILBERT, max_iter=64):
     """x, y, z: device tensors (input order). Returns h (input order) and the final neighbour counts."""
     n = x.numel()
@@ -132,3 +102,23 @@ def h_for_k_neighbors(x, y, z, box, k=100, bucket=64, key_bits=64, kind=HILBERT,
     nc_in = torch.empty_like(nc)
     nc_in[out["order"].long()] = nc
     return h_in, nc_in
+
+
+def chunk_sets(sets, chunk_cap=64 * 1024 * 1024):
+    """groups consecutive sets of batched_sets(...) into chunks of at most chunk_cap particles (a larger set forms a
+    chunk of its own); per chunk: (set indices, offsets[len + 1], concatenated x, y, z, h device tensors)"""
+    chunks, cur, acc = [], [], 0
+    for s, st in enumerate(sets):
+        if cur and acc + st["n"] > chunk_cap:
+            chunks.append(cur)
+            cur, acc = [], 0
+        cur.append(s)
+        acc += st["n"]
+    if cur:
+        chunks.append(cur)
+    packed = []
+    for ch in chunks:
+        offs = np.concatenate([[0], np.cumsum([sets[s]["n"] for s in ch])])
+        xyzh = [torch.cat([sets[s][c] for s in ch]) for c in "xyzh"]
+        packed.append((ch, offs, xyzh))
+    return packed

@@ -301,6 +301,15 @@ int cs_find_neighbors_f64(cs_stream_t stream, const double* x, const double* y, 
                           uint32_t first, uint32_t last, const cs_box* box, const cs_ns_view* tree, unsigned ngmax,
                           uint32_t* neighbors, uint32_t* counts);
 
+/* No call counterpart in the reference (its findNeighbors leaves the ngmax-strided rows to the caller): compaction of
+ * the rows written by cs_find_neighbors_* into CSR form. offsets (u64, n + 1 entries, offsets[n] = total) and list
+ * (list_capacity entries) may be device or pinned host memory; row i's min(neighbor_counts[i], ngmax) entries go to
+ * list[offsets[i] ..). Entries at or past list_capacity are skipped; compare offsets[n] with it. */
+size_t cs_neighbors_csr_workspace_bytes(size_t n);
+int cs_neighbors_csr(cs_stream_t stream, const uint32_t* neighbors, const uint32_t* neighbor_counts, size_t n,
+                     unsigned ngmax, uint64_t* offsets, uint32_t* list, size_t list_capacity, void* workspace,
+                     size_t workspace_bytes);
+
 /* ---- whole path: keys -> sort -> gather -> computeOctree -> link -> geometry -> findHalos -> findNeighbors ---------
  * The single-rank inner part of the reference's Domain::sync + discoverHalos + neighbour search
  * (domain/assignment.hpp:105-120, focus/octree_focus_mpi.hpp:512-568, findneighbors.hpp:156-177), as one object that
@@ -371,6 +380,23 @@ int cs_pipeline_run_host_async(cs_pipeline p, cs_stream_t stream, const void* x,
 /* waits for the results of the last cs_pipeline_run_host_async; returns the first device error (sort look-back
  * timeout, traversal stack overflow) of the runs since the previous wait */
 int cs_pipeline_wait(cs_pipeline p);
+/* The host-buffer runs above with the neighbour lists returned as well, in compressed sparse row form: row i's first
+ * min(nc_i, ngmax) neighbours (ascending, as findNeighbors stores them into its ngmax-strided `neighbors` argument,
+ * findneighbors.hpp:156-177) are list_host[offsets_host[i] .. offsets_host[i+1]), offsets_host has n + 1 entries and
+ * offsets_host[n] is the total. Both buffers must be pinned host memory (cudaHostAlloc / cudaHostRegister): the
+ * lists are compacted on the device and written straight into them over the host link, on the copy-back stream.
+ * Entries past list_capacity are not written and the wait reports CS_ERR_CAPACITY (offsets_host[n] = entries
+ * needed). The _async form follows cs_pipeline_run_host_async (results valid after cs_pipeline_wait). */
+int cs_pipeline_run_host_csr(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
+                             const void* h, size_t n, const cs_box* box, uint64_t focus_start, uint64_t focus_end,
+                             uint32_t* neighbor_counts_host, uint8_t* halo_flags_host, size_t halo_flags_capacity,
+                             uint64_t* offsets_host, uint32_t* list_host, size_t list_capacity,
+                             cs_pipeline_result* result);
+int cs_pipeline_run_host_csr_async(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
+                                   const void* h, size_t n, const cs_box* box, uint64_t focus_start,
+                                   uint64_t focus_end, uint32_t* neighbor_counts_host, uint8_t* halo_flags_host,
+                                   size_t halo_flags_capacity, uint64_t* offsets_host, uint32_t* list_host,
+                                   size_t list_capacity, cs_pipeline_result* result);
 int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out);
 /* bytes of device memory the pipeline holds */
 size_t cs_pipeline_device_bytes(cs_pipeline p);

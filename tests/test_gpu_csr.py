@@ -1,0 +1,87 @@
+"""Neighbour lists returned in compressed sparse row form, against the oracle's ngmax-strided rows.
+
+findNeighbors (findneighbors.hpp:156-177) stores particle i's first min(nc_i, ngmax) neighbours in row i of an
+n x ngmax array. cs_neighbors_csr compacts those rows on the device; cs_pipeline_run_host_csr runs the whole path from
+host buffers and writes the compacted lists straight into pinned host memory. Both must reproduce the oracle's rows
+exactly (integer work: bit for bit), including truncated rows (nc > ngmax) and empty ones.
+"""
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import u32, uniform
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_csr(nb, nc, ngmax):
+    m = np.minimum(nc, ngmax).astype(np.int64)
+    off = np.zeros(nc.size + 1, np.int64)
+    np.cumsum(m, out=off[1:])
+    lst = np.concatenate([nb[i, : m[i]] for i in range(nc.size)]) if nc.size else np.zeros(0, np.uint32)
+    return off, lst.astype(np.uint32)
+
+
+def _case(O, n, ngmax, h, seed):
+    x, y, z = uniform(O, seed, n, -1.0, 1.0)
+    hh = np.full(n, h)
+    # a few isolated particles (empty rows) and a dense clump (rows truncated at ngmax)
+    x[:5] = 50.0 + np.arange(5)
+    y[:5] = 50.0
+    z[:5] = 50.0
+    x[5:400] = 0.001 * np.arange(395) / 395
+    y[5:400] = 0.0
+    z[5:400] = 0.0
+    box = O.make_box(-1.0, 60.0)
+    ref = O.pipeline(x, y, z, hh, box, 16, ngmax)
+    return x, y, z, hh, ref
+
+
+def test_neighbors_csr_on_device_matches_oracle(cs, O):
+    n, ngmax = 30_000, 48
+    x, y, z, h, ref = _case(O, n, ngmax, 0.05, 3)
+    assert (ref["nc"] > ngmax).any() and (ref["nc"] == 0).any()
+    nb = torch.from_numpy(ref["nb"].astype(np.int64).astype(np.int32)).cuda()
+    nc = torch.from_numpy(ref["nc"].astype(np.int32)).cuda()
+    off, lst = cs.neighbors_csr(nb, nc, ngmax)
+    torch.cuda.synchronize()
+    roff, rlst = _oracle_csr(ref["nb"], ref["nc"], ngmax)
+    assert np.array_equal(off.cpu().numpy(), roff)
+    assert np.array_equal(u32(lst[: roff[-1]]), rlst)
+
+
+def test_pipeline_run_host_csr_matches_oracle(cs, O):
+    n, ngmax = 30_000, 48
+    x, y, z, h, ref = _case(O, n, ngmax, 0.05, 4)
+    roff, rlst = _oracle_csr(ref["nb"], ref["nc"], ngmax)
+    hx, hy, hz, hh = (torch.from_numpy(a).pin_memory() for a in (x, y, z, h))
+    off = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    lst = torch.empty(int(roff[-1]) + 7, dtype=torch.int32).pin_memory()
+    nc = torch.empty(n, dtype=torch.int32).pin_memory()
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, 16, ngmax, 1.0, 1.0, False, True)
+    box = cs.make_box(-1.0, 60.0)
+    for asynchronous in (False, True, True):  # the async calls reuse the same host buffers
+        pipe.run_host_csr(hx, hy, hz, hh, box, (0, 0), off, lst, nc_out=nc, asynchronous=asynchronous)
+    pipe.wait()
+    assert np.array_equal(nc.numpy().view(np.uint32), ref["nc"])
+    assert np.array_equal(off.numpy(), roff)
+    assert np.array_equal(lst.numpy()[: roff[-1]].view(np.uint32), rlst)
+
+
+def test_pipeline_run_host_csr_reports_a_small_list_buffer(cs, O):
+    n, ngmax = 30_000, 48
+    x, y, z, h, ref = _case(O, n, ngmax, 0.05, 5)
+    roff, _ = _oracle_csr(ref["nb"], ref["nc"], ngmax)
+    hx, hy, hz, hh = (torch.from_numpy(a).pin_memory() for a in (x, y, z, h))
+    off = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    lst = torch.empty(int(roff[-1]) // 2, dtype=torch.int32).pin_memory()
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, 16, ngmax, 1.0, 1.0, False, True)
+    box = cs.make_box(-1.0, 60.0)
+    with pytest.raises(cs.CsError) as e:
+        pipe.run_host_csr(hx, hy, hz, hh, box, (0, 0), off, lst)
+    assert e.value.code == cs.CS_ERR_CAPACITY
+    assert int(off[-1]) == int(roff[-1])
+    # the flag is cleared by the wait that reported it: a large enough buffer works again
+    big = torch.empty(int(roff[-1]), dtype=torch.int32).pin_memory()
+    pipe.run_host_csr(hx, hy, hz, hh, box, (0, 0), off, big)
+    assert np.array_equal(off.numpy(), roff)
