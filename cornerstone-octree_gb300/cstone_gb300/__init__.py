@@ -669,3 +669,159 @@ class _CudaArray:
         self.__cuda_array_interface__ = {"shape": (nbytes,), "typestr": "|u1", "data": (int(ptr), False),
                                          "version": 3}
 
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# around the path: upsweeps, source centres, target groups, SFC gaps, focus tree
+# ---------------------------------------------------------------------------------------------------------------
+
+for _name in ("cs_upsweep_workspace_bytes", "cs_group_splits_workspace_bytes", "cs_spanning_tree_workspace_bytes",
+              "cs_node_layout_workspace_bytes", "cs_neighbors_csr_workspace_bytes"):
+    getattr(lib, _name).restype = C.c_size_t
+
+
+def _host_i32(a):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.int32))
+    return a, a.ctypes.data_as(C.c_void_p)
+
+
+def upsweep_sum(child_offsets, node_counts, parents=None, level_range=None):
+    """upsweepSumGpu in place on node_counts (uint32 as int32, leaf values set): one launch with parents, else level by
+    level from level_range (host array)"""
+    n = child_offsets.numel()
+    lr, lrp = _host_i32(level_range if level_range is not None else [0])
+    nl = lr.size - 1 if level_range is not None else 0
+    _check(lib.cs_upsweep_sum(_stream(), nl, lrp if level_range is not None else None, _p(child_offsets),
+                              _p(parents), n, _p(node_counts), None, C.c_size_t(0)))
+    return node_counts
+
+
+def leaf_source_centers(x, y, z, m, leaf_to_internal_leaves, layout, centers):
+    """mass centres of the leaves into centers[num_nodes, 4] (f64 coordinates with f64 or f32 masses, or all f32)"""
+    if x.dtype == torch.float64:
+        fn = lib.cs_leaf_source_centers_f64 if m.dtype == torch.float64 else lib.cs_leaf_source_centers_f64_m32
+    else:
+        fn = lib.cs_leaf_source_centers_f32
+    _check(fn(_stream(), _p(x), _p(y), _p(z), _p(m), _p(leaf_to_internal_leaves), leaf_to_internal_leaves.numel(),
+              _p(layout), _p(centers)))
+    return centers
+
+
+def upsweep_source_centers(child_offsets, centers, parents=None, level_range=None):
+    n = child_offsets.numel()
+    lr, lrp = _host_i32(level_range if level_range is not None else [0])
+    nl = lr.size - 1 if level_range is not None else 0
+    fn = lib.cs_upsweep_source_centers_f64 if centers.dtype == torch.float64 else lib.cs_upsweep_source_centers_f32
+    _check(fn(_stream(), nl, lrp if level_range is not None else None, _p(child_offsets), _p(parents), n,
+              _p(centers), None, C.c_size_t(0)))
+    return centers
+
+
+def group_splits(first, last, x, y, z, h, leaves, layout, box, group_size=32, tol=8.0):
+    """computeGroupSplits: returns the group boundaries (num_groups + 1 int32 device tensor)"""
+    cap = 2 * ((last - first) // group_size + 2)
+    fn = lib.cs_group_splits_f64 if x.dtype == torch.float64 else lib.cs_group_splits_f32
+    while True:
+        groups = torch.empty(cap, dtype=torch.int32, device=x.device)
+        ng = C.c_uint32()
+        rc = fn(_stream(), C.c_uint32(first), C.c_uint32(last), _p(x), _p(y), _p(z), _p(h), _p(leaves),
+                leaves.numel() - 1, _p(layout), C.byref(box), C.c_uint(group_size), C.c_float(tol), _p(groups),
+                C.c_size_t(cap), C.byref(ng), None, C.c_size_t(0))
+        if rc == CS_ERR_CAPACITY:
+            cap = ng.value + 1
+            continue
+        _check(rc)
+        return groups[: ng.value + 1]
+
+
+def spanning_tree(keys):
+    """computeSpanningTree of sorted keys (first 0, last nodeRange(0)); int32/int64 tensors hold u32/u64 keys"""
+    bits = key_bits(keys)
+    fn = lib.cs_spanning_tree_u32 if bits == 32 else lib.cs_spanning_tree_u64
+    cap = 8 * keys.numel() + 64
+    while True:
+        out = torch.empty(cap, dtype=keys.dtype, device=keys.device)
+        size = C.c_int32()
+        rc = fn(_stream(), _p(keys), keys.numel(), _p(out), cap, C.byref(size), None, C.c_size_t(0))
+        if rc == CS_ERR_CAPACITY:
+            cap = size.value
+            continue
+        _check(rc)
+        return out[: size.value]
+
+
+def count_sfc_gaps(tree):
+    bits = key_bits(tree)
+    ops = torch.empty(tree.numel(), dtype=torch.int32, device=tree.device)
+    fn = lib.cs_count_sfc_gaps_u32 if bits == 32 else lib.cs_count_sfc_gaps_u64
+    _check(fn(_stream(), _p(tree), tree.numel() - 1, _p(ops)))
+    return ops[: tree.numel() - 1]
+
+
+def fill_sfc_gaps(tree, scanned_ops):
+    bits = key_bits(tree)
+    out = torch.empty(int(scanned_ops[-1]) + 1, dtype=tree.dtype, device=tree.device)
+    fn = lib.cs_fill_sfc_gaps_u32 if bits == 32 else lib.cs_fill_sfc_gaps_u64
+    _check(fn(_stream(), _p(tree), tree.numel() - 1, _p(scanned_ops), _p(out)))
+    return out
+
+
+def _kf(bits, name):
+    return getattr(lib, f"{name}_u{bits}")
+
+
+def rebalance_decision_essential(prefixes, child_offsets, parents, counts, macs, focus, bucket):
+    bits = key_bits(prefixes)
+    n = prefixes.numel()
+    ops = torch.empty(n, dtype=torch.int32, device=prefixes.device)
+    kt = C.c_uint32 if bits == 32 else C.c_uint64
+    _check(_kf(bits, "cs_rebalance_decision_essential")(_stream(), _p(prefixes), _p(child_offsets), _p(parents),
+                                                        _p(counts), _p(macs), kt(focus[0]), kt(focus[1]),
+                                                        C.c_uint(bucket), _p(ops), n))
+    return ops
+
+
+def mac_refine_decision(prefixes, macs, leaf_to_internal_leaves, focus_first, focus_last):
+    bits = key_bits(prefixes)
+    L = leaf_to_internal_leaves.numel()
+    ops = torch.empty(L, dtype=torch.int32, device=prefixes.device)
+    _check(_kf(bits, "cs_mac_refine_decision")(_stream(), _p(prefixes), _p(macs), _p(leaf_to_internal_leaves), L,
+                                               focus_first, focus_last, _p(ops)))
+    return ops
+
+
+def protect_ancestors(prefixes, parents, ops):
+    """in place on ops; returns converged (no op differs from 1)"""
+    bits = key_bits(prefixes)
+    changed = torch.zeros(1, dtype=torch.int32, device=prefixes.device)
+    conv = C.c_int()
+    _check(_kf(bits, "cs_protect_ancestors")(_stream(), _p(prefixes), _p(parents), _p(ops), prefixes.numel(),
+                                             _p(changed), C.byref(conv)))
+    return bool(conv.value)
+
+
+def enforce_keys(forced_keys, prefixes, child_offsets, parents, ops):
+    """in place on ops; returns the status (0 converged, 1 cancelMerge, 2 rebalance, 3 failed)"""
+    bits = key_bits(prefixes)
+    sdev = torch.zeros(1, dtype=torch.int32, device=prefixes.device)
+    st = C.c_int()
+    _check(_kf(bits, "cs_enforce_keys")(_stream(), _p(forced_keys), forced_keys.numel(), _p(prefixes),
+                                        _p(child_offsets), _p(parents), _p(ops), _p(sdev), C.byref(st)))
+    return st.value
+
+
+def range_count(leaves, counts, leaves_focus, focus_idx, counts_focus=None):
+    bits = key_bits(leaves)
+    if counts_focus is None:
+        counts_focus = torch.zeros(leaves_focus.numel() - 1, dtype=torch.int32, device=leaves.device)
+    _check(_kf(bits, "cs_range_count")(_stream(), _p(leaves), leaves.numel(), _p(counts), _p(leaves_focus),
+                                       _p(focus_idx), focus_idx.numel(), _p(counts_focus)))
+    return counts_focus
+
+
+def node_layout(focus_leaf_counts, flags, leaf_to_internal_leaves, first, last):
+    L = focus_leaf_counts.numel()
+    out = torch.empty(L + 1, dtype=torch.int32, device=focus_leaf_counts.device)
+    _check(lib.cs_node_layout(_stream(), _p(focus_leaf_counts), L, _p(flags), _p(leaf_to_internal_leaves), first,
+                              last, _p(out), None, C.c_size_t(0)))
+    return out

@@ -310,6 +310,119 @@ int cs_neighbors_csr(cs_stream_t stream, const uint32_t* neighbors, const uint32
                      unsigned ngmax, uint64_t* offsets, uint32_t* list, size_t list_capacity, void* workspace,
                      size_t workspace_bytes);
 
+/* ---- upsweeps and source centres ------------------------------------------------------------------------------
+ * cs_upsweep_sum replaces upsweepSumGpu(exec, numLevels, levelRange, childOffsets, nodeCounts)
+ * (tree/octree_gpu.cu:218-236, NodeCount tree/octree.hpp:603-615): counts of nodes with children become
+ * min(2^32 - 1, sum of their 8 children); leaf counts are inputs. With `parents` (the OctreeView array) the whole
+ * upsweep is one launch (arrival counters per node, workspace cs_upsweep_workspace_bytes); with parents = NULL it runs
+ * level by level from level_range_host (num_levels + 1 host entries), as the reference does.
+ * cs_leaf_source_centers_* replace computeLeafSourceCenterGpu (focus/source_center_gpu.cu:103-170): per leaf the mass
+ * centre (x, y, z, sum |m|) written to centers[4 * leafToInternal[leaf]], evaluated in the order of the reference's
+ * CPU massCenter (focus/source_center.hpp:70-81). cs_upsweep_source_centers_* replace upsweepCentersGpu
+ * (focus/source_center_gpu.cu:173-205) with CombineSourceCenter (focus/source_center.hpp:84-98). */
+size_t cs_upsweep_workspace_bytes(int32_t num_nodes);
+int cs_upsweep_sum(cs_stream_t stream, int num_levels, const int32_t* level_range_host, const int32_t* child_offsets,
+                   const int32_t* parents, int32_t num_nodes, uint32_t* node_counts, void* workspace,
+                   size_t workspace_bytes);
+int cs_leaf_source_centers_f64(cs_stream_t stream, const double* x, const double* y, const double* z,
+                               const double* m, const int32_t* leaf_to_internal, int32_t num_leaves,
+                               const uint32_t* layout, double* centers);
+int cs_leaf_source_centers_f64_m32(cs_stream_t stream, const double* x, const double* y, const double* z,
+                                   const float* m, const int32_t* leaf_to_internal, int32_t num_leaves,
+                                   const uint32_t* layout, double* centers);
+int cs_leaf_source_centers_f32(cs_stream_t stream, const float* x, const float* y, const float* z, const float* m,
+                               const int32_t* leaf_to_internal, int32_t num_leaves, const uint32_t* layout,
+                               float* centers);
+int cs_upsweep_source_centers_f64(cs_stream_t stream, int num_levels, const int32_t* level_range_host,
+                                  const int32_t* child_offsets, const int32_t* parents, int32_t num_nodes,
+                                  double* centers, void* workspace, size_t workspace_bytes);
+int cs_upsweep_source_centers_f32(cs_stream_t stream, int num_levels, const int32_t* level_range_host,
+                                  const int32_t* child_offsets, const int32_t* parents, int32_t num_nodes,
+                                  float* centers, void* workspace, size_t workspace_bytes);
+
+/* ---- target groups ----------------------------------------------------------------------------------------------
+ * replaces computeGroupSplits(exec, first, last, x, y, z, h, leaves, numLeaves, layout, box, groupSize, tolFactor,
+ * numSplitsPerGroup, groups) (traversal/groups_gpu.h:63-78, traversal/groups_gpu.cu, groupSplitsKernel in
+ * traversal/groups_gpu.cuh): fixed groups of group_size (32 or 64) particles from `first`, cut after particle j where
+ * |X_{j+1} - X_j|^2 > min(distCrit^2, (2 h_j / minExtent)^2) in unit-box coordinates; distCrit = tol times the edge of
+ * the smallest leaf among the group's first 32 particles. h may be NULL. groups receives the group starts and `last`
+ * (num_groups + 1 entries); *num_groups is set (host) and CS_ERR_CAPACITY returned if groups_capacity is too small.
+ * Synchronises the stream, as the reference does. */
+size_t cs_group_splits_workspace_bytes(uint32_t num_particles, unsigned group_size);
+int cs_group_splits_f64(cs_stream_t stream, uint32_t first, uint32_t last, const double* x, const double* y,
+                        const double* z, const double* h, const uint64_t* leaves, int32_t num_leaves,
+                        const uint32_t* layout, const cs_box* box, unsigned group_size, float tol, uint32_t* groups,
+                        size_t groups_capacity, uint32_t* num_groups, void* workspace, size_t workspace_bytes);
+int cs_group_splits_f32(cs_stream_t stream, uint32_t first, uint32_t last, const float* x, const float* y,
+                        const float* z, const float* h, const uint64_t* leaves, int32_t num_leaves,
+                        const uint32_t* layout, const cs_box* box, unsigned group_size, float tol, uint32_t* groups,
+                        size_t groups_capacity, uint32_t* num_groups, void* workspace, size_t workspace_bytes);
+
+/* ---- SFC gaps and spanning trees ------------------------------------------------------------------------------
+ * cs_count_sfc_gaps / cs_fill_sfc_gaps replace countSfcGapsGpu / fillSfcGapsGpu (tree/csarray_gpu.h:73-82,
+ * tree/csarray_gpu.cu:238-270): node_ops[i] = spanSfcRange(tree[i], tree[i+1]) (sfc/common.hpp:422-460); after an
+ * exclusive scan of node_ops (num_nodes + 1 entries), the fill writes the keys of every interval and the last key.
+ * cs_spanning_tree replaces computeSpanningTree (tree/csarray.hpp:482-506): the smallest cornerstone leaf array that
+ * contains the given sorted keys (first 0, last nodeRange(0)); *out_size = its number of keys (host, synchronised). */
+int cs_count_sfc_gaps_u32(cs_stream_t stream, const uint32_t* tree, int32_t num_nodes, int32_t* node_ops);
+int cs_count_sfc_gaps_u64(cs_stream_t stream, const uint64_t* tree, int32_t num_nodes, int32_t* node_ops);
+int cs_fill_sfc_gaps_u32(cs_stream_t stream, const uint32_t* tree, int32_t num_nodes, const int32_t* node_ops,
+                         uint32_t* new_tree);
+int cs_fill_sfc_gaps_u64(cs_stream_t stream, const uint64_t* tree, int32_t num_nodes, const int32_t* node_ops,
+                         uint64_t* new_tree);
+size_t cs_spanning_tree_workspace_bytes(int32_t num_keys);
+int cs_spanning_tree_u32(cs_stream_t stream, const uint32_t* keys, int32_t num_keys, uint32_t* out, int32_t capacity,
+                         int32_t* out_size, void* workspace, size_t workspace_bytes);
+int cs_spanning_tree_u64(cs_stream_t stream, const uint64_t* keys, int32_t num_keys, uint64_t* out, int32_t capacity,
+                         int32_t* out_size, void* workspace, size_t workspace_bytes);
+
+/* ---- focus (locally essential) tree ---------------------------------------------------------------------------
+ * cs_rebalance_decision_essential replaces rebalanceDecisionEssentialGpu (focus/rebalance_gpu.h:21-33,
+ * mergeCountAndMacOp focus/rebalance.hpp:31-73): node_ops[i] in {0 merge, 1 keep, 8, 64, 512, 4096 split} per node.
+ * cs_mac_refine_decision replaces macRefineDecisionGpu (focus/rebalance_gpu.h:35-48): per leaf, 8 where the leaf's
+ * MAC fails outside [focus_first, focus_last), else 1. cs_protect_ancestors replaces protectAncestorsGpu
+ * (focus/rebalance_gpu.h:50-52, nzAncestorOp focus/rebalance.hpp:96-118), in place; changed_dev (one device int) counts
+ * the ops that differ from 1, *converged_host (if not NULL, synchronised) = that count is zero. cs_enforce_keys replaces
+ * enforceKeysGpu (focus/rebalance_gpu.h:54-61, enforceKeySingle focus/rebalance.hpp:183-236): keys processed in order;
+ * status 0 converged, 1 cancelMerge, 2 rebalance, 3 failed in status_dev (and *status_host, synchronised, if not
+ * NULL). cs_range_count replaces rangeCountGpu (focus/rebalance_gpu.h:63-70, focus/rebalance.hpp:263-286).
+ * cs_node_layout replaces computeNodeLayout (domain/layout.hpp:154-186): layout (num_leaves + 1) = exclusive scan of
+ * the counts of the leaves in [first, last) or flagged (flags indexed by node) through leaf_to_internal. */
+int cs_rebalance_decision_essential_u32(cs_stream_t stream, const uint32_t* prefixes, const int32_t* child_offsets,
+                                        const int32_t* parents, const uint32_t* counts, const uint8_t* macs,
+                                        uint32_t focus_start, uint32_t focus_end, unsigned bucket, int32_t* node_ops,
+                                        int32_t num_nodes);
+int cs_rebalance_decision_essential_u64(cs_stream_t stream, const uint64_t* prefixes, const int32_t* child_offsets,
+                                        const int32_t* parents, const uint32_t* counts, const uint8_t* macs,
+                                        uint64_t focus_start, uint64_t focus_end, unsigned bucket, int32_t* node_ops,
+                                        int32_t num_nodes);
+int cs_mac_refine_decision_u32(cs_stream_t stream, const uint32_t* prefixes, const uint8_t* macs,
+                               const int32_t* leaf_to_internal, int32_t num_leaves, int32_t focus_first,
+                               int32_t focus_last, int32_t* node_ops);
+int cs_mac_refine_decision_u64(cs_stream_t stream, const uint64_t* prefixes, const uint8_t* macs,
+                               const int32_t* leaf_to_internal, int32_t num_leaves, int32_t focus_first,
+                               int32_t focus_last, int32_t* node_ops);
+int cs_protect_ancestors_u32(cs_stream_t stream, const uint32_t* prefixes, const int32_t* parents, int32_t* node_ops,
+                             int32_t num_nodes, int* changed_dev, int* converged_host);
+int cs_protect_ancestors_u64(cs_stream_t stream, const uint64_t* prefixes, const int32_t* parents, int32_t* node_ops,
+                             int32_t num_nodes, int* changed_dev, int* converged_host);
+int cs_enforce_keys_u32(cs_stream_t stream, const uint32_t* forced_keys, int32_t num_forced, const uint32_t* prefixes,
+                        const int32_t* child_offsets, const int32_t* parents, int32_t* node_ops, int* status_dev,
+                        int* status_host);
+int cs_enforce_keys_u64(cs_stream_t stream, const uint64_t* forced_keys, int32_t num_forced, const uint64_t* prefixes,
+                        const int32_t* child_offsets, const int32_t* parents, int32_t* node_ops, int* status_dev,
+                        int* status_host);
+int cs_range_count_u32(cs_stream_t stream, const uint32_t* leaves, int32_t num_leaf_keys, const uint32_t* counts,
+                       const uint32_t* leaves_focus, const int32_t* focus_idx, int32_t num_idx,
+                       uint32_t* counts_focus);
+int cs_range_count_u64(cs_stream_t stream, const uint64_t* leaves, int32_t num_leaf_keys, const uint32_t* counts,
+                       const uint64_t* leaves_focus, const int32_t* focus_idx, int32_t num_idx,
+                       uint32_t* counts_focus);
+size_t cs_node_layout_workspace_bytes(int32_t num_leaves);
+int cs_node_layout(cs_stream_t stream, const uint32_t* focus_leaf_counts, int32_t num_leaves, const uint8_t* flags,
+                   const int32_t* leaf_to_internal, int32_t first, int32_t last, uint32_t* layout, void* workspace,
+                   size_t workspace_bytes);
+
 /* ---- whole path: keys -> sort -> gather -> computeOctree -> link -> geometry -> findHalos -> findNeighbors ---------
  * The single-rank inner part of the reference's Domain::sync + discoverHalos + neighbour search
  * (domain/assignment.hpp:105-120, focus/octree_focus_mpi.hpp:512-568, findneighbors.hpp:156-177), as one object that

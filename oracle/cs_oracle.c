@@ -757,3 +757,5 @@ int cso_num_threads(void)
     return 1;
 #endif
 }
+
+#include "cs_oracle_next.inc"

@@ -108,6 +108,46 @@ void cso_philox_uniform_f64(uint64_t seed, uint64_t stream, double* out, size_t 
 void cso_plummer_f64(uint64_t seed, double* x, double* y, double* z, size_t n, double rmax);
 int cso_num_threads(void);
 
+/* ---- around the path: upsweeps, source centres, groups, SFC gaps, focus rebalance (cs_oracle_next.inc) ---- */
+int32_t cso_span_sfc_range(uint64_t a, uint64_t b, uint64_t* out, int key_bits);
+int32_t cso_fill_sfc_gaps(const uint64_t* keys, int32_t num_nodes, uint64_t* out, int32_t cap, int key_bits);
+void cso_upsweep_sum(const int32_t* level_range, int num_levels, const int32_t* child_offsets, uint32_t* counts);
+void cso_leaf_mass_centers_f64(const double* x, const double* y, const double* z, const double* m,
+                               const int32_t* leaf_to_internal, int32_t num_leaves, const uint32_t* layout,
+                               double* centers);
+void cso_leaf_mass_centers_f64m32(const double* x, const double* y, const double* z, const float* m,
+                                  const int32_t* leaf_to_internal, int32_t num_leaves, const uint32_t* layout,
+                                  double* centers);
+void cso_leaf_mass_centers_f32(const float* x, const float* y, const float* z, const float* m,
+                               const int32_t* leaf_to_internal, int32_t num_leaves, const uint32_t* layout,
+                               float* centers);
+void cso_upsweep_centers_f64(const int32_t* level_range, int num_levels, const int32_t* child_offsets,
+                             double* centers);
+void cso_upsweep_centers_f32(const int32_t* level_range, int num_levels, const int32_t* child_offsets,
+                             float* centers);
+int32_t cso_group_splits_f64(uint32_t first, uint32_t last, const double* x, const double* y, const double* z,
+                             const double* h, const uint64_t* leaves, int32_t num_leaves, const uint32_t* layout,
+                             const double* box_lo, const double* box_hi, unsigned group_size, float tol,
+                             uint32_t* groups, int32_t cap, int key_bits);
+int32_t cso_group_splits_f32(uint32_t first, uint32_t last, const float* x, const float* y, const float* z,
+                             const float* h, const uint64_t* leaves, int32_t num_leaves, const uint32_t* layout,
+                             const double* box_lo, const double* box_hi, unsigned group_size, float tol,
+                             uint32_t* groups, int32_t cap, int key_bits);
+void cso_rebalance_decision_essential(const uint64_t* prefixes, const int32_t* child_offsets, const int32_t* parents,
+                                      const uint32_t* counts, const uint8_t* macs, int32_t num_nodes,
+                                      uint64_t focus_start, uint64_t focus_end, unsigned bucket, int32_t* ops,
+                                      int key_bits);
+void cso_mac_refine_decision(const uint64_t* prefixes, const uint8_t* macs, const int32_t* l2i, int32_t num_leaves,
+                             int32_t focus_first, int32_t focus_last, int32_t* ops, int key_bits);
+int cso_protect_ancestors(const uint64_t* prefixes, const int32_t* parents, int32_t* ops, int32_t num_nodes,
+                          int key_bits);
+int cso_enforce_keys(const uint64_t* keys, int32_t n_keys, const uint64_t* prefixes, const int32_t* child_offsets,
+                     const int32_t* parents, int32_t* ops, int key_bits);
+void cso_range_count(const uint64_t* leaves, int32_t n_leaf_keys, const uint32_t* counts, const uint64_t* leaves_focus,
+                     const int32_t* focus_idx, int32_t n_idx, uint32_t* counts_focus);
+void cso_node_layout(const uint32_t* focus_leaf_counts, int32_t num_leaves, const uint8_t* flags, const int32_t* l2i,
+                     int32_t first, int32_t last, uint32_t* layout);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,7 +31,8 @@ def make_box(lo, hi, boundary=(0, 0, 0)):
 
 def build(force=False):
     """Compile the restatement with the committed Makefile (gcc, OpenMP)."""
-    if force or not os.path.exists(LIB_PATH) or _stale(LIB_PATH, ["cs_oracle.c", "cs_oracle_real.inc", "cs_oracle.h"]):
+    if force or not os.path.exists(LIB_PATH) or _stale(LIB_PATH, ["cs_oracle.c", "cs_oracle_real.inc",
+                                                                  "cs_oracle_next.inc", "cs_oracle.h"]):
         subprocess.check_call(["make", "-s", "-C", HERE, "libcsoracle.so"])
 
 
@@ -70,6 +71,10 @@ def lib():
         _lib.cso_compute_octree.restype = C.c_int32
         _lib.cso_binary_key_weight.restype = C.c_int32
         _lib.cso_num_threads.restype = C.c_int
+        for name in ("cso_span_sfc_range", "cso_fill_sfc_gaps", "cso_group_splits_f64", "cso_group_splits_f32"):
+            getattr(_lib, name).restype = C.c_int32
+        _lib.cso_protect_ancestors.restype = C.c_int
+        _lib.cso_enforce_keys.restype = C.c_int
     return _lib
 
 
@@ -86,6 +91,10 @@ def ref():
         _ref.csr_compute_octree.restype = C.c_int32
         _ref.csr_update_octree.restype = C.c_int
         _ref.csr_binary_key_weight.restype = C.c_int32
+        _ref.csr_spanning_tree.restype = C.c_int32
+        _ref.csr_mac_refine_op.restype = C.c_int
+        _ref.csr_protect_ancestors.restype = C.c_int
+        _ref.csr_enforce_keys.restype = C.c_int
     return _ref
 
 
@@ -538,3 +547,158 @@ def timed_pipeline(x, y, z, h, box, bucket, ngmax, focus=(0, 0), kind=HILBERT, k
              halos=c7 - c6, neighbors=c8 - c7, total=c8 - c0)
     return t, dict(sorted_keys=skeys, perm=perm, leaves=leaves, counts=counts, iterations=iters, tree=tree,
                    centers=centers, sizes=sizes, flags=flags, nb=nb, nc=nc)
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# around the path: upsweeps, source centres, groups, SFC gaps, focus rebalance (cs_oracle_next.inc) and the
+# reference's own versions (csr_*) where it has CPU code
+# ---------------------------------------------------------------------------------------------------------------
+
+def span_sfc_range(a, b, key_bits=64):
+    n = lib().cso_span_sfc_range(C.c_uint64(a), C.c_uint64(b), None, key_bits)
+    out = np.zeros(max(n, 1), np.uint64)
+    lib().cso_span_sfc_range(C.c_uint64(a), C.c_uint64(b), _p(out), key_bits)
+    return out[:n]
+
+
+def fill_sfc_gaps(keys, key_bits=64):
+    keys = np.ascontiguousarray(keys, np.uint64)
+    cap = 64
+    while True:
+        out = np.zeros(cap, np.uint64)
+        r = lib().cso_fill_sfc_gaps(_p(keys), keys.size - 1, _p(out), cap, key_bits)
+        if r > 0:
+            return out[:r]
+        cap = -r
+
+
+def ref_spanning_tree(keys, key_bits=64):
+    keys = np.ascontiguousarray(keys, np.uint64)
+    cap = 64
+    while True:
+        out = np.zeros(cap, np.uint64)
+        r = ref().csr_spanning_tree(_p(keys), keys.size, _p(out), cap, key_bits)
+        if r > 0:
+            return out[:r]
+        cap = -r
+
+
+def upsweep_sum(level_range, child_offsets, counts, use_ref=False):
+    lr = np.ascontiguousarray(level_range, np.int32)
+    c = np.ascontiguousarray(counts, np.uint32).copy()
+    fn = ref().csr_upsweep_sum if use_ref else lib().cso_upsweep_sum
+    fn(_p(lr), lr.size - 1, _p(np.ascontiguousarray(child_offsets, np.int32)), _p(c))
+    return c
+
+
+def leaf_mass_centers(x, y, z, m, leaf_to_internal, layout, num_nodes, use_ref=False):
+    dt = np.float64 if x.dtype == np.float64 else np.float32
+    cen = np.zeros((num_nodes, 4), dt)
+    l2i = np.ascontiguousarray(leaf_to_internal, np.int32)
+    lay = np.ascontiguousarray(layout, np.uint32)
+    if use_ref:
+        fn = ref().csr_leaf_mass_centers_f64 if dt == np.float64 else ref().csr_leaf_mass_centers_f32
+        fn(_p(x), _p(y), _p(z), _p(m), _p(l2i), l2i.size, _p(lay), _p(cen), C.c_size_t(x.size))
+    else:
+        if dt == np.float64:
+            fn = lib().cso_leaf_mass_centers_f64 if m.dtype == np.float64 else lib().cso_leaf_mass_centers_f64m32
+        else:
+            fn = lib().cso_leaf_mass_centers_f32
+        fn(_p(x), _p(y), _p(z), _p(m), _p(l2i), l2i.size, _p(lay), _p(cen))
+    return cen
+
+
+def upsweep_centers(level_range, child_offsets, centers, use_ref=False):
+    lr = np.ascontiguousarray(level_range, np.int32)
+    c = np.ascontiguousarray(centers).copy()
+    if use_ref:
+        fn = ref().csr_upsweep_centers_f64 if c.dtype == np.float64 else ref().csr_upsweep_centers_f32
+    else:
+        fn = lib().cso_upsweep_centers_f64 if c.dtype == np.float64 else lib().cso_upsweep_centers_f32
+    fn(_p(lr), lr.size - 1, _p(np.ascontiguousarray(child_offsets, np.int32)), _p(c))
+    return c
+
+
+def group_splits(first, last, x, y, z, h, leaves, layout, lo, hi, group_size, tol, key_bits=64):
+    dt = x.dtype
+    fn = lib().cso_group_splits_f64 if dt == np.float64 else lib().cso_group_splits_f32
+    lo = np.array(lo, np.float64)
+    hi = np.array(hi, np.float64)
+    leaves = np.ascontiguousarray(leaves, np.uint64)
+    lay = np.ascontiguousarray(layout, np.uint32)
+    cap = 2 * ((last - first) // max(1, group_size) + 2)
+    while True:
+        g = np.zeros(cap, np.uint32)
+        r = fn(C.c_uint32(first), C.c_uint32(last), _p(x), _p(y), _p(z), _p(h), _p(leaves), leaves.size - 1, _p(lay),
+               _p(lo), _p(hi), C.c_uint(group_size), C.c_float(tol), _p(g), cap, key_bits)
+        if r >= 0:
+            return g[: r + 1]
+        cap = -r + 1
+
+
+def rebalance_decision_essential(prefixes, child_offsets, parents, counts, macs, focus, bucket, key_bits=64,
+                                 use_ref=False):
+    N = prefixes.size
+    ops = np.zeros(N, np.int32)
+    args = [_p(np.ascontiguousarray(prefixes, np.uint64)), _p(np.ascontiguousarray(child_offsets, np.int32)),
+            _p(np.ascontiguousarray(parents, np.int32)), _p(np.ascontiguousarray(counts, np.uint32)),
+            _p(np.ascontiguousarray(macs, np.uint8)), N, C.c_uint64(focus[0]), C.c_uint64(focus[1]),
+            C.c_uint(bucket), _p(ops), key_bits]
+    (ref().csr_rebalance_decision_essential if use_ref else lib().cso_rebalance_decision_essential)(*args)
+    return ops
+
+
+def mac_refine_decision(prefixes, macs, l2i, focus_first, focus_last, key_bits=64):
+    L = l2i.size
+    ops = np.zeros(L, np.int32)
+    lib().cso_mac_refine_decision(_p(np.ascontiguousarray(prefixes, np.uint64)),
+                                  _p(np.ascontiguousarray(macs, np.uint8)), _p(np.ascontiguousarray(l2i, np.int32)),
+                                  L, focus_first, focus_last, _p(ops), key_bits)
+    return ops
+
+
+def protect_ancestors(prefixes, parents, ops, key_bits=64, use_ref=False):
+    o = np.ascontiguousarray(ops, np.int32).copy()
+    pre = np.ascontiguousarray(prefixes, np.uint64)
+    par = np.ascontiguousarray(parents, np.int32)
+    fn = ref().csr_protect_ancestors if use_ref else lib().cso_protect_ancestors
+    conv = fn(_p(pre), _p(par), _p(o), pre.size, key_bits)
+    return o, bool(conv)
+
+
+def enforce_keys(keys, prefixes, child_offsets, parents, ops, key_bits=64, use_ref=False):
+    o = np.ascontiguousarray(ops, np.int32).copy()
+    k = np.ascontiguousarray(keys, np.uint64)
+    pre = np.ascontiguousarray(prefixes, np.uint64)
+    co = np.ascontiguousarray(child_offsets, np.int32)
+    par = np.ascontiguousarray(parents, np.int32)
+    if use_ref:
+        st = ref().csr_enforce_keys(_p(k), k.size, _p(pre), pre.size, _p(co), _p(par), _p(o), key_bits)
+    else:
+        st = lib().cso_enforce_keys(_p(k), k.size, _p(pre), _p(co), _p(par), _p(o), key_bits)
+    return o, int(st)
+
+
+def range_count(leaves, counts, leaves_focus, focus_idx, key_bits=64, use_ref=False):
+    lv = np.ascontiguousarray(leaves, np.uint64)
+    lf = np.ascontiguousarray(leaves_focus, np.uint64)
+    idx = np.ascontiguousarray(focus_idx, np.int32)
+    out = np.zeros(lf.size - 1, np.uint32)
+    cnt = np.ascontiguousarray(counts, np.uint32)
+    if use_ref:
+        ref().csr_range_count(_p(lv), lv.size, _p(cnt), _p(lf), lf.size, _p(idx), idx.size, _p(out), key_bits)
+    else:
+        lib().cso_range_count(_p(lv), lv.size, _p(cnt), _p(lf), _p(idx), idx.size, _p(out))
+    return out
+
+
+def node_layout(focus_leaf_counts, flags, l2i, first, last, use_ref=False):
+    c = np.ascontiguousarray(focus_leaf_counts, np.uint32)
+    f = np.ascontiguousarray(flags, np.uint8)
+    l2 = np.ascontiguousarray(l2i, np.int32)
+    out = np.zeros(c.size + 1, np.uint32)
+    if use_ref:
+        ref().csr_node_layout(_p(c), c.size, _p(f), f.size, _p(l2), first, last, _p(out))
+    else:
+        lib().cso_node_layout(_p(c), c.size, _p(f), _p(l2), first, last, _p(out))
+    return out

@@ -10,7 +10,9 @@
 #include <span>
 #include <vector>
 
+#include "cstone/domain/layout.hpp"
 #include "cstone/findneighbors.hpp"
+#include "cstone/focus/rebalance.hpp"
 #include "cstone/focus/source_center.hpp"
 #include "cstone/sfc/sfc.hpp"
 #include "cstone/traversal/collisions.hpp"
@@ -343,5 +345,140 @@ extern "C"
         auto box = makeBox<float>(lo, hi, bnd);
         findNeighborsImpl<uint64_t, float>(x, y, z, h, first, last, box, numLeaves, numNodes, childOffsets, parents,
                                            i2l, layout, centers, sizes, ext, ngmax, nb, nc);
+    }
+}
+
+// ---- around the path: upsweeps, source centres, SFC gaps, focus rebalance ----
+namespace
+{
+template<class K>
+int32_t spanningTreeImpl(const uint64_t* keys64, int32_t nKeys, uint64_t* out, int32_t cap)
+{
+    auto keys = narrow<K>(keys64, size_t(nKeys));
+    auto t    = computeSpanningTree<K>(std::span<const K>(keys));
+    if (int32_t(t.size()) > cap) return -int32_t(t.size());
+    for (size_t i = 0; i < t.size(); ++i)
+        out[i] = t[i];
+    return int32_t(t.size());
+}
+
+template<class K>
+void essentialImpl(const uint64_t* prefixes64, const int32_t* childOffsets, const int32_t* parents,
+                   const uint32_t* counts, const uint8_t* macs, int32_t numNodes, uint64_t f0, uint64_t f1,
+                   unsigned bucket, int32_t* ops)
+{
+    auto prefixes = narrow<K>(prefixes64, size_t(numNodes));
+    rebalanceDecisionEssential<K>(std::span<const K>(prefixes), childOffsets, parents, counts, macs, K(f0), K(f1),
+                                  bucket, ops);
+}
+
+template<class K>
+int protectImpl(const uint64_t* prefixes64, const int32_t* parents, int32_t* ops, int32_t numNodes)
+{
+    auto prefixes = narrow<K>(prefixes64, size_t(numNodes));
+    return protectAncestors<K>(std::span<const K>(prefixes), parents, ops) ? 1 : 0;
+}
+
+template<class K>
+int enforceImpl(const uint64_t* keys64, int32_t nKeys, const uint64_t* prefixes64, int32_t numNodes,
+                const int32_t* childOffsets, const int32_t* parents, int32_t* ops)
+{
+    auto keys     = narrow<K>(keys64, size_t(nKeys));
+    auto prefixes = narrow<K>(prefixes64, size_t(numNodes));
+    return int(enforceKeys<K>(std::span<const K>(keys), prefixes.data(), childOffsets, parents, ops));
+}
+
+template<class K>
+void rangeCountImpl(const uint64_t* leaves64, int32_t nLeafKeys, const uint32_t* counts, const uint64_t* focus64,
+                    int32_t nFocusKeys, const int32_t* idx, int32_t nIdx, uint32_t* countsFocus)
+{
+    auto leaves = narrow<K>(leaves64, size_t(nLeafKeys));
+    auto focus  = narrow<K>(focus64, size_t(nFocusKeys));
+    rangeCount<K>(std::span<const K>(leaves), std::span<const unsigned>(counts, size_t(nLeafKeys - 1)),
+                  std::span<const K>(focus), std::span<const TreeNodeIndex>(idx, size_t(nIdx)),
+                  std::span<unsigned>(countsFocus, size_t(nFocusKeys - 1)));
+}
+} // namespace
+
+extern "C"
+{
+    int32_t csr_spanning_tree(const uint64_t* keys, int32_t nKeys, uint64_t* out, int32_t cap, int bits)
+    {
+        return bits == 64 ? spanningTreeImpl<uint64_t>(keys, nKeys, out, cap)
+                          : spanningTreeImpl<unsigned>(keys, nKeys, out, cap);
+    }
+    void csr_upsweep_sum(const int32_t* levelRange, int numLevels, const int32_t* childOffsets, uint32_t* counts)
+    {
+        std::vector<TreeNodeIndex> lr(levelRange, levelRange + numLevels + 1);
+        upsweep(std::span<const TreeNodeIndex>(lr), childOffsets, counts, NodeCount<unsigned>{});
+    }
+    void csr_leaf_mass_centers_f64(const double* x, const double* y, const double* z, const double* m,
+                                   const int32_t* l2i, int32_t numLeaves, const uint32_t* layout, double* centers,
+                                   size_t n)
+    {
+        computeLeafMassCenter<double, double, double>(
+            std::span<const double>(x, n), std::span<const double>(y, n), std::span<const double>(z, n),
+            std::span<const double>(m, n), std::span<const TreeNodeIndex>(l2i, size_t(numLeaves)), layout,
+            reinterpret_cast<SourceCenterType<double>*>(centers));
+    }
+    void csr_leaf_mass_centers_f32(const float* x, const float* y, const float* z, const float* m, const int32_t* l2i,
+                                   int32_t numLeaves, const uint32_t* layout, float* centers, size_t n)
+    {
+        computeLeafMassCenter<float, float, float>(
+            std::span<const float>(x, n), std::span<const float>(y, n), std::span<const float>(z, n),
+            std::span<const float>(m, n), std::span<const TreeNodeIndex>(l2i, size_t(numLeaves)), layout,
+            reinterpret_cast<SourceCenterType<float>*>(centers));
+    }
+    void csr_upsweep_centers_f64(const int32_t* levelRange, int numLevels, const int32_t* childOffsets,
+                                 double* centers)
+    {
+        std::vector<TreeNodeIndex> lr(levelRange, levelRange + numLevels + 1);
+        upsweep(std::span<const TreeNodeIndex>(lr), childOffsets, reinterpret_cast<SourceCenterType<double>*>(centers),
+                CombineSourceCenter<double>{});
+    }
+    void csr_upsweep_centers_f32(const int32_t* levelRange, int numLevels, const int32_t* childOffsets,
+                                 float* centers)
+    {
+        std::vector<TreeNodeIndex> lr(levelRange, levelRange + numLevels + 1);
+        upsweep(std::span<const TreeNodeIndex>(lr), childOffsets, reinterpret_cast<SourceCenterType<float>*>(centers),
+                CombineSourceCenter<float>{});
+    }
+    void csr_rebalance_decision_essential(const uint64_t* prefixes, const int32_t* childOffsets,
+                                          const int32_t* parents, const uint32_t* counts, const uint8_t* macs,
+                                          int32_t numNodes, uint64_t f0, uint64_t f1, unsigned bucket, int32_t* ops,
+                                          int bits)
+    {
+        if (bits == 64) essentialImpl<uint64_t>(prefixes, childOffsets, parents, counts, macs, numNodes, f0, f1, bucket, ops);
+        else essentialImpl<unsigned>(prefixes, childOffsets, parents, counts, macs, numNodes, f0, f1, bucket, ops);
+    }
+    int csr_mac_refine_op(uint64_t prefix, int mac, int bits)
+    {
+        return bits == 64 ? macRefineOp<uint64_t>(prefix, char(mac)) : macRefineOp<unsigned>(unsigned(prefix), char(mac));
+    }
+    int csr_protect_ancestors(const uint64_t* prefixes, const int32_t* parents, int32_t* ops, int32_t numNodes,
+                              int bits)
+    {
+        return bits == 64 ? protectImpl<uint64_t>(prefixes, parents, ops, numNodes)
+                          : protectImpl<unsigned>(prefixes, parents, ops, numNodes);
+    }
+    int csr_enforce_keys(const uint64_t* keys, int32_t nKeys, const uint64_t* prefixes, int32_t numNodes,
+                         const int32_t* childOffsets, const int32_t* parents, int32_t* ops, int bits)
+    {
+        return bits == 64 ? enforceImpl<uint64_t>(keys, nKeys, prefixes, numNodes, childOffsets, parents, ops)
+                          : enforceImpl<unsigned>(keys, nKeys, prefixes, numNodes, childOffsets, parents, ops);
+    }
+    void csr_range_count(const uint64_t* leaves, int32_t nLeafKeys, const uint32_t* counts, const uint64_t* focus,
+                         int32_t nFocusKeys, const int32_t* idx, int32_t nIdx, uint32_t* countsFocus, int bits)
+    {
+        if (bits == 64) rangeCountImpl<uint64_t>(leaves, nLeafKeys, counts, focus, nFocusKeys, idx, nIdx, countsFocus);
+        else rangeCountImpl<unsigned>(leaves, nLeafKeys, counts, focus, nFocusKeys, idx, nIdx, countsFocus);
+    }
+    void csr_node_layout(const uint32_t* counts, int32_t numLeaves, const uint8_t* flags, int32_t numNodes,
+                         const int32_t* l2i, int32_t first, int32_t last, uint32_t* layout)
+    {
+        computeNodeLayout(execution::Cpu{}, std::span<const unsigned>(counts, size_t(numLeaves)),
+                          std::span<const uint8_t>(flags, size_t(numNodes)),
+                          std::span<const TreeNodeIndex>(l2i, size_t(numLeaves)), TreeIndexPair(first, last),
+                          std::span<LocalIndex>(layout, size_t(numLeaves) + 1));
     }
 }
