@@ -1,0 +1,466 @@
+// Neighbour-list consumers (the reference's ijLoop neighbourhoods, traversal/ijloop/).
+//
+// Two ways to loop over neighbours, both evaluated with a fixed interaction here (an SPH density sum, the
+// interaction the tests and the benchmark use); the C++ header include/cstone_gb300/ijloop_gb300.cuh runs any
+// interaction functor over the same cluster lists.
+//
+// 1. Over stored neighbour lists (CpuFullNbListNeighborhood::jLoop, traversal/ijloop/cpu_fullnblist.hpp:94-112):
+//    one thread per target walks its ngmax-strided row in order. Results equal the CPU full list bit for bit.
+//
+// 2. Over cluster-pair lists (the role of the reference's supercluster lists, traversal/ijloop/
+//    gpu_superclusternblist.cuh and gpu_superclusternblist/{build,loop}.cuh, built differently here). Particles are
+//    cut into clusters of 8 consecutive (SFC-ordered) particles. For each i-cluster a warp walks the octree with the
+//    cluster's search box (the union of its particles' 2h boxes, rounded outwards to float and widened by one finest
+//    cell, which covers particles that lie slightly outside their leaf's box) and lists, in ascending order and
+//    without repeats, every j-cluster whose float bounding box meets it; capacity ncmax j-clusters per i-cluster.
+//    The loop then runs 4 i-clusters per warp, one target per lane: each j-cluster's 8 particles are loaded by the 8
+//    lanes of the segment and broadcast with shuffles, so every target adds its neighbours in ascending j. The list is
+//    a superset of the neighbours of every target, so the sum equals the brute-force sum over all j with
+//    d2 < (2 h_i)^2, in ascending j, bit for bit. Open boxes only (no periodic images).
+//
+// Interaction: contribution m_j w(q), q = sqrt(d2) hinv_i, w = (1 - 1.5 q^2) + (0.75 q^2) q for q < 1, else
+// 0.25 (2 - q)^3 evaluated as 0.25 ((t t) t); the sum starts with i's own contribution (w(0) = 1, as the reference's
+// loops start from interaction(i, i)); rho_i = sum * hinv^3. Round-to-nearest intrinsics, no contraction.
+#include "cs_common.cuh"
+
+#include <type_traits>
+#include <vector>
+
+namespace csg
+{
+
+constexpr int CLUSTER = 8;
+
+template<class T>
+__device__ __forceinline__ T sqrtRn(T a)
+{
+    if constexpr (std::is_same_v<T, double>) return __dsqrt_rn(a);
+    else return __fsqrt_rn(a);
+}
+
+template<class T>
+__device__ __forceinline__ T divRn(T a, T b)
+{
+    if constexpr (std::is_same_v<T, double>) return __ddiv_rn(a, b);
+    else return __fdiv_rn(a, b);
+}
+
+template<class T>
+__device__ __forceinline__ T densityW(T d2, T hinv)
+{
+    using R = RN<T>;
+    T q  = R::mul(sqrtRn<T>(d2), hinv);
+    T q2 = R::mul(q, q);
+    if (q < T(1)) return R::add(R::sub(T(1), R::mul(T(1.5), q2)), R::mul(R::mul(T(0.75), q2), q));
+    T t = R::sub(T(2), q);
+    return R::mul(T(0.25), R::mul(R::mul(t, t), t));
+}
+
+template<class T>
+__device__ __forceinline__ T foldRn(T d, int pbc, T len, T ilen)
+{
+    return RN<T>::sub(d, RN<T>::mul(RN<T>::mul(T(pbc), len), RN<T>::rint_(RN<T>::mul(d, ilen))));
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// 1. stored neighbour lists
+// ---------------------------------------------------------------------------------------------------------------
+template<class T>
+__global__ void densityListKernel(const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z,
+                                  const T* __restrict__ h, const T* __restrict__ m, uint32_t first, uint32_t last,
+                                  BoxParams<T> b, int anyPbc, const uint32_t* __restrict__ nb,
+                                  const uint32_t* __restrict__ nc, unsigned ngmax, T* __restrict__ rho)
+{
+    using R          = RN<T>;
+    const uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= last) return;
+    const T xi = x[i], yi = y[i], zi = z[i], hi = h[i];
+    const T hinv = divRn<T>(T(1), hi);
+    const T r2   = R::mul(R::mul(T(4), hi), hi);
+    bool pbc     = false;
+    if (anyPbc)
+    {
+        T r2h       = R::mul(T(2), hi);
+        bool inside = R::sub(xi, r2h) >= b.lo[0] && R::sub(yi, r2h) >= b.lo[1] && R::sub(zi, r2h) >= b.lo[2] &&
+                      R::add(xi, r2h) <= b.hi[0] && R::add(yi, r2h) <= b.hi[1] && R::add(zi, r2h) <= b.hi[2];
+        pbc = !inside;
+    }
+    T sum              = R::mul(m[i], densityW<T>(T(0), hinv));
+    const unsigned cnt = min(nc[i - first], ngmax);
+    const uint32_t* row = nb + size_t(i - first) * ngmax;
+    for (unsigned k = 0; k < cnt; ++k)
+    {
+        uint32_t j = __ldg(row + k);
+        T dx = R::sub(xi, __ldg(x + j)), dy = R::sub(yi, __ldg(y + j)), dz = R::sub(zi, __ldg(z + j));
+        if (pbc)
+        {
+            dx = foldRn<T>(dx, b.pbc[0], b.len[0], b.ilen[0]);
+            dy = foldRn<T>(dy, b.pbc[1], b.len[1], b.ilen[1]);
+            dz = foldRn<T>(dz, b.pbc[2], b.len[2], b.ilen[2]);
+        }
+        T d2 = R::add(R::add(R::mul(dx, dx), R::mul(dy, dy)), R::mul(dz, dz));
+        if (d2 < r2) sum = R::add(sum, R::mul(__ldg(m + j), densityW<T>(d2, hinv)));
+    }
+    rho[i - first] = R::mul(sum, R::mul(R::mul(hinv, hinv), hinv));
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// 2. cluster-pair lists
+// ---------------------------------------------------------------------------------------------------------------
+template<class T>
+__device__ __forceinline__ float toFloatRd(T v)
+{
+    if constexpr (std::is_same_v<T, double>) return __double2float_rd(v);
+    else return v;
+}
+template<class T>
+__device__ __forceinline__ float toFloatRu(T v)
+{
+    if constexpr (std::is_same_v<T, double>) return __double2float_ru(v);
+    else return v;
+}
+
+// float bounding box (rounded outwards) of each cluster of 8 consecutive particles: lo xyz, hi xyz
+template<class T>
+__global__ void jClusterBoxKernel(const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z, size_t n,
+                                  size_t numClusters, float4* __restrict__ boxes)
+{
+    size_t c = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (c >= numClusters) return;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t j = c * CLUSTER; j < min(n, c * CLUSTER + CLUSTER); ++j)
+    {
+        T p[3] = {x[j], y[j], z[j]};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            lo[k] = fminf(lo[k], toFloatRd<T>(p[k]));
+            hi[k] = fmaxf(hi[k], toFloatRu<T>(p[k]));
+        }
+    }
+    boxes[2 * c]     = make_float4(lo[0], lo[1], lo[2], 0.f);
+    boxes[2 * c + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+}
+
+constexpr int CB_WARPS = 4;
+constexpr int CB_STACK = 192;
+
+template<class T>
+struct ClusterBuildArgs
+{
+    const T *x, *y, *z, *h;
+    size_t n, numIClusters;
+    const int32_t* childOffsets;
+    const int32_t* internalToLeaf;
+    const uint32_t* layout;
+    const T *centers, *sizes;
+    const float4* jBoxes;
+    float margin[3];
+    unsigned ncmax;
+    uint32_t* lists;
+    uint32_t* counts;
+    uint32_t* err; // bit 0: a list overflowed ncmax; bit 1: traversal stack overflow
+};
+
+template<class T>
+__global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuildArgs<T> a)
+{
+    __shared__ int sStack[CB_WARPS][CB_STACK];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t ic = size_t(blockIdx.x) * CB_WARPS + warp;
+    if (ic >= a.numIClusters) return;
+
+    // the cluster's search box: union over its particles of [x - 2h, x + 2h], rounded outwards, plus the margin
+    float blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    const size_t i = ic * CLUSTER + lane;
+    if (lane < CLUSTER && i < a.n)
+    {
+        T p[3]  = {a.x[i], a.y[i], a.z[i]};
+        float r = toFloatRu<T>(RN<T>::mul(T(2), a.h[i]));
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            blo[k] = __fsub_rd(toFloatRd<T>(p[k]), r);
+            bhi[k] = __fadd_ru(toFloatRu<T>(p[k]), r);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            blo[k] = fminf(blo[k], __shfl_xor_sync(0xffffffffu, blo[k], o));
+            bhi[k] = fmaxf(bhi[k], __shfl_xor_sync(0xffffffffu, bhi[k], o));
+        }
+        blo[k] = __fsub_rd(blo[k], a.margin[k]);
+        bhi[k] = __fadd_ru(bhi[k], a.margin[k]);
+    }
+
+    auto nodeMeets = [&](int node) {
+        bool meet = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            T c      = a.centers[3 * size_t(node) + k];
+            T s      = a.sizes[3 * size_t(node) + k];
+            float lo = __fsub_rd(__fsub_rd(toFloatRd<T>(c), toFloatRu<T>(s)), a.margin[k]);
+            float hi = __fadd_ru(__fadd_ru(toFloatRu<T>(c), toFloatRu<T>(s)), a.margin[k]);
+            meet     = meet && lo <= bhi[k] && blo[k] <= hi;
+        }
+        return meet;
+    };
+
+    uint32_t* list = a.lists + ic * size_t(a.ncmax);
+    unsigned count = 0;
+    long long lastJ = -1;
+    int* stack      = sStack[warp];
+    int top         = 0;
+    if (nodeMeets(0))
+    {
+        if (lane == 0) stack[0] = 0;
+        top = 1;
+    }
+    __syncwarp();
+    while (top > 0)
+    {
+        const int node = stack[top - 1];
+        --top;
+        const int c0 = a.childOffsets[node];
+        if (c0 == 0)
+        {
+            // a leaf: its particles' j-clusters, tested 32 at a time, appended in ascending order without repeats
+            const int leaf     = a.internalToLeaf[node];
+            const uint32_t pf  = a.layout[leaf], pl = a.layout[leaf + 1];
+            if (pl > pf)
+            {
+                const long long J0 = pf / CLUSTER, J1 = (pl - 1) / CLUSTER;
+                for (long long Jb = J0; Jb <= J1; Jb += 32)
+                {
+                    const long long J = Jb + lane;
+                    bool hit          = false;
+                    if (J <= J1 && J != lastJ)
+                    {
+                        float4 lo = a.jBoxes[2 * J], hi = a.jBoxes[2 * J + 1];
+                        hit = lo.x <= bhi[0] && blo[0] <= hi.x && lo.y <= bhi[1] && blo[1] <= hi.y &&
+                              lo.z <= bhi[2] && blo[2] <= hi.z;
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, hit);
+                    if (hit)
+                    {
+                        unsigned pos = count + __popc(m & ((1u << lane) - 1u));
+                        if (pos < a.ncmax) list[pos] = uint32_t(J);
+                    }
+                    count += __popc(m);
+                    if (m) lastJ = Jb + 31 - __clz(m);
+                }
+            }
+            continue;
+        }
+        // an internal node: lanes 0-7 test the children; accepted ones pushed highest first
+        bool ok          = lane < 8 && nodeMeets(c0 + lane);
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        __syncwarp();
+        if (top + 8 > CB_STACK)
+        {
+            if (lane == 0) atomicOr(a.err, 2u);
+            break;
+        }
+        if (ok) stack[top + __popc(m >> (lane + 1))] = c0 + lane;
+        top += __popc(m);
+        __syncwarp();
+    }
+    if (lane == 0)
+    {
+        a.counts[ic] = count;
+        if (count > a.ncmax) atomicOr(a.err, 1u);
+    }
+}
+
+// 4 i-clusters per warp, one target per lane; each j-cluster's particles broadcast within the 8-lane segment
+template<class T>
+__global__ void __launch_bounds__(128) densityClusterKernel(const T* __restrict__ x, const T* __restrict__ y,
+                                                            const T* __restrict__ z, const T* __restrict__ h,
+                                                            const T* __restrict__ m, size_t n, size_t numIClusters,
+                                                            const uint32_t* __restrict__ lists,
+                                                            const uint32_t* __restrict__ counts, unsigned ncmax,
+                                                            T* __restrict__ rho)
+{
+    using R          = RN<T>;
+    const int lane   = threadIdx.x & 31;
+    const size_t gw  = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const size_t ic  = gw * 4 + (lane >> 3);
+    const int k      = lane & 7;
+    const int seg0   = lane & ~7;
+    const size_t i   = ic * CLUSTER + k;
+    const bool activeI = ic < numIClusters && i < n;
+    const size_t iSafe = activeI ? i : 0;
+    const T xi = x[iSafe], yi = y[iSafe], zi = z[iSafe], hi = h[iSafe];
+    const T hinv = divRn<T>(T(1), hi);
+    const T r2   = R::mul(R::mul(T(4), hi), hi);
+    T sum        = R::mul(m[iSafe], densityW<T>(T(0), hinv));
+    const unsigned cnt = ic < numIClusters ? min(counts[ic], ncmax) : 0u;
+    const unsigned maxCnt = __reduce_max_sync(0xffffffffu, cnt);
+    const uint32_t* list  = lists + (ic < numIClusters ? ic : 0) * size_t(ncmax);
+    for (unsigned t = 0; t < maxCnt; ++t)
+    {
+        const bool segOn = t < cnt;
+        const size_t J   = segOn ? __ldg(list + t) : 0;
+        const size_t jk  = J * CLUSTER + k;
+        const bool jOk   = segOn && jk < n;
+        T xj = jOk ? x[jk] : T(0), yj = jOk ? y[jk] : T(0), zj = jOk ? z[jk] : T(0), mj = jOk ? m[jk] : T(0);
+#pragma unroll
+        for (int q = 0; q < CLUSTER; ++q)
+        {
+            T xq = __shfl_sync(0xffffffffu, xj, seg0 + q);
+            T yq = __shfl_sync(0xffffffffu, yj, seg0 + q);
+            T zq = __shfl_sync(0xffffffffu, zj, seg0 + q);
+            T mq = __shfl_sync(0xffffffffu, mj, seg0 + q);
+            const size_t j = J * CLUSTER + q;
+            if (activeI && segOn && j < n && j != i)
+            {
+                T dx = R::sub(xi, xq), dy = R::sub(yi, yq), dz = R::sub(zi, zq);
+                T d2 = R::add(R::add(R::mul(dx, dx), R::mul(dy, dy)), R::mul(dz, dz));
+                if (d2 < r2) sum = R::add(sum, R::mul(mq, densityW<T>(d2, hinv)));
+            }
+        }
+    }
+    if (activeI) rho[i] = R::mul(sum, R::mul(R::mul(hinv, hinv), hinv));
+}
+
+} // namespace csg
+
+using namespace csg;
+
+#define CS_IJLOOP_ENTRIES(SUF, T)                                                                                      \
+    extern "C" int cs_ijloop_density_list_##SUF(cs_stream_t stream, const T* x, const T* y, const T* z, const T* h,   \
+                                               const T* m, uint32_t first, uint32_t last, const cs_box* box,          \
+                                               const uint32_t* neighbors, const uint32_t* neighbor_counts,            \
+                                               unsigned ngmax, T* rho)                                                 \
+    {                                                                                                                  \
+        if (last <= first) return CS_OK;                                                                               \
+        if (!x || !y || !z || !h || !m || !box || !rho || (ngmax && (!neighbors || !neighbor_counts)))               \
+        {                                                                                                              \
+            setLastError("ijloop density (lists): null argument");                                                    \
+            return CS_ERR_INVALID;                                                                                     \
+        }                                                                                                              \
+        BoxParams<T> b = makeBoxParams<T>(*box);                                                                       \
+        int anyPbc     = b.pbc[0] | b.pbc[1] | b.pbc[2];                                                               \
+        densityListKernel<T><<<iceil(last - first, 256), 256, 0, cudaStream_t(stream)>>>(                             \
+            x, y, z, h, m, first, last, b, anyPbc, neighbors, neighbor_counts, ngmax, rho);                            \
+        CSG_CHECK_LAUNCH();                                                                                            \
+        return CS_OK;                                                                                                  \
+    }                                                                                                                  \
+    extern "C" int cs_cluster_nblist_build_##SUF(cs_stream_t stream, const T* x, const T* y, const T* z, const T* h,  \
+                                                size_t n, const cs_ns_view* tree, const cs_box* box, int key_bits,    \
+                                                unsigned ncmax, uint32_t* lists, uint32_t* counts, void* workspace,   \
+                                                size_t workspace_bytes, int* max_count_host)                          \
+    {                                                                                                                  \
+        return clusterBuild<T>(cudaStream_t(stream), x, y, z, h, n, tree, box, key_bits, ncmax, lists, counts,        \
+                               workspace, workspace_bytes, max_count_host);                                           \
+    }                                                                                                                  \
+    extern "C" int cs_ijloop_density_clusters_##SUF(cs_stream_t stream, const T* x, const T* y, const T* z,           \
+                                                   const T* h, const T* m, size_t n, const uint32_t* lists,           \
+                                                   const uint32_t* counts, unsigned ncmax, T* rho)                     \
+    {                                                                                                                  \
+        if (n == 0) return CS_OK;                                                                                      \
+        if (!x || !y || !z || !h || !m || !lists || !counts || !rho || ncmax == 0)                                     \
+        {                                                                                                              \
+            setLastError("ijloop density (clusters): invalid argument");                                              \
+            return CS_ERR_INVALID;                                                                                     \
+        }                                                                                                              \
+        size_t nic   = (n + CLUSTER - 1) / CLUSTER;                                                                    \
+        size_t warps = (nic + 3) / 4;                                                                                  \
+        densityClusterKernel<T><<<iceil(warps * 32, 128), 128, 0, cudaStream_t(stream)>>>(x, y, z, h, m, n, nic,      \
+                                                                                          lists, counts, ncmax, rho); \
+        CSG_CHECK_LAUNCH();                                                                                            \
+        return CS_OK;                                                                                                  \
+    }
+
+namespace csg
+{
+size_t clusterWorkspaceBytes(size_t n) { return ((n + CLUSTER - 1) / CLUSTER) * 2 * sizeof(float4) + 512; }
+
+template<class T>
+int clusterBuild(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, size_t n, const cs_ns_view* tree,
+                 const cs_box* box, int keyBits, unsigned ncmax, uint32_t* lists, uint32_t* counts, void* ws,
+                 size_t wsb, int* maxCountHost)
+{
+    if (n == 0) return CS_OK;
+    if (keyBits != 32 && keyBits != 64)
+    {
+        setLastError("cluster neighbour lists: key_bits must be 32 or 64");
+        return CS_ERR_INVALID;
+    }
+    if (!x || !y || !z || !h || !tree || !box || !lists || !counts || ncmax == 0 || n >= (size_t(1) << 32) ||
+        !tree->child_offsets || !tree->internal_to_leaf || !tree->layout || !tree->centers || !tree->sizes)
+    {
+        setLastError("cluster neighbour lists: invalid argument");
+        return CS_ERR_INVALID;
+    }
+    if (box->boundary[0] == CS_PERIODIC || box->boundary[1] == CS_PERIODIC || box->boundary[2] == CS_PERIODIC)
+    {
+        setLastError("cluster neighbour lists: periodic boxes are not supported");
+        return CS_ERR_INVALID;
+    }
+    const size_t nic = (n + CLUSTER - 1) / CLUSTER;
+    const size_t need = clusterWorkspaceBytes(n) + 256;
+    Workspace w;
+    int rc = w.acquire(ws, wsb, need, s);
+    if (rc) return rc;
+    Arena ar{static_cast<char*>(w.ptr), 0, need};
+    float4* jBoxes = ar.take<float4>(2 * nic);
+    uint32_t* err  = ar.take<uint32_t>(4);
+    CSG_CUDA_TRY(cudaMemsetAsync(err, 0, 4 * sizeof(uint32_t), s));
+    jClusterBoxKernel<T><<<iceil(nic, 256), 256, 0, s>>>(x, y, z, n, nic, jBoxes);
+    CSG_CHECK_LAUNCH();
+    BoxParams<T> bp = makeBoxParams<T>(*box);
+    ClusterBuildArgs<T> a{};
+    a.x = x, a.y = y, a.z = z, a.h = h, a.n = n, a.numIClusters = nic;
+    a.childOffsets   = tree->child_offsets;
+    a.internalToLeaf = tree->internal_to_leaf;
+    a.layout         = tree->layout;
+    a.centers        = static_cast<const T*>(tree->centers);
+    a.sizes          = static_cast<const T*>(tree->sizes);
+    a.jBoxes         = jBoxes;
+    // one finest cell of the keys (box length / 2^maxLevel), rounded up: the slack between a particle and the box of
+    // the leaf its key selects
+    const int maxLevel = keyBits == 32 ? 10 : 21;
+    for (int k = 0; k < 3; ++k)
+        a.margin[k] = float(double(bp.len[k]) / double(1ull << maxLevel) * 1.0001);
+    a.ncmax  = ncmax;
+    a.lists  = lists;
+    a.counts = counts;
+    a.err    = err;
+    clusterBuildKernel<T><<<iceil(nic, CB_WARPS), CB_WARPS * 32, 0, s>>>(a);
+    CSG_CHECK_LAUNCH();
+    uint32_t herr = 0;
+    CSG_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CSG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (herr & 2u)
+    {
+        setLastError("cluster neighbour lists: traversal stack overflow (malformed tree)");
+        return CS_ERR_DEVICE;
+    }
+    if (herr & 1u)
+    {
+        if (maxCountHost)
+        {
+            // the largest count, for the caller to size ncmax
+            unsigned mx = 0;
+            std::vector<uint32_t> hc(nic);
+            CSG_CUDA_TRY(cudaMemcpy(hc.data(), counts, nic * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            for (uint32_t c : hc)
+                mx = c > mx ? c : mx;
+            *maxCountHost = int(mx);
+        }
+        setLastError("cluster neighbour lists: an i-cluster needs more than ncmax = %u j-clusters", ncmax);
+        return CS_ERR_CAPACITY;
+    }
+    return CS_OK;
+}
+} // namespace csg
+
+CS_IJLOOP_ENTRIES(f64, double)
+CS_IJLOOP_ENTRIES(f32, float)
+
+extern "C" size_t cs_cluster_nblist_workspace_bytes(size_t n) { return clusterWorkspaceBytes(n) + 256; }

@@ -825,3 +825,54 @@ def node_layout(focus_leaf_counts, flags, leaf_to_internal_leaves, first, last):
     _check(lib.cs_node_layout(_stream(), _p(focus_leaf_counts), L, _p(flags), _p(leaf_to_internal_leaves), first,
                               last, _p(out), None, C.c_size_t(0)))
     return out
+
+
+# ---------------------------------------------------------------------------------------------------------------
+# neighbour-list consumers (ijLoop with an SPH density interaction)
+# ---------------------------------------------------------------------------------------------------------------
+
+lib.cs_cluster_nblist_workspace_bytes.restype = C.c_size_t
+
+
+def _ns_view(tree, layout, centers, sizes, search_ext=1.0):
+    return NsView(tree.num_leaves, tree.num_nodes, C.c_void_p(tree.child_offsets.data_ptr()),
+                  C.c_void_p(tree.parents.data_ptr()), C.c_void_p(tree.internal_to_leaf.data_ptr()),
+                  C.c_void_p(layout.data_ptr()), C.c_void_p(centers.data_ptr()), C.c_void_p(sizes.data_ptr()),
+                  search_ext)
+
+
+def ijloop_density_list(x, y, z, h, m, box, nb, nc, first=0, last=None):
+    """density over the ngmax-strided neighbour rows nb (n x ngmax) with counts nc"""
+    last = x.numel() if last is None else last
+    rho = torch.empty(last - first, dtype=x.dtype, device=x.device)
+    fn = lib.cs_ijloop_density_list_f64 if x.dtype == torch.float64 else lib.cs_ijloop_density_list_f32
+    _check(fn(_stream(), _p(x), _p(y), _p(z), _p(h), _p(m), C.c_uint32(first), C.c_uint32(last), C.byref(box),
+              _p(nb), _p(nc), C.c_uint(nb.shape[1]), _p(rho)))
+    return rho
+
+
+def cluster_nblist(x, y, z, h, box, tree, layout, centers, sizes, key_bits=64, ncmax=256):
+    """cluster-pair lists: (lists[n_icl, ncmax], counts[n_icl]); ncmax grows to the largest count when needed"""
+    n = x.numel()
+    nic = (n + 7) // 8
+    view = _ns_view(tree, layout, centers, sizes)
+    fn = lib.cs_cluster_nblist_build_f64 if x.dtype == torch.float64 else lib.cs_cluster_nblist_build_f32
+    while True:
+        lists = torch.empty((nic, ncmax), dtype=torch.int32, device=x.device)
+        counts = torch.empty(nic, dtype=torch.int32, device=x.device)
+        mx = C.c_int()
+        rc = fn(_stream(), _p(x), _p(y), _p(z), _p(h), C.c_size_t(n), C.byref(view), C.byref(box), key_bits,
+                C.c_uint(ncmax), _p(lists), _p(counts), None, C.c_size_t(0), C.byref(mx))
+        if rc == CS_ERR_CAPACITY:
+            ncmax = mx.value
+            continue
+        _check(rc)
+        return lists, counts
+
+
+def ijloop_density_clusters(x, y, z, h, m, lists, counts):
+    rho = torch.empty_like(x)
+    fn = lib.cs_ijloop_density_clusters_f64 if x.dtype == torch.float64 else lib.cs_ijloop_density_clusters_f32
+    _check(fn(_stream(), _p(x), _p(y), _p(z), _p(h), _p(m), C.c_size_t(x.numel()), _p(lists), _p(counts),
+              C.c_uint(lists.shape[1]), _p(rho)))
+    return rho

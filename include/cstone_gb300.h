@@ -423,6 +423,44 @@ int cs_node_layout(cs_stream_t stream, const uint32_t* focus_leaf_counts, int32_
                    const int32_t* leaf_to_internal, int32_t first, int32_t last, uint32_t* layout, void* workspace,
                    size_t workspace_bytes);
 
+/* ---- neighbour-list consumers (ijLoop) ------------------------------------------------------------------------
+ * An SPH density interaction over neighbours: rho_i = hinv^3 (m_i w(0) + sum_j m_j w(|x_i - x_j| hinv)), hinv = 1/h_i,
+ * w(q) = (1 - 1.5 q^2) + 0.75 q^3 for q < 1, else 0.25 (2 - q)^3, over j != i with |x_i - x_j|^2 < (2 h_i)^2, summed in
+ * ascending j with round-to-nearest arithmetic (no fused multiply-add).
+ * cs_ijloop_density_list_* replaces the loop of CpuFullNbListNeighborhood (traversal/ijloop/cpu_fullnblist.hpp:94-112)
+ * over the ngmax-strided rows of cs_find_neighbors_* (results equal it bit for bit; periodic boxes folded as
+ * posDiffAndDistSq does, traversal/ijloop/common.hpp:154-172).
+ * cs_cluster_nblist_build_* / cs_ijloop_density_clusters_* take the role of GpuSuperclusterNbListNeighborhoodBuilder
+ * (traversal/ijloop/gpu_superclusternblist.cuh:248-360): clusters of 8 consecutive particles; lists holds, per
+ * i-cluster i (n/8 rounded up of them), counts[i] j-cluster indices at lists[i * ncmax ..], ascending, covering every
+ * j within 2 h of the cluster's particles (open boxes only). key_bits is the key width the tree was built with. If an
+ * i-cluster needs more than ncmax j-clusters the build returns CS_ERR_CAPACITY and *max_count_host (if not NULL) the
+ * largest count. The build synchronises the stream. The cluster loop's results equal the sum over all pairs within
+ * 2 h_i in ascending j, bit for bit. */
+int cs_ijloop_density_list_f64(cs_stream_t stream, const double* x, const double* y, const double* z, const double* h,
+                               const double* m, uint32_t first, uint32_t last, const cs_box* box,
+                               const uint32_t* neighbors, const uint32_t* neighbor_counts, unsigned ngmax,
+                               double* rho);
+int cs_ijloop_density_list_f32(cs_stream_t stream, const float* x, const float* y, const float* z, const float* h,
+                               const float* m, uint32_t first, uint32_t last, const cs_box* box,
+                               const uint32_t* neighbors, const uint32_t* neighbor_counts, unsigned ngmax,
+                               float* rho);
+size_t cs_cluster_nblist_workspace_bytes(size_t n);
+int cs_cluster_nblist_build_f64(cs_stream_t stream, const double* x, const double* y, const double* z,
+                                const double* h, size_t n, const cs_ns_view* tree, const cs_box* box, int key_bits,
+                                unsigned ncmax, uint32_t* lists, uint32_t* counts, void* workspace,
+                                size_t workspace_bytes, int* max_count_host);
+int cs_cluster_nblist_build_f32(cs_stream_t stream, const float* x, const float* y, const float* z, const float* h,
+                                size_t n, const cs_ns_view* tree, const cs_box* box, int key_bits, unsigned ncmax,
+                                uint32_t* lists, uint32_t* counts, void* workspace, size_t workspace_bytes,
+                                int* max_count_host);
+int cs_ijloop_density_clusters_f64(cs_stream_t stream, const double* x, const double* y, const double* z,
+                                   const double* h, const double* m, size_t n, const uint32_t* lists,
+                                   const uint32_t* counts, unsigned ncmax, double* rho);
+int cs_ijloop_density_clusters_f32(cs_stream_t stream, const float* x, const float* y, const float* z, const float* h,
+                                   const float* m, size_t n, const uint32_t* lists, const uint32_t* counts,
+                                   unsigned ncmax, float* rho);
+
 /* ---- whole path: keys -> sort -> gather -> computeOctree -> link -> geometry -> findHalos -> findNeighbors ---------
  * The single-rank inner part of the reference's Domain::sync + discoverHalos + neighbour search
  * (domain/assignment.hpp:105-120, focus/octree_focus_mpi.hpp:512-568, findneighbors.hpp:156-177), as one object that

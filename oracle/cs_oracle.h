@@ -147,6 +147,16 @@ void cso_range_count(const uint64_t* leaves, int32_t n_leaf_keys, const uint32_t
                      const int32_t* focus_idx, int32_t n_idx, uint32_t* counts_focus);
 void cso_node_layout(const uint32_t* focus_leaf_counts, int32_t num_leaves, const uint8_t* flags, const int32_t* l2i,
                      int32_t first, int32_t last, uint32_t* layout);
+void cso_ijloop_density_list_f64(const double* x, const double* y, const double* z, const double* h, const double* m,
+                                 uint32_t first, uint32_t last, const cso_box* box, const uint32_t* nb,
+                                 const uint32_t* nc, unsigned ngmax, double* rho);
+void cso_ijloop_density_list_f32(const float* x, const float* y, const float* z, const float* h, const float* m,
+                                 uint32_t first, uint32_t last, const cso_box* box, const uint32_t* nb,
+                                 const uint32_t* nc, unsigned ngmax, float* rho);
+void cso_ijloop_density_all_f64(const double* x, const double* y, const double* z, const double* h, const double* m,
+                                uint32_t n, const cso_box* box, double* rho);
+void cso_ijloop_density_all_f32(const float* x, const float* y, const float* z, const float* h, const float* m,
+                                uint32_t n, const cso_box* box, float* rho);
 
 #ifdef __cplusplus
 }

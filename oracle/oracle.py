@@ -702,3 +702,22 @@ def node_layout(focus_leaf_counts, flags, l2i, first, last, use_ref=False):
     else:
         lib().cso_node_layout(_p(c), c.size, _p(f), _p(l2), first, last, _p(out))
     return out
+
+
+def ijloop_density_list(x, y, z, h, m, first, last, box, nb, nc, ngmax):
+    """the SPH density of the tests' ijLoop interaction over the CPU full neighbour lists (ngmax-strided rows)"""
+    dt = x.dtype
+    rho = np.zeros(last - first, dt)
+    fn = lib().cso_ijloop_density_list_f64 if dt == np.float64 else lib().cso_ijloop_density_list_f32
+    fn(_p(x), _p(y), _p(z), _p(h), _p(m), C.c_uint32(first), C.c_uint32(last), C.byref(box),
+       _p(np.ascontiguousarray(nb, np.uint32)), _p(np.ascontiguousarray(nc, np.uint32)), C.c_uint(ngmax), _p(rho))
+    return rho
+
+
+def ijloop_density_all(x, y, z, h, m, box):
+    """the same density over every pair within 2 h_i, ascending j (brute force: small n only)"""
+    dt = x.dtype
+    rho = np.zeros(x.size, dt)
+    fn = lib().cso_ijloop_density_all_f64 if dt == np.float64 else lib().cso_ijloop_density_all_f32
+    fn(_p(x), _p(y), _p(z), _p(h), _p(m), C.c_uint32(x.size), C.byref(box), _p(rho))
+    return rho
