@@ -31,10 +31,10 @@ __device__ __forceinline__ int ordKey(float v)
 }
 __device__ __forceinline__ float ordVal(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7fffffff)); }
 
-template<class T>
+template<class T, class Th>
 __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z,
-                                  const T* __restrict__ h, const uint32_t* __restrict__ layout, int firstLeaf,
-                                  int lastLeaf, T scale, const int32_t* __restrict__ l2i,
+                                  const Th* __restrict__ h, const uint32_t* __restrict__ layout, int firstLeaf,
+                                  int lastLeaf, Th scale, const int32_t* __restrict__ l2i,
                                   const T* __restrict__ nodeCenters, T* __restrict__ sc, T* __restrict__ ss)
 {
     using I           = std::conditional_t<std::is_same_v<T, double>, long long, int>;
@@ -56,13 +56,14 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
         constexpr int U = 4;
         for (uint32_t i0 = first + sub; i0 < last; i0 += U * TPL)
         {
-            T ph[U], px[U], py[U], pz[U];
+            Th ph[U];
+            T px[U], py[U], pz[U];
 #pragma unroll
             for (int u = 0; u < U; ++u)
             {
                 const uint32_t i = i0 + u * TPL;
                 const bool ok    = i < last;
-                ph[u]            = ok ? h[i] : T(0);
+                ph[u]            = ok ? h[i] : Th(0);
                 px[u]            = ok ? x[i] : T(0);
                 py[u]            = ok ? y[i] : T(0);
                 pz[u]            = ok ? z[i] : T(0);
@@ -71,7 +72,8 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
             for (int u = 0; u < U; ++u)
             {
                 if (i0 + u * TPL >= last) continue;
-                T r    = RN<T>::mul(ph[u], scale);
+                // r = h * scale in the precision of h (computeBoundingBox, focus/source_center.hpp:33)
+                T r    = T(RN<Th>::mul(ph[u], scale));
                 T p[3] = {px[u], py[u], pz[u]};
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
@@ -112,14 +114,14 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
     }
 }
 
-template<class T>
-int searchBoxes(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, const uint32_t* layout, int first,
-                int last, T scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss)
+template<class T, class Th>
+int searchBoxes(cudaStream_t s, const T* x, const T* y, const T* z, const Th* h, const uint32_t* layout, int first,
+                int last, Th scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss)
 {
     if (last <= first) return CS_OK;
     size_t threads = size_t(last - first) * 8;
-    searchBoxesKernel<T><<<iceil(threads, 256), 256, 0, s>>>(x, y, z, h, layout, first, last, scale, l2i, nodeCenters,
-                                                             sc, ss);
+    searchBoxesKernel<T, Th><<<iceil(threads, 256), 256, 0, s>>>(x, y, z, h, layout, first, last, scale, l2i,
+                                                                 nodeCenters, sc, ss);
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }
@@ -355,10 +357,14 @@ int findHalos(cudaStream_t s, const K* prefixes, const int32_t* childOffsets, co
     return CS_OK;
 }
 
-template int searchBoxes<float>(cudaStream_t, const float*, const float*, const float*, const float*, const uint32_t*,
-                                int, int, float, const int32_t*, const float*, float*, float*);
-template int searchBoxes<double>(cudaStream_t, const double*, const double*, const double*, const double*,
-                                 const uint32_t*, int, int, double, const int32_t*, const double*, double*, double*);
+template int searchBoxes<float, float>(cudaStream_t, const float*, const float*, const float*, const float*,
+                                       const uint32_t*, int, int, float, const int32_t*, const float*, float*, float*);
+template int searchBoxes<double, double>(cudaStream_t, const double*, const double*, const double*, const double*,
+                                         const uint32_t*, int, int, double, const int32_t*, const double*, double*,
+                                         double*);
+template int searchBoxes<double, float>(cudaStream_t, const double*, const double*, const double*, const float*,
+                                        const uint32_t*, int, int, float, const int32_t*, const double*, double*,
+                                        double*);
 template int findHalos<uint32_t, float>(cudaStream_t, const uint32_t*, const int32_t*, const int32_t*, const float*,
                                         const float*, const uint32_t*, const float*, const float*, const cs_box&, int,
                                         int, uint8_t*, uint32_t*, const float4*);
@@ -377,13 +383,19 @@ extern "C" int cs_search_boxes_f32(cs_stream_t stream, const float* x, const flo
                                    const uint32_t* layout, int32_t first, int32_t last, float scale,
                                    const int32_t* l2i, const float* nc, float* sc, float* ss)
 {
-    return searchBoxes<float>(cudaStream_t(stream), x, y, z, h, layout, first, last, scale, l2i, nc, sc, ss);
+    return searchBoxes<float, float>(cudaStream_t(stream), x, y, z, h, layout, first, last, scale, l2i, nc, sc, ss);
 }
 extern "C" int cs_search_boxes_f64(cs_stream_t stream, const double* x, const double* y, const double* z,
                                    const double* h, const uint32_t* layout, int32_t first, int32_t last, double scale,
                                    const int32_t* l2i, const double* nc, double* sc, double* ss)
 {
-    return searchBoxes<double>(cudaStream_t(stream), x, y, z, h, layout, first, last, scale, l2i, nc, sc, ss);
+    return searchBoxes<double, double>(cudaStream_t(stream), x, y, z, h, layout, first, last, scale, l2i, nc, sc, ss);
+}
+extern "C" int cs_search_boxes_f64_hf32(cs_stream_t stream, const double* x, const double* y, const double* z,
+                                        const float* h, const uint32_t* layout, int32_t first, int32_t last,
+                                        float scale, const int32_t* l2i, const double* nc, double* sc, double* ss)
+{
+    return searchBoxes<double, float>(cudaStream_t(stream), x, y, z, h, layout, first, last, scale, l2i, nc, sc, ss);
 }
 
 #define CS_HALOS_ENTRY(kb, K, tb, T)                                                                                   \

@@ -5,9 +5,10 @@
 namespace csg
 {
 
-template<class T>
-int searchBoxes(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, const uint32_t* layout, int first,
-                int last, T scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss);
+//! Th: the type of h (T, or float with T = double as computeBoundingBoxGpu<double, float>)
+template<class T, class Th>
+int searchBoxes(cudaStream_t s, const T* x, const T* y, const T* z, const Th* h, const uint32_t* layout, int first,
+                int last, Th scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss);
 
 //! nrec (may be null): the neighbour search's float node records (NbPrep::nrec: centre and half size rounded to
 //! nearest at [3i] and [3i + 2]); with T = double and no periodic axis they enable the float pre-filter of the node

@@ -140,6 +140,30 @@ __device__ __forceinline__ float warpMaxF(float v)
     return v;
 }
 
+// radiusSq = 4 h h and cellRadiusSq = radiusSq ext ext in the precision of h (findneighbors.hpp:93-94), and the 2 h
+// of the periodic-crossing test (:100): h of type T, or float with T coordinates when hf is set (the reference's
+// findNeighbors with Tc = double and Th = float: both radii rounded to float, compared with T distances)
+template<class T>
+__device__ __forceinline__ void targetRadii(const T* h, const float* hf, uint32_t i, float ext, T& r2, T& cellR2,
+                                            T& twoh)
+{
+    if (hf)
+    {
+        const float hh  = hf[i];
+        const float r2f = __fmul_rn(__fmul_rn(4.f, hh), hh);
+        r2              = T(r2f);
+        cellR2          = T(__fmul_rn(__fmul_rn(r2f, ext), ext));
+        twoh            = RN<T>::mul(T(2), T(hh));
+    }
+    else
+    {
+        const T hi = h[i];
+        r2         = RN<T>::mul(RN<T>::mul(T(4.0), hi), hi);
+        cellR2     = RN<T>::mul(RN<T>::mul(r2, T(ext)), T(ext));
+        twoh       = RN<T>::mul(T(2), hi);
+    }
+}
+
 template<class T, bool Stats>
 __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, NbPrep prep)
 {
@@ -157,13 +181,11 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
 
     // ---- target state in the reference precision ----
     T xi = a.x[i], yi = a.y[i], zi = a.z[i];
-    T hi      = a.h[i];
-    T r2      = RN<T>::mul(RN<T>::mul(T(4.0), hi), hi);
-    T cellR2  = RN<T>::mul(RN<T>::mul(r2, T(a.ext)), T(a.ext));
+    T r2, cellR2, twoh;
+    targetRadii<T>(a.h, a.hf, i, a.ext, r2, cellR2, twoh);
     bool pbc  = false;
     if (a.anyPbc)
     {
-        T twoh      = RN<T>::mul(T(2), hi);
         bool inside = RN<T>::sub(xi, twoh) >= a.b.lo[0] && RN<T>::sub(yi, twoh) >= a.b.lo[1] &&
                       RN<T>::sub(zi, twoh) >= a.b.lo[2] && RN<T>::add(xi, twoh) <= a.b.hi[0] &&
                       RN<T>::add(yi, twoh) <= a.b.hi[1] && RN<T>::add(zi, twoh) <= a.b.hi[2];
@@ -463,6 +485,7 @@ template<class T>
 struct TargetRef
 {
     const T *x, *y, *z, *h;
+    const float* hf;
     float ext;
     uint32_t i;
 };
@@ -473,9 +496,8 @@ __device__ __forceinline__ void loadTarget(const TargetRef<T>& t, T& xi, T& yi, 
     xi       = t.x[t.i];
     yi       = t.y[t.i];
     zi       = t.z[t.i];
-    T hi     = t.h[t.i];
-    r2       = RN<T>::mul(RN<T>::mul(T(4.0), hi), hi);
-    cellR2   = RN<T>::mul(RN<T>::mul(r2, T(t.ext)), T(t.ext));
+    T twoh;
+    targetRadii<T>(t.h, t.hf, t.i, t.ext, r2, cellR2, twoh);
 }
 
 // a candidate in the FP32 band (T = double) or past Tsafe (T = float): the pair and path decision
@@ -557,8 +579,9 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         size_t ip  = b32 + lane;
         bool act   = ip < size_t(a.last);
         uint32_t q = act ? uint32_t(ip) : uint32_t(b32);
-        T hq = a.h[q], xq = a.x[q], yq = a.y[q], zq = a.z[q];
-        T twoh      = RN<T>::mul(T(2), hq);
+        T xq = a.x[q], yq = a.y[q], zq = a.z[q];
+        T r2q, cr2q, twoh;
+        targetRadii<T>(a.h, a.hf, q, a.ext, r2q, cr2q, twoh);
         bool inside = RN<T>::sub(xq, twoh) >= a.b.lo[0] && RN<T>::sub(yq, twoh) >= a.b.lo[1] &&
                       RN<T>::sub(zq, twoh) >= a.b.lo[2] && RN<T>::add(xq, twoh) <= a.b.hi[0] &&
                       RN<T>::add(yq, twoh) <= a.b.hi[1] && RN<T>::add(zq, twoh) <= a.b.hi[2];
@@ -569,9 +592,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     const uint32_t i  = active ? uint32_t(i64) : uint32_t(base0);
 
     T xi = a.x[i], yi = a.y[i], zi = a.z[i];
-    T hi     = a.h[i];
-    T r2     = RN<T>::mul(RN<T>::mul(T(4.0), hi), hi);
-    T cellR2 = RN<T>::mul(RN<T>::mul(r2, T(a.ext)), T(a.ext));
+    T r2, cellR2, twohI;
+    targetRadii<T>(a.h, a.hf, i, a.ext, r2, cellR2, twohI);
 
     // ---- the warp's float frame: P = lane 0's position rounded to float, b = x_i - P ----
     float P[3], b[3];
@@ -785,7 +807,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
         sTgtB[warp][lane] = nTupS;
         __syncwarp();
     }
-    const TargetRef<T> tref{a.x, a.y, a.z, a.h, a.ext, i};
+    const TargetRef<T> tref{a.x, a.y, a.z, a.h, a.hf, a.ext, i};
     auto decideSlow = [&](uint32_t jj, int node, bool contained) -> bool {
         return slowPairAt<T>(tref, kappa, jj, node, a.parents, a.centers, a.sizes, contained, rootNode);
     };
@@ -1643,9 +1665,10 @@ NbArgs<T> makeNbArgs(const T* x, const T* y, const T* z, const T* h, uint32_t fi
 
 template<class T>
 int findNeighborsEntry(cudaStream_t s, const T* x, const T* y, const T* z, const T* h, uint32_t first, uint32_t last,
-                       const cs_box& box, const cs_ns_view& v, unsigned ngmax, uint32_t* nb, uint32_t* nc)
+                       const cs_box& box, const cs_ns_view& v, unsigned ngmax, uint32_t* nb, uint32_t* nc,
+                       const float* hf = nullptr)
 {
-    if (last < first || (last > first && (!x || !y || !z || !h || !nc || (ngmax && !nb) || !v.child_offsets ||
+    if (last < first || (last > first && (!x || !y || !z || (!h && !hf) || !nc || (ngmax && !nb) || !v.child_offsets ||
                                           !v.parents || !v.internal_to_leaf || !v.layout || !v.centers || !v.sizes)))
     {
         setLastError("find neighbors: invalid arguments");
@@ -1653,6 +1676,7 @@ int findNeighborsEntry(cudaStream_t s, const T* x, const T* y, const T* z, const
     }
     if (last == first) return CS_OK;
     NbArgs<T> a = makeNbArgs<T>(x, y, z, h, first, last, box, v, ngmax, nb, nc);
+    a.hf        = hf;
     // the float shadows and the outside flags cover every particle a leaf can reference: [0, layout[L])
     uint32_t nAll = 0;
     CSG_CUDA_TRY(cudaMemcpyAsync(&nAll, v.layout + v.num_leaf_nodes, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -1702,4 +1726,18 @@ extern "C" int cs_find_neighbors_f64(cs_stream_t stream, const double* x, const 
     }
     return findNeighborsEntry<double>(cudaStream_t(stream), x, y, z, h, first, last, *box, *tree, ngmax, neighbors,
                                       counts);
+}
+
+extern "C" int cs_find_neighbors_f64_hf32(cs_stream_t stream, const double* x, const double* y, const double* z,
+                                          const float* h, uint32_t first, uint32_t last, const cs_box* box,
+                                          const cs_ns_view* tree, unsigned ngmax, uint32_t* neighbors,
+                                          uint32_t* counts)
+{
+    if (!box || !tree || (last > first && !h))
+    {
+        setLastError("find neighbors: null box, tree or h");
+        return CS_ERR_INVALID;
+    }
+    return findNeighborsEntry<double>(cudaStream_t(stream), x, y, z, nullptr, first, last, *box, *tree, ngmax,
+                                      neighbors, counts, h);
 }

@@ -30,6 +30,9 @@ struct NbArgs
     int pathOnlyPbcWarps = 0;
     //! device error word (may be null): traversal stack overflow of the group kernel
     uint32_t* errWord = nullptr;
+    //! smoothing lengths in float with coordinates of type T (then h is unused): the reference's findNeighbors with
+    //! Tc = double, Th = float (radii rounded to float)
+    const float* hf = nullptr;
     //! targets per warp of the group traversal (8, 16 or 32)
     int groupSize = 32;
     //! one target per lane (groupSize 32): a candidate batch runs the by-target loop when 19 x (needing lanes) is

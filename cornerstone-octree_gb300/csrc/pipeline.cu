@@ -662,7 +662,7 @@ struct Pipeline final : PipelineBase
             if ((rc = sc.ensure(3 * size_t(L) * sizeof(T)))) return rc;
             if ((rc = ss.ensure(3 * size_t(L) * sizeof(T)))) return rc;
             T scale = T(2.0f * cfg.halo_search_ext);
-            if ((rc = searchBoxes<T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), layout.as<uint32_t>(),
+            if ((rc = searchBoxes<T, T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), layout.as<uint32_t>(),
                                      br.focusFirst, br.focusLast, scale, l2i.as<int32_t>() + I, centers.as<T>(),
                                      sc.as<T>(), ss.as<T>())))
                 return rc;

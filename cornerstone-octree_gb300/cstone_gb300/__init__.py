@@ -293,6 +293,10 @@ def search_boxes(x, y, z, h, layout, first, last, scale, leaf_to_internal_leaves
         _check(lib.cs_search_boxes_f32(_stream(), _p(x), _p(y), _p(z), _p(h), _p(layout), first, last,
                                        C.c_float(scale), _p(leaf_to_internal_leaves), _p(node_centers), _p(sc),
                                        _p(ss)))
+    elif h.dtype == torch.float32:  # double coordinates, float h
+        _check(lib.cs_search_boxes_f64_hf32(_stream(), _p(x), _p(y), _p(z), _p(h), _p(layout), first, last,
+                                            C.c_float(scale), _p(leaf_to_internal_leaves), _p(node_centers), _p(sc),
+                                            _p(ss)))
     else:
         _check(lib.cs_search_boxes_f64(_stream(), _p(x), _p(y), _p(z), _p(h), _p(layout), first, last,
                                        C.c_double(scale), _p(leaf_to_internal_leaves), _p(node_centers), _p(sc),
@@ -324,6 +328,8 @@ def find_neighbors(x, y, z, h, first, last, box, o, layout, centers, sizes, ngma
         nb, nc = out
     v = ns_view(o, layout, centers, sizes, search_ext)
     fn = lib.cs_find_neighbors_f32 if x.dtype == torch.float32 else lib.cs_find_neighbors_f64
+    if x.dtype == torch.float64 and h.dtype == torch.float32:  # double coordinates, float h
+        fn = lib.cs_find_neighbors_f64_hf32
     _check(fn(_stream(), _p(x), _p(y), _p(z), _p(h), C.c_uint32(first), C.c_uint32(last), C.byref(box),
               C.byref(v), C.c_uint(ngmax), _p(nb), _p(nc)))
     return nb, nc

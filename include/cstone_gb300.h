@@ -274,6 +274,11 @@ int cs_search_boxes_f64(cs_stream_t stream, const double* x, const double* y, co
                         const uint32_t* layout, int32_t first_leaf, int32_t last_leaf, double scale,
                         const int32_t* leaf_to_internal, const double* node_centers, double* search_centers,
                         double* search_sizes);
+/* computeBoundingBoxGpu<double, float> (focus/source_center_gpu.cu:95-101): double coordinates, float h; the radius
+ * h * scale is rounded to float */
+int cs_search_boxes_f64_hf32(cs_stream_t stream, const double* x, const double* y, const double* z, const float* h,
+                             const uint32_t* layout, int32_t first, int32_t last, float scale, const int32_t* l2i,
+                             const double* node_centers, double* search_centers, double* search_sizes);
 int cs_find_halos_u32_f32(cs_stream_t stream, const uint32_t* prefixes, const int32_t* child_offsets,
                           const int32_t* parents, const float* node_centers, const float* node_sizes,
                           const uint32_t* leaves, const float* search_centers, const float* search_sizes,
@@ -300,6 +305,11 @@ int cs_find_neighbors_f32(cs_stream_t stream, const float* x, const float* y, co
 int cs_find_neighbors_f64(cs_stream_t stream, const double* x, const double* y, const double* z, const double* h,
                           uint32_t first, uint32_t last, const cs_box* box, const cs_ns_view* tree, unsigned ngmax,
                           uint32_t* neighbors, uint32_t* counts);
+/* The reference's findNeighbors with double coordinates and float smoothing lengths (Tc = double, ThP = const float*,
+ * findneighbors.hpp:77-177): radiusSq = 4 h h and the cell radius are rounded to float, distances are double. */
+int cs_find_neighbors_f64_hf32(cs_stream_t stream, const double* x, const double* y, const double* z, const float* h,
+                               uint32_t first, uint32_t last, const cs_box* box, const cs_ns_view* tree,
+                               unsigned ngmax, uint32_t* neighbors, uint32_t* counts);
 
 /* No call counterpart in the reference (its findNeighbors leaves the ngmax-strided rows to the caller): compaction of
  * the rows written by cs_find_neighbors_* into CSR form. offsets (u64, n + 1 entries, offsets[n] = total) and list

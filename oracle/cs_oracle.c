@@ -758,4 +758,59 @@ int cso_num_threads(void)
 #endif
 }
 
+/* findNeighbors and computeBoundingBox with double coordinates and float h (Tc = double, Th = float,
+ * findneighbors.hpp:77-99, focus/source_center.hpp:28-43): the radii are float expressions, promoted where they meet
+ * double distances */
+void cso_find_neighbors_f64_hf32(const double* x, const double* y, const double* z, const float* h, uint32_t first,
+                                 uint32_t last, const cso_box* box, const int32_t* child_offsets,
+                                 const int32_t* parents, const int32_t* internal_to_leaf, const uint32_t* layout,
+                                 const double* centers, const double* sizes, float search_ext, unsigned ngmax,
+                                 uint32_t* neighbors, uint32_t* counts)
+{
+    rbox_f64 b  = make_rbox_f64(box);
+    int any_pbc = b.pbc[0] || b.pbc[1] || b.pbc[2];
+    uint32_t nw = last - first;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (uint32_t w = 0; w < nw; ++w)
+    {
+        uint32_t i   = w + first;
+        float hi     = h[i];
+        float r2     = 4.0f * hi * hi;
+        float cellR2 = r2 * search_ext * search_ext;
+        counts[w]    = find_neighbors_one_f64(i, x, y, z, (double)r2, (double)cellR2, 2.0 * (double)hi, &b, any_pbc,
+                                              child_offsets, parents, internal_to_leaf, layout, centers, sizes, ngmax,
+                                              neighbors + (size_t)w * ngmax);
+    }
+}
+
+void cso_search_boxes_f64_hf32(const double* x, const double* y, const double* z, const float* h,
+                               const uint32_t* layout, int32_t first_leaf, int32_t last_leaf, float scale,
+                               const int32_t* leaf_to_internal, const double* node_centers, double* search_centers,
+                               double* search_sizes)
+{
+#pragma omp parallel for
+    for (int32_t leaf = first_leaf; leaf < last_leaf; ++leaf)
+    {
+        const double* init = node_centers + 3 * (size_t)leaf_to_internal[leaf];
+        double mn[3] = {init[0], init[1], init[2]};
+        double mx[3] = {init[0], init[1], init[2]};
+        for (uint32_t i = layout[leaf]; i < layout[leaf + 1]; ++i)
+        {
+            float r     = h[i] * scale;
+            double p[3] = {x[i], y[i], z[i]};
+            for (int k = 0; k < 3; ++k)
+            {
+                double a = p[k] - r, c = p[k] + r;
+                mn[k]    = a < mn[k] ? a : mn[k];
+                mx[k]    = mx[k] < c ? c : mx[k];
+            }
+        }
+        for (int k = 0; k < 3; ++k)
+        {
+            search_centers[3 * (size_t)leaf + k] = (mx[k] + mn[k]) * 0.5;
+            search_sizes[3 * (size_t)leaf + k]   = (mx[k] - mn[k]) * 0.5;
+        }
+    }
+}
+
 #include "cs_oracle_next.inc"

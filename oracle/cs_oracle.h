@@ -103,6 +103,16 @@ void cso_find_neighbors_f32(const float* x, const float* y, const float* z, cons
                             const float* centers, const float* sizes, float search_ext, unsigned ngmax,
                             uint32_t* neighbors, uint32_t* counts);
 
+void cso_find_neighbors_f64_hf32(const double* x, const double* y, const double* z, const float* h, uint32_t first,
+                                 uint32_t last, const cso_box* box, const int32_t* child_offsets,
+                                 const int32_t* parents, const int32_t* internal_to_leaf, const uint32_t* layout,
+                                 const double* centers, const double* sizes, float search_ext, unsigned ngmax,
+                                 uint32_t* neighbors, uint32_t* counts);
+void cso_search_boxes_f64_hf32(const double* x, const double* y, const double* z, const float* h,
+                               const uint32_t* layout, int32_t first_leaf, int32_t last_leaf, float scale,
+                               const int32_t* leaf_to_internal, const double* node_centers, double* search_centers,
+                               double* search_sizes);
+
 /* ---- workload generators (seeded, counter-based; shared by every test and benchmark) ---- */
 void cso_philox_uniform_f64(uint64_t seed, uint64_t stream, double* out, size_t n, double lo, double hi);
 void cso_plummer_f64(uint64_t seed, double* x, double* y, double* z, size_t n, double rmax);

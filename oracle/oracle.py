@@ -251,8 +251,18 @@ def node_fp_centers(prefixes, box, dtype=np.float64, kind=HILBERT, key_bits=64):
     return c, s
 
 
-def search_boxes(x, y, z, h, layout, first, last, scale, leaf_to_internal_leaves, node_centers):
+def search_boxes(x, y, z, h, layout, first, last, scale, leaf_to_internal_leaves, node_centers, use_ref=False):
+    """computeBoundingBox per leaf; h may be float32 with double coordinates (Th = float)"""
     dt = x.dtype
+    if dt == np.float64 and h.dtype == np.float32:
+        L = layout.size - 1
+        sc = np.zeros((L, 3), dt)
+        ss = np.zeros((L, 3), dt)
+        fn = ref().csr_search_boxes_f64_hf32 if use_ref else lib().cso_search_boxes_f64_hf32
+        fn(_p(x), _p(y), _p(z), _p(h), _p(np.ascontiguousarray(layout, np.uint32)), first, last, C.c_float(scale),
+           _p(np.ascontiguousarray(leaf_to_internal_leaves, np.int32)), _p(np.ascontiguousarray(node_centers, dt)),
+           _p(sc), _p(ss))
+        return sc, ss
     L = layout.size - 1
     sc = np.zeros((L, 3), dt)
     ss = np.zeros((L, 3), dt)
@@ -275,11 +285,14 @@ def find_halos(tree, node_centers, node_sizes, search_centers, search_sizes, box
 
 
 def find_neighbors(x, y, z, h, first, last, box, tree, layout, centers, sizes, ngmax, search_ext=1.0):
+    """findNeighbors over [first, last); h may be float32 with double coordinates (Th = float)"""
     dt = x.dtype
     n = last - first
     nb = np.zeros(n * ngmax, np.uint32)
     nc = np.zeros(n, np.uint32)
     fn = lib().cso_find_neighbors_f64 if dt == np.float64 else lib().cso_find_neighbors_f32
+    if dt == np.float64 and h.dtype == np.float32:
+        fn = lib().cso_find_neighbors_f64_hf32
     fn(_p(x), _p(y), _p(z), _p(h), C.c_uint32(first), C.c_uint32(last), C.byref(box), _p(tree.child_offsets),
        _p(tree.parents), _p(tree.internal_to_leaf), _p(np.ascontiguousarray(layout, np.uint32)), _p(centers),
        _p(sizes), C.c_float(search_ext), C.c_uint(ngmax), _p(nb), _p(nc))
@@ -462,6 +475,8 @@ def ref_find_neighbors(x, y, z, h, first, last, box, tree, layout, centers, size
     nc = np.zeros(n, np.uint32)
     lo, hi, b = _box_arrays(box)
     fn = ref().csr_find_neighbors_f64 if dt == np.float64 else ref().csr_find_neighbors_f32
+    if dt == np.float64 and h.dtype == np.float32:
+        fn = ref().csr_find_neighbors_f64_hf32
     fn(_p(x), _p(y), _p(z), _p(h), C.c_uint32(first), C.c_uint32(last), _p(lo), _p(hi), _p(b), tree.num_leaves,
        tree.num_nodes, _p(tree.child_offsets), _p(tree.parents), _p(tree.internal_to_leaf),
        _p(np.ascontiguousarray(layout, np.uint32)), _p(centers), _p(sizes), C.c_float(search_ext), C.c_uint(ngmax),

@@ -131,9 +131,9 @@ void centersImpl(const uint64_t* prefixes64, int32_t numNodes, const Box<T>& box
                      box);
 }
 
-template<class T>
-void searchBoxesImpl(const T* x, const T* y, const T* z, const T* h, const uint32_t* layout, int32_t first,
-                     int32_t last, T scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss)
+template<class T, class Th = T>
+void searchBoxesImpl(const T* x, const T* y, const T* z, const Th* h, const uint32_t* layout, int32_t first,
+                     int32_t last, Th scale, const int32_t* l2i, const T* nodeCenters, T* sc, T* ss)
 {
     for (int32_t leaf = first; leaf < last; ++leaf)
     {
@@ -161,8 +161,8 @@ void findHalosImpl(const uint64_t* prefixes64, const int32_t* childOffsets, cons
               reinterpret_cast<const Vec3<T>*>(ss), box, first, last, flags);
 }
 
-template<class K, class T>
-void findNeighborsImpl(const T* x, const T* y, const T* z, const T* h, uint32_t first, uint32_t last,
+template<class K, class T, class Th = T>
+void findNeighborsImpl(const T* x, const T* y, const T* z, const Th* h, uint32_t first, uint32_t last,
                        const Box<T>& box, int32_t numLeaves, int32_t numNodes, const int32_t* childOffsets,
                        const int32_t* parents, const int32_t* i2l, const uint32_t* layout, const T* centers,
                        const T* sizes, float ext, unsigned ngmax, uint32_t* nb, uint32_t* nc)
@@ -293,6 +293,23 @@ extern "C"
                               const double* nodeCenters, double* sc, double* ss)
     {
         searchBoxesImpl<double>(x, y, z, h, layout, first, last, scale, l2i, nodeCenters, sc, ss);
+    }
+    void csr_search_boxes_f64_hf32(const double* x, const double* y, const double* z, const float* h,
+                                   const uint32_t* layout, int32_t first, int32_t last, float scale,
+                                   const int32_t* l2i, const double* nodeCenters, double* sc, double* ss)
+    {
+        searchBoxesImpl<double, float>(x, y, z, h, layout, first, last, scale, l2i, nodeCenters, sc, ss);
+    }
+    void csr_find_neighbors_f64_hf32(const double* x, const double* y, const double* z, const float* h,
+                                     uint32_t first, uint32_t last, const double* lo, const double* hi,
+                                     const int* bnd, int32_t numLeaves, int32_t numNodes,
+                                     const int32_t* childOffsets, const int32_t* parents, const int32_t* i2l,
+                                     const uint32_t* layout, const double* centers, const double* sizes, float ext,
+                                     unsigned ngmax, uint32_t* nb, uint32_t* nc)
+    {
+        auto box = makeBox<double>(lo, hi, bnd);
+        findNeighborsImpl<uint64_t, double, float>(x, y, z, h, first, last, box, numLeaves, numNodes, childOffsets,
+                                                   parents, i2l, layout, centers, sizes, ext, ngmax, nb, nc);
     }
     void csr_search_boxes_f32(const float* x, const float* y, const float* z, const float* h,
                               const uint32_t* layout, int32_t first, int32_t last, float scale, const int32_t* l2i,

@@ -140,3 +140,30 @@ def test_group_splits_structure(O, g, group_size):
     assert grp.size - 1 > (last - first + group_size - 1) // group_size  # some groups were cut
     # every fixed-group start is a group start
     assert set(range(first, last, group_size)) <= set(grp.tolist())
+
+
+@pytest.mark.parametrize("bnd", [0, 1])
+def test_float_h_with_double_coordinates_against_reference(ref, bnd):
+    """findNeighbors and computeBoundingBox with Tc = double, Th = float: radii rounded to float"""
+    O = ref
+    rng = np.random.default_rng(11 + bnd)
+    n = 20000
+    x, y, z = (rng.random(n) for _ in range(3))
+    h = (0.02 + 0.02 * rng.random(n)).astype(np.float32)
+    box = O.make_box(0.0, 1.0, bnd)
+    sk, perm = O.sort_by_key(O.sfc_keys(x, y, z, box))
+    xs, ys, zs, hs = x[perm], y[perm], z[perm], h[perm]
+    lv, ct, _ = O.compute_octree(sk, 16)
+    tr = O.build_octree(lv)
+    cen, siz = O.node_fp_centers(tr.prefixes, box)
+    lay = O.layout_from_counts(ct)
+    a = O.find_neighbors(xs, ys, zs, hs, 0, n, box, tr, lay, cen, siz, 80)
+    b = O.ref_find_neighbors(xs, ys, zs, hs, 0, n, box, tr, lay, cen, siz, 80)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    # the float radius differs from the double one: some pair must change side for the test to mean something
+    d = O.find_neighbors(xs, ys, zs, hs.astype(np.float64), 0, n, box, tr, lay, cen, siz, 80)
+    assert a[1].sum() > 0 and d[1].sum() > 0
+    l2i = tr.leaf_to_internal[tr.num_internal:]
+    s1 = O.search_boxes(xs, ys, zs, hs, lay, 0, tr.num_leaves, 2.0, l2i, cen)
+    s2 = O.search_boxes(xs, ys, zs, hs, lay, 0, tr.num_leaves, 2.0, l2i, cen, use_ref=True)
+    assert np.array_equal(s1[0], s2[0]) and np.array_equal(s1[1], s2[1])
