@@ -17,9 +17,19 @@
 //   computeBoundingBoxGpu       focus/source_center_gpu.h:40-51  -> cs_search_boxes_{f32,f64} (in/out init mode)
 //   findHalosGpu                traversal/collisions_gpu.h:46-59 -> cs_find_halos_*
 //
+//   gather                      primitives/primitives_gpu.h:48-49 -> cs_gather_{f32,f64}
+//   updateOctreeGpu             tree/update_gpu.cuh:43-68        (the reference's header template runs on the
+//                                                                 functions above; standalone builds get the same
+//                                                                 step defined here)
+//
 // Instantiations the C ABI does not cover fail to compile here (static_assert) instead of linking silently:
-// sortByKey with 64-bit values or float keys, exclusiveScan into 64-bit sums, computeBoundingBoxGpu with a float h
-// under double coordinates. Those stay with the reference's own library.
+// sortByKey with 64-bit values or float keys, exclusiveScan into 64-bit sums, gather between different types. Those
+// stay with the reference's own library.
+//
+// Two ways to build: against the reference's include directory (the default; its declarations check these
+// definitions), or with -DCSTONE_GB300_STANDALONE and no reference headers at all, where cstone_types.hpp restates the
+// interface types (Box, OctreeView, OctreeNsView, key types, execution::Gpu, DeviceVector) so that code written for
+// the reference compiles against this library alone.
 //
 // Errors: the reference prints and exits on a CUDA error (cuda/errorcheck.cuh:15-27); here every failing call throws
 // std::runtime_error with cs_last_error(). Synchronisation: calls that return host values (computeNodeOpsGpu,
@@ -34,6 +44,10 @@
 
 #include <cuda_runtime.h>
 
+#ifdef CSTONE_GB300_STANDALONE
+// no reference headers: the interface types restated in cstone_types.hpp
+#include "cstone_gb300/cstone_types.hpp"
+#else
 #include "cstone/execution.hpp"
 #include "cstone/focus/source_center_gpu.h"
 #include "cstone/primitives/primitives_gpu.h"
@@ -45,6 +59,7 @@
 #include "cstone/tree/definitions.h"
 #include "cstone/tree/octree.hpp"
 #include "cstone/tree/octree_gpu.h"
+#endif
 
 #include "cstone_gb300.h"
 
@@ -192,6 +207,34 @@ template void exclusiveScan(execution::Gpu, const int*, const int*, int*, int);
 template void exclusiveScan(execution::Gpu, const int*, const int*, unsigned*, unsigned);
 template void exclusiveScan(execution::Gpu, const unsigned*, const unsigned*, unsigned*, unsigned);
 
+// ---- permutation gather -----------------------------------------------------------------------------------------
+// a bit copy out[i] = in[perm[i]]: any 4- or 8-byte element type maps onto the float or double gather
+template<class TS, class TD, class IndexType>
+void gather(execution::Gpu exec, const IndexType* ordering, size_t numElements, const TS* src, TD* buffer)
+{
+    static_assert(sizeof(IndexType) == 4, "32-bit permutation");
+    static_assert(std::is_same_v<TS, TD> && (sizeof(TS) == 4 || sizeof(TS) == 8),
+                  "the same 4- or 8-byte element type on both sides");
+    auto* perm = reinterpret_cast<const uint32_t*>(ordering);
+    int rc;
+    if constexpr (sizeof(TS) == 8)
+        rc = cs_gather_f64(gb300::stream(exec), perm, reinterpret_cast<const double*>(src),
+                           reinterpret_cast<double*>(buffer), numElements);
+    else
+        rc = cs_gather_f32(gb300::stream(exec), perm, reinterpret_cast<const float*>(src),
+                           reinterpret_cast<float*>(buffer), numElements);
+    gb300::check(rc, "gather");
+}
+
+template void gather(execution::Gpu, const unsigned*, size_t, const double*, double*);
+template void gather(execution::Gpu, const unsigned*, size_t, const float*, float*);
+template void gather(execution::Gpu, const unsigned*, size_t, const int*, int*);
+template void gather(execution::Gpu, const unsigned*, size_t, const unsigned*, unsigned*);
+template void gather(execution::Gpu, const unsigned*, size_t, const unsigned long*, unsigned long*);
+template void gather(execution::Gpu, const int*, size_t, const int*, int*);
+template void gather(execution::Gpu, const int*, size_t, const uint32_t*, uint32_t*);
+template void gather(execution::Gpu, const int*, size_t, const uint64_t*, uint64_t*);
+
 // ---- cornerstone leaf array -----------------------------------------------------------------------------------
 template<class KeyType>
 void computeNodeCountsGpu(execution::Gpu exec, const KeyType* tree, unsigned* counts, TreeNodeIndex numNodes,
@@ -332,12 +375,16 @@ void computeBoundingBoxGpu(execution::Gpu exec, const Tc* x, const Tc* y, const 
                            const LocalIndex* layout, TreeNodeIndex first, TreeNodeIndex last, Th scale,
                            Vec3<Tc>* centers, Vec3<Tc>* sizes)
 {
-    static_assert(std::is_same_v<Tc, Th>, "h in the coordinate type");
+    static_assert(std::is_same_v<Tc, Th> || (std::is_same_v<Tc, double> && std::is_same_v<Th, float>),
+                  "h in the coordinate type, or float h with double coordinates");
     auto* c = reinterpret_cast<Tc*>(centers);
     auto* s = reinterpret_cast<Tc*>(sizes);
     int rc;
     // NULL leaf-to-node map: initialised from the caller's centres[leaf], as the reference kernel reads them
-    if constexpr (std::is_same_v<Tc, double>)
+    if constexpr (std::is_same_v<Tc, double> && std::is_same_v<Th, float>)
+        rc = cs_search_boxes_f64_hf32(gb300::stream(exec), x, y, z, h, layout, first, last, scale, nullptr, nullptr, c,
+                                      s);
+    else if constexpr (std::is_same_v<Tc, double>)
         rc = cs_search_boxes_f64(gb300::stream(exec), x, y, z, h, layout, first, last, scale, nullptr, nullptr, c, s);
     else
         rc = cs_search_boxes_f32(gb300::stream(exec), x, y, z, h, layout, first, last, scale, nullptr, nullptr, c, s);
@@ -346,6 +393,9 @@ void computeBoundingBoxGpu(execution::Gpu exec, const Tc* x, const Tc* y, const 
 
 template void computeBoundingBoxGpu(execution::Gpu, const double*, const double*, const double*, const double*,
                                     const LocalIndex*, TreeNodeIndex, TreeNodeIndex, double, Vec3<double>*,
+                                    Vec3<double>*);
+template void computeBoundingBoxGpu(execution::Gpu, const double*, const double*, const double*, const float*,
+                                    const LocalIndex*, TreeNodeIndex, TreeNodeIndex, float, Vec3<double>*,
                                     Vec3<double>*);
 template void computeBoundingBoxGpu(execution::Gpu, const float*, const float*, const float*, const float*,
                                     const LocalIndex*, TreeNodeIndex, TreeNodeIndex, float, Vec3<float>*,
@@ -388,5 +438,25 @@ template void findHalosGpu(execution::Gpu, const uint64_t*, const TreeNodeIndex*
 template void findHalosGpu(execution::Gpu, const uint64_t*, const TreeNodeIndex*, const TreeNodeIndex*,
                            const Vec3<double>*, const Vec3<double>*, const uint64_t*, const Vec3<double>*,
                            const Vec3<double>*, const Box<double>&, TreeNodeIndex, TreeNodeIndex, uint8_t*);
+
+#ifdef CSTONE_GB300_STANDALONE
+// ---- one rebalance/count step (tree/update_gpu.cuh:43-68 is a header template in the reference) ----------------
+template<class KeyType, class DevKeyVec, class DevCountVec, class DevIdxVec>
+bool updateOctreeGpu(execution::Gpu exec, std::span<const KeyType> keys, unsigned bucketSize, DevKeyVec& tree,
+                     DevCountVec& counts, DevKeyVec& tmpTree, DevIdxVec& workArray,
+                     unsigned maxCount = 0xFFFFFFFFu)
+{
+    workArray.resize(tree.size());
+    TreeNodeIndex newNumNodes =
+        computeNodeOpsGpu(exec, rawPtr(tree), nNodes(tree), rawPtr(counts), bucketSize, rawPtr(workArray));
+    tmpTree.resize(newNumNodes + 1);
+    bool converged = rebalanceTreeGpu(exec, rawPtr(tree), nNodes(tree), newNumNodes, rawPtr(workArray),
+                                      rawPtr(tmpTree));
+    swap(tree, tmpTree);
+    counts.resize(nNodes(tree));
+    computeNodeCountsGpu(exec, rawPtr(tree), rawPtr(counts), nNodes(tree), keys, maxCount, true);
+    return converged;
+}
+#endif
 
 } // namespace cstone
