@@ -50,12 +50,14 @@ def parse():
     p.add_argument("--requests", type=int, default=600, help="requests of the served workload")
     p.add_argument("--rate", type=float, default=2000.0, help="Poisson arrival rate (requests/s), served workload")
     p.add_argument("--workload", default="plummer",
-                   choices=["plummer", "incremental", "batched", "served", "sort"],
+                   choices=["plummer", "incremental", "batched", "served", "sort", "ijloop"],
                    help="plummer: the 16M keys->neighbours pass (default); incremental: 64M FP32 time steps with one "
                         "updateOctree step each, replayed from CUDA graphs; batched: 4096 uneven FP32 sets in "
                         "one batched run per chunk against a per-set loop of the single-set pipeline; served: a "
                         "Poisson stream of build and update requests through the request server; sort: the stable "
-                        "key sort of the 16M Plummer workload's Hilbert keys alone, with its HBM fraction")
+                        "key sort of the 16M Plummer workload's Hilbert keys alone, with its HBM fraction; ijloop: "
+                        "the neighbour-list consumers on the 16M Plummer particles (cluster-pair lists built and an "
+                        "SPH density summed over them, and the same sum over the stored neighbour lists)")
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--cpu-sample", type=int, default=1 << 20, help="particles of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -470,10 +472,12 @@ def run_sort(args, world, rank, local):
                 acc += e0.elapsed_time(e1)
     ms = max_over_ranks(acc / args.steps, world)
     ok = bool((kk[1:] >= kk[:-1]).all())
+    sorted_ref = kk.clone()
     passes = 8
     algo = n * (8 + 20 + (passes - 1) * 24)
     peak, peak_kind = measured_hbm_peak()
     achieved = algo / (ms * 1e-3) / 1e9
+    cub = cub_sort_leg(args, k0, sorted_ref, stream, dev, peak, world)
     if rank == 0:
         line = {"metric": "Mkeys/s stable sort (16M Hilbert64 keys of the Plummer workload)",
                 "value": round(world * n / (ms * 1e-3) / 1e6, 3), "unit": "Mkeys/s", "n_gpus": world,
@@ -485,7 +489,135 @@ def run_sort(args, world, rank, local):
                 "roofline": {"kernel": "histogram + onesweep passes", "bound": "hbm", "achieved": round(achieved, 1),
                              "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                              "algorithmic_bytes": algo},
+                "cub": cub,
                 "clocks": clocks.summary()}
+        print(json.dumps(line), flush=True)
+
+
+def cub_sort_leg(args, k0, sorted_ref, stream, dev, peak, world):
+    """CUB's DeviceRadixSort::SortPairs (the sort behind the reference's sortByKey) on the same keys with iota values,
+    over bits [0, 63) like the library's sort and over [0, 64) as the reference calls it; event-timed like the
+    library's sort, results checked equal to it"""
+    import ctypes as C
+
+    import torch
+
+    path = os.path.join(ROOT, "cornerstone-octree_gb300", "baseline", "libcub_sort.so")
+    if not os.path.exists(path):
+        return {"unavailable": "baseline/libcub_sort.so not built"}
+    cub = C.CDLL(path)
+    cub.cub_sort_pairs_u64_temp_bytes.restype = C.c_size_t
+    n = k0.numel()
+    kin = torch.empty_like(k0)
+    kout = torch.empty_like(k0)
+    vin = torch.arange(n, dtype=torch.int32, device=dev)
+    vout = torch.empty_like(vin)
+    out = {"api": "cub::DeviceRadixSort::SortPairs (CUDA toolkit CUB), keys u64, values u32 iota"}
+    for end_bit in (63, 64):
+        tb = cub.cub_sort_pairs_u64_temp_bytes(C.c_size_t(n), 0, end_bit)
+        tmp = torch.empty(tb, dtype=torch.uint8, device=dev)
+        acc = 0.0
+        for it in range(args.warmup + args.steps):
+            kin.copy_(k0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = cub.cub_sort_pairs_u64(C.c_void_p(stream.cuda_stream), C.c_void_p(kin.data_ptr()),
+                                        C.c_void_p(kout.data_ptr()), C.c_void_p(vin.data_ptr()),
+                                        C.c_void_p(vout.data_ptr()), C.c_size_t(n), 0, end_bit,
+                                        C.c_void_p(tmp.data_ptr()), C.c_size_t(tb))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rc:
+                return {"unavailable": f"CUB SortPairs returned {rc}"}
+            if it >= args.warmup:
+                acc += e0.elapsed_time(e1)
+        ms = max_over_ranks(acc / args.steps, world)
+        passes = (end_bit + 7) // 8
+        algo = n * (8 + 20 + (passes - 1) * 24)
+        out[f"bits_0_{end_bit}"] = {"ms": round(ms, 4), "Mkeys_per_s": round(n / (ms * 1e-3) / 1e6, 3),
+                                    "hbm_frac": round(algo / (ms * 1e-3) / 1e9 / peak, 4),
+                                    "same_result": bool(torch.equal(kout, sorted_ref))}
+    return out
+
+
+def run_ijloop(args, world, rank, local):
+    """Neighbour-list consumers on the 16M FP64 Plummer workload (same particles, h for 100 neighbours, Hilbert64,
+    bucket 64): per step the cluster-pair lists are built (8-particle clusters, octree walk) and an SPH density is
+    summed over them (FP64, ascending j); beside it, the same density over the stored neighbour lists of the pipeline
+    (ngmax 200). Algorithmic bytes of the cluster loop: x, y, z, h, m read and rho written per particle (48 B), plus
+    the list entries read (4 B per listed j-cluster per i-cluster)."""
+    import numpy as np
+    import torch
+    import types
+
+    import cstone_gb300 as cs
+    from cstone_gb300 import workloads as W
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.n or 16 * 1024 * 1024
+    x, y, z = W.plummer(n, args.seed + rank)
+    lo, hi = W.tight_box(x, y, z)
+    box = cs.make_box(lo, hi)
+    tx, ty, tz = (torch.from_numpy(a).to(dev) for a in (x, y, z))
+    th, _ = W.h_for_k_neighbors(tx, ty, tz, box, K_NEIGHBORS, BUCKET)
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, BUCKET, NGMAX, 1.0, 1.0, False, True)
+    r = pipe.run(tx, ty, tz, th, box)
+    out = pipe.outputs()
+    tree = types.SimpleNamespace(num_leaves=r.num_leaves, num_nodes=r.num_nodes, child_offsets=out["child_offsets"],
+                                 parents=out["parents"], internal_to_leaf=out["internal_to_leaf"])
+    m = torch.rand(n, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(5)) + 0.5
+    xs, ys, zs, hs = out["x"], out["y"], out["z"], out["h"]
+    cen, siz = out["centers"].reshape(-1), out["sizes"].reshape(-1)
+    stream = torch.cuda.current_stream()
+    lists, counts = cs.cluster_nblist(xs, ys, zs, hs, box, tree, out["layout"], cen, siz, 64, 512)
+    ncmax = lists.shape[1]
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    with ClockSampler(local) as clocks:
+        build_ms = timed(lambda: cs.cluster_nblist(xs, ys, zs, hs, box, tree, out["layout"], cen, siz, 64, ncmax))
+        loop_ms = timed(lambda: cs.ijloop_density_clusters(xs, ys, zs, hs, m, lists, counts))
+        list_ms = timed(lambda: cs.ijloop_density_list(xs, ys, zs, hs, m, box, out["neighbors"],
+                                                        out["neighbor_counts"]))
+    rho_c = cs.ijloop_density_clusters(xs, ys, zs, hs, m, lists, counts)
+    rho_l = cs.ijloop_density_list(xs, ys, zs, hs, m, box, out["neighbors"], out["neighbor_counts"])
+    nc = out["neighbor_counts"]
+    complete = bool((nc <= NGMAX).all())
+    # both sums add every neighbour of every particle in ascending j when no list was truncated
+    agree = float((rho_c == rho_l).double().mean())
+    listed = float(counts.clamp(max=ncmax).double().sum())
+    step_ms = max_over_ranks(build_ms + loop_ms, world)
+    peak, peak_kind = measured_hbm_peak()
+    algo = n * 48 + 4 * listed
+    achieved = algo / (loop_ms * 1e-3) / 1e9
+    if rank == 0:
+        line = {"metric": "Mparticles/s neighbour-list consumers: cluster-pair lists + SPH density (16M Plummer, FP64)",
+                "value": round(world * n / (step_ms * 1e-3) / 1e6, 3), "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic",
+                "config": {"workload": "ijloop-density", "n_particles_per_gpu": n, "neighbours_target": K_NEIGHBORS,
+                           "cluster": 8, "ncmax": ncmax, "keys": "hilbert64", "bucket_size": BUCKET,
+                           "l2": "inputs (640 MB) larger than L2", "parallelism": f"replicas x{world}"},
+                "stages_ms": {"cluster_lists": round(build_ms, 4), "density_over_clusters": round(loop_ms, 4),
+                              "density_over_stored_lists": round(list_ms, 4)},
+                "pair_tests_per_neighbour": round(8 * listed * 8 / max(1.0, float(nc.double().sum())), 3),
+                "roofline": {"kernel": "densityClusterKernel<double>", "bound": "fp64",
+                             "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                             "frac": round(achieved / peak, 4), "algorithmic_bytes": algo,
+                             "note": "hbm fraction of the loop; its distance tests and kernel run in FP64"},
+                "stored_lists_complete": complete, "rho_identical_frac": agree, "clocks": clocks.summary()}
         print(json.dumps(line), flush=True)
 
 
@@ -590,6 +722,9 @@ def main():
         return
     if args.workload == "sort":
         run_sort(args, world, rank, local)
+        return
+    if args.workload == "ijloop":
+        run_ijloop(args, world, rank, local)
         return
 
     import numpy as np

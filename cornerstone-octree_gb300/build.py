@@ -66,5 +66,20 @@ def build(verbose=False, jobs=None):
     return LIB
 
 
+BASELINE_SRC = os.path.join(HERE, "baseline", "cub_sort.cu")
+BASELINE_LIB = os.path.join(HERE, "baseline", "libcub_sort.so")
+
+
+def build_baseline():
+    """the CUB sort the reference calls, as a separate library for the benchmark's comparison leg (not the product)"""
+    if os.path.exists(BASELINE_LIB) and os.path.getmtime(BASELINE_LIB) >= os.path.getmtime(BASELINE_SRC):
+        return BASELINE_LIB
+    cmd = [NVCC, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", BASELINE_SRC, "-o", BASELINE_LIB]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"baseline build failed:\n{r.stdout}\n{r.stderr}")
+    return BASELINE_LIB
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
