@@ -657,21 +657,24 @@ def run_served(args, world, rank, local):
     for t in trees:
         p = pool[t]
         srv.wait(srv.submit(*p["xyz"], p["h"], p["box"], cs.REQ_BUILD, t), counts=False)
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
-    plan = []
     flip = {t: 0 for t in trees}
-    for k in range(args.requests):
-        if rng.random() < 0.3:
-            t = int(rng.choice(trees))
-            flip[t] ^= 1
-            p = pool[t]
-            plan.append((t, p["moved"] if flip[t] else p["xyz"], p, cs.REQ_UPDATE))
-        else:
-            p = pool[int(rng.integers(len(pool)))]
-            plan.append((-1, p["xyz"], p, cs.REQ_BUILD))
-    ids = []
-    t0 = time.perf_counter()
-    with ClockSampler(local) as clocks:
+
+    def serve(rate, nreq, clocks=None):
+        """Poisson arrivals at `rate` of nreq requests (30 % updates of resident trees); returns sorted latencies
+        (ms), particles, seconds from the first arrival to the last result, the last arrival time"""
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        plan = []
+        for k in range(nreq):
+            if rng.random() < 0.3:
+                t = int(rng.choice(trees))
+                flip[t] ^= 1
+                p = pool[t]
+                plan.append((t, p["moved"] if flip[t] else p["xyz"], p, cs.REQ_UPDATE))
+            else:
+                p = pool[int(rng.integers(len(pool)))]
+                plan.append((-1, p["xyz"], p, cs.REQ_BUILD))
+        ids = []
+        t0 = time.perf_counter()
         for k, (t, xyz, p, kind) in enumerate(plan):
             wait = t0 + arrivals[k] - time.perf_counter()
             if wait > 0:
@@ -682,10 +685,17 @@ def run_served(args, world, rank, local):
             r, _ = srv.wait(rid, counts=False)
             lat.append(r.latency_ms)
             parts += n
-        elapsed = time.perf_counter() - t0  # first arrival -> last result (the warm-up builds are not counted)
+        return np.sort(np.array(lat)), parts, time.perf_counter() - t0, arrivals[-1]
+
+    with ClockSampler(local) as clocks:
+        lat, parts, elapsed, last_arrival = serve(args.rate, args.requests)
+        # a rate the server sustains: 70 % of the completion rate it reached under the offered load
+        sustain_rate = 0.7 * args.requests / elapsed
+        nsus = max(60, args.requests // 3)
+        slat, sparts, selapsed, slast = serve(sustain_rate, nsus)
     st = srv.stats()
     srv.close()
-    lat = np.sort(np.array(lat))
+    arrivals = [last_arrival]
     if rank == 0:
         line = {"metric": "served requests: p50/p99 latency and Mparticles/s (Poisson 2000/s, 2^12..2^22 FP64)",
                 "value": round(parts / elapsed / 1e6, 3), "unit": "Mparticles/s", "n_gpus": world,
@@ -699,9 +709,16 @@ def run_served(args, world, rank, local):
                            "slots": 4, "hbm_budget_gb": 150, "pool_sets": len(pool),
                            "parallelism": f"replicas x{world}"},
                 "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
-                "completed": int(st.completed) - len(trees), "failed": int(st.failed), "particles": parts,
+                "completed": int(st.completed) - len(trees) - nsus, "failed": int(st.failed), "particles": parts,
                 "offered_Mparticles_per_s": round(parts / arrivals[-1] / 1e6, 3),
-                "elapsed_s": round(elapsed, 3), "clocks": clocks.summary()}
+                "elapsed_s": round(elapsed, 3),
+                "sustainable_rate": {"rate_per_s": round(sustain_rate, 2), "requests": nsus,
+                                     "p50_ms": round(float(np.percentile(slat, 50)), 3),
+                                     "p99_ms": round(float(np.percentile(slat, 99)), 3),
+                                     "Mparticles_per_s": round(sparts / selapsed / 1e6, 3),
+                                     "offered_Mparticles_per_s": round(sparts / slast / 1e6, 3),
+                                     "note": "70 % of the completion rate reached at the configured rate"},
+                "clocks": clocks.summary()}
         print(json.dumps(line), flush=True)
 
 
