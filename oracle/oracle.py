@@ -648,7 +648,7 @@ def group_splits(first, last, x, y, z, h, leaves, layout, lo, hi, group_size, to
                _p(lo), _p(hi), C.c_uint(group_size), C.c_float(tol), _p(g), cap, key_bits)
         if r >= 0:
             return g[: r + 1]
-        cap = -r + 1
+        cap = -r
 
 
 def rebalance_decision_essential(prefixes, child_offsets, parents, counts, macs, focus, bucket, key_bits=64,
