@@ -141,6 +141,47 @@ __global__ void __launch_bounds__(CSR_THREADS) csrWriteKernel(const uint32_t* __
     }
 }
 
+// Copies min(*total, capacity) list entries from device memory to pinned host memory with 16-byte stores (the host
+// link runs at its copy-engine rate this way; 4-byte stores at unaligned row offsets reach about half of it). The
+// length comes from device memory, so the copy needs no host synchronisation. src is 16-byte aligned; the first few
+// entries bring dst to a 16-byte boundary. A total above the capacity sets *overflow (when given).
+__global__ void __launch_bounds__(256) copyListKernel(const uint32_t* __restrict__ src, uint32_t* dst,
+                                                      const uint64_t* __restrict__ total, size_t capacity,
+                                                      uint32_t* overflow)
+{
+    const unsigned long long t = *total;
+    const size_t m             = t < capacity ? size_t(t) : capacity;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && overflow && t > capacity) *overflow = 1u;
+    const size_t head = min(size_t((16u - (reinterpret_cast<uintptr_t>(dst) & 15u)) / 4u & 3u), m);
+    const size_t nv   = (m - head) / 4;
+    if (blockIdx.x == 0)
+    {
+        if (threadIdx.x < head) dst[threadIdx.x] = src[threadIdx.x];
+        const size_t tail0 = head + 4 * nv;
+        if (tail0 + threadIdx.x < m) dst[tail0 + threadIdx.x] = src[tail0 + threadIdx.x];
+    }
+    const uint4* s4 = reinterpret_cast<const uint4*>(src + head);
+    uint4* d4       = reinterpret_cast<uint4*>(dst + head);
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nv; i += stride)
+        d4[i] = __ldcs(s4 + i);
+}
+
+int copyListToHost(cudaStream_t s, const uint32_t* src, uint32_t* dst, const uint64_t* totalDev, size_t capacity,
+                   uint32_t* overflow)
+{
+    if (!src || !totalDev || (capacity && !dst) || (reinterpret_cast<uintptr_t>(dst) & 3u) ||
+        (reinterpret_cast<uintptr_t>(src) & 15u))
+    {
+        setLastError("list copy: null or misaligned pointer");
+        return CS_ERR_INVALID;
+    }
+    // 64 blocks saturate the host link (measured) while leaving the SMs to the next run's kernels
+    copyListKernel<<<64, 256, 0, s>>>(src, dst, totalDev, capacity, overflow);
+    CSG_CHECK_LAUNCH();
+    return CS_OK;
+}
+
 size_t neighborCsrWorkspaceBytes(size_t n) { return ((n + CSR_TILE - 1) / CSR_TILE + 1) * 8 + 256; }
 
 int neighborCsr(cudaStream_t s, const uint32_t* nb, const uint32_t* nc, size_t n, unsigned ngmax, uint64_t* offsets,

@@ -73,12 +73,13 @@ struct Pipeline final : PipelineBase
     cudaEvent_t copyEv[kCopyChunks]  = {};
     cudaEvent_t inUsed[2]            = {}; // on the compute stream after the keys of the last run that read the set
     bool inUsedRec[2]                = {false, false};
-    // results to host: a stream of their own; the error words first (errCopied), then counts and flags (outDone)
+    // results to host: a stream of their own; the error words first (errCopied), then counts, flags and the list
+    // compaction (reuseReady: the next run may overwrite its outputs), then the lists themselves (outDone)
     cudaStream_t d2hStream = nullptr;
-    cudaEvent_t outReady = nullptr, errCopied = nullptr, outDone = nullptr;
+    cudaEvent_t outReady = nullptr, errCopied = nullptr, reuseReady = nullptr, outDone = nullptr;
     uint32_t* herrHost   = nullptr; // pinned, the last copied error words
     uint32_t* listOverflowHost = nullptr; // pinned, set by the list compaction when a list buffer was too small
-    DevBuf csrWs;
+    DevBuf csrWs, csrOff, csrList; // the compacted lists on the device, copied to the caller's host buffers
     bool outPending      = false;   // a copy-back whose errors are not yet reported
     int stickyRc         = CS_OK;   // an earlier run's device error, reported by the next wait
     char stickyMsg[160]  = {};
@@ -108,7 +109,7 @@ struct Pipeline final : PipelineBase
         for (auto& e : inUsed)
             if (e) cudaEventDestroy(e);
         if (d2hStream) cudaStreamDestroy(d2hStream);
-        for (cudaEvent_t e : {outReady, errCopied, outDone})
+        for (cudaEvent_t e : {outReady, errCopied, reuseReady, outDone})
             if (e) cudaEventDestroy(e);
         if (herrHost) cudaFreeHost(herrHost);
         if (listOverflowHost) cudaFreeHost(listOverflowHost);
@@ -344,7 +345,7 @@ struct Pipeline final : PipelineBase
              const cs_box& box, bool useGraph, cs_pipeline_result* res) override
     {
         int rc;
-        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, outDone, 0)); // a copy-back still reads the outputs
+        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, reuseReady, 0)); // a copy-back still reads the outputs
         lastNIn = 0; // autotune reruns plain runs only (a step's inputs need not outlive it)
         if (incCur < 0 || nIn != incN)
         {
@@ -655,7 +656,7 @@ struct Pipeline final : PipelineBase
         // ---- halos for the focus leaves ----
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_HALOS], s));
         if ((rc = flags.ensure(size_t(N)))) return rc;
-        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, outDone, 0)); // the previous copy-back of flags, counts
+        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, reuseReady, 0)); // the previous copy-back of flags, counts
         CSG_CUDA_TRY(cudaMemsetAsync(flags.p, 0, size_t(N), s));
         if (cfg.do_halos && br.focusLast > br.focusFirst)
         {
@@ -781,7 +782,7 @@ struct Pipeline final : PipelineBase
         if (!d2hStream)
         {
             CSG_CUDA_TRY(cudaStreamCreateWithFlags(&d2hStream, cudaStreamNonBlocking));
-            for (cudaEvent_t* e : {&outReady, &errCopied, &outDone})
+            for (cudaEvent_t* e : {&outReady, &errCopied, &reuseReady, &outDone})
                 CSG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
             CSG_CUDA_TRY(cudaHostAlloc(&herrHost, 4 * sizeof(uint32_t), cudaHostAllocDefault));
             CSG_CUDA_TRY(cudaHostAlloc(&listOverflowHost, sizeof(uint32_t), cudaHostAllocMapped));
@@ -807,16 +808,31 @@ struct Pipeline final : PipelineBase
         if (flagsHost)
             CSG_CUDA_TRY(
                 cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, d2hStream));
+        const size_t devCap = listOffsets ? std::min(listCap, n * size_t(cfg.ngmax)) : 0;
         if (listOffsets)
         {
-            // the stored neighbour indices, compacted straight into the caller's pinned buffers over the host link
+            // the stored neighbour indices compacted on the device (the next run may then overwrite the rows)
             int rc = csrWs.ensure(neighborCsrWorkspaceBytes(n));
+            if (!rc) rc = csrOff.ensure((n + 1) * sizeof(uint64_t));
+            if (!rc) rc = csrList.ensure(std::max<size_t>(devCap, 4) * sizeof(uint32_t));
             if (rc) return rc;
+            if ((rc = neighborCsr(d2hStream, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax,
+                                  csrOff.as<uint64_t>(), csrList.as<uint32_t>(), devCap, csrWs.p, csrWs.bytes,
+                                  nullptr)))
+                return rc;
+        }
+        CSG_CUDA_TRY(cudaEventRecord(reuseReady, d2hStream));
+        if (listOffsets)
+        {
+            // then to the caller's pinned buffers: the offsets by the copy engine, the list by 16-byte stores whose
+            // length the compaction left in device memory
+            CSG_CUDA_TRY(cudaMemcpyAsync(listOffsets, csrOff.p, (n + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                         d2hStream));
             uint32_t* flag = nullptr;
             CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&flag), listOverflowHost, 0));
-            if ((rc = neighborCsr(d2hStream, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax, listOffsets,
-                                  listHost, listHost ? listCap : 0, csrWs.p, csrWs.bytes, flag)))
-                return rc;
+            int rc = copyListToHost(d2hStream, csrList.as<uint32_t>(), listHost, csrOff.as<uint64_t>() + n,
+                                    listHost ? listCap : 0, flag);
+            if (rc) return rc;
         }
         CSG_CUDA_TRY(cudaEventRecord(outDone, d2hStream));
         outPending = true;
