@@ -276,29 +276,89 @@ __global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuild
     }
 }
 
-// 4 i-clusters per warp, one target per lane; each j-cluster's particles broadcast within the 8-lane segment
+// The cluster loop in two phases per warp (4 i-clusters, one target per lane; each j-cluster's particles are broadcast
+// within the lane's 8-lane segment):
+//  - screen: every candidate j of the lane's target is tested in FP32; the ones that may lie within 2 h_i go, in
+//    ascending j, into the lane's queue in shared memory;
+//  - flush (when a queue may not take another j-cluster, and at the end): every lane runs its own queue through the
+//    exact test and the interaction, so the lanes of a warp do the expensive arithmetic on their own pairs instead of
+//    all lanes following the few that accept each candidate.
+// For float coordinates the screen is the exact test itself. For double coordinates it is a proven lower bound:
+// with xf = float(x) (round to nearest), a = |float(xi_f - xj_f)| and S = |xi_f| + |xj_f|,
+//   |xi - xj| >= a (1 - 2^-24) - 2^-24 S - 2^-149,
+// and u = max(fma(-2^-21, a + S, a), 0) stays below that bound after its own roundings. A j is dropped only when
+// ux^2 + uy^2 + uz^2 (three float roundings, under 2^-21.4 relative) exceeds float_ru(r2) (1 + 2^-20): then the exact
+// d2 exceeds r2 (1 + 2^-22), and the double d2 (five roundings, under 2^-50) still exceeds r2, so the double test
+// would have dropped it too. NaN and infinite coordinates give u = 0 (never dropped); a threshold below 2^-100 is
+// raised to 2^-100 so that subnormal roundings cannot matter. The sums are those of the one-phase loop, bit for bit.
+constexpr int DC_WARPS = 4;
+constexpr int DC_QCAP  = 32; // queued candidates per target; a j-cluster adds at most CLUSTER
+
 template<class T>
-__global__ void __launch_bounds__(128) densityClusterKernel(const T* __restrict__ x, const T* __restrict__ y,
-                                                            const T* __restrict__ z, const T* __restrict__ h,
-                                                            const T* __restrict__ m, size_t n, size_t numIClusters,
-                                                            const uint32_t* __restrict__ lists,
-                                                            const uint32_t* __restrict__ counts, unsigned ncmax,
-                                                            T* __restrict__ rho)
+__device__ __forceinline__ float toFloatRn(T v)
 {
-    using R          = RN<T>;
-    const int lane   = threadIdx.x & 31;
-    const size_t gw  = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const size_t ic  = gw * 4 + (lane >> 3);
-    const int k      = lane & 7;
-    const int seg0   = lane & ~7;
-    const size_t i   = ic * CLUSTER + k;
+    if constexpr (std::is_same_v<T, double>) return __double2float_rn(v);
+    else return v;
+}
+
+__device__ __forceinline__ float screenAxis(float fi, float absFi, float fj)
+{
+    const float a = fabsf(__fsub_rn(fi, fj));
+    const float t = __fadd_rn(a, __fadd_rn(absFi, fabsf(fj)));
+    return fmaxf(__fmaf_rn(-0x1p-21f, t, a), 0.f);
+}
+
+template<class T>
+__global__ void __launch_bounds__(DC_WARPS * 32) densityClusterKernel(const T* __restrict__ x, const T* __restrict__ y,
+                                                                      const T* __restrict__ z, const T* __restrict__ h,
+                                                                      const T* __restrict__ m, size_t n,
+                                                                      size_t numIClusters,
+                                                                      const uint32_t* __restrict__ lists,
+                                                                      const uint32_t* __restrict__ counts,
+                                                                      unsigned ncmax, T* __restrict__ rho)
+{
+    constexpr bool kExactScreen = std::is_same_v<T, float>;
+    __shared__ uint32_t sQueue[DC_WARPS][DC_QCAP][32];
+    using R            = RN<T>;
+    const int lane     = threadIdx.x & 31;
+    const int warp     = threadIdx.x >> 5;
+    const size_t gw    = size_t(blockIdx.x) * DC_WARPS + warp;
+    const size_t ic    = gw * 4 + (lane >> 3);
+    const int k        = lane & 7;
+    const int seg0     = lane & ~7;
+    const size_t i     = ic * CLUSTER + k;
     const bool activeI = ic < numIClusters && i < n;
     const size_t iSafe = activeI ? i : 0;
     const T xi = x[iSafe], yi = y[iSafe], zi = z[iSafe], hi = h[iSafe];
     const T hinv = divRn<T>(T(1), hi);
     const T r2   = R::mul(R::mul(T(4), hi), hi);
     T sum        = R::mul(m[iSafe], densityW<T>(T(0), hinv));
-    const unsigned cnt = ic < numIClusters ? min(counts[ic], ncmax) : 0u;
+
+    const float fxi = toFloatRn<T>(xi), fyi = toFloatRn<T>(yi), fzi = toFloatRn<T>(zi);
+    const float axi = fabsf(fxi), ayi = fabsf(fyi), azi = fabsf(fzi);
+    float thr = 0.f;
+    if constexpr (!kExactScreen) thr = fmaxf(__fmul_ru(__double2float_ru(r2), 1.f + 0x1p-20f), 0x1p-100f);
+
+    uint32_t(*queue)[32] = sQueue[warp];
+    unsigned qn          = 0;
+    auto flush           = [&]() {
+        const unsigned qmax = __reduce_max_sync(0xffffffffu, qn);
+        __syncwarp();
+        for (unsigned s = 0; s < qmax; ++s)
+        {
+            if (s < qn)
+            {
+                const uint32_t j = queue[s][lane];
+                T dx = R::sub(xi, __ldg(x + j)), dy = R::sub(yi, __ldg(y + j)), dz = R::sub(zi, __ldg(z + j));
+                T d2 = R::add(R::add(R::mul(dx, dx), R::mul(dy, dy)), R::mul(dz, dz));
+                if (d2 < r2) sum = R::add(sum, R::mul(__ldg(m + j), densityW<T>(d2, hinv)));
+            }
+        }
+        __syncwarp();
+        qn = 0;
+    };
+
+    const unsigned cnt    = ic < numIClusters ? min(counts[ic], ncmax) : 0u;
     const unsigned maxCnt = __reduce_max_sync(0xffffffffu, cnt);
     const uint32_t* list  = lists + (ic < numIClusters ? ic : 0) * size_t(ncmax);
     for (unsigned t = 0; t < maxCnt; ++t)
@@ -307,23 +367,34 @@ __global__ void __launch_bounds__(128) densityClusterKernel(const T* __restrict_
         const size_t J   = segOn ? __ldg(list + t) : 0;
         const size_t jk  = J * CLUSTER + k;
         const bool jOk   = segOn && jk < n;
-        T xj = jOk ? x[jk] : T(0), yj = jOk ? y[jk] : T(0), zj = jOk ? z[jk] : T(0), mj = jOk ? m[jk] : T(0);
+        const float fxj = jOk ? toFloatRn<T>(x[jk]) : 0.f, fyj = jOk ? toFloatRn<T>(y[jk]) : 0.f;
+        const float fzj = jOk ? toFloatRn<T>(z[jk]) : 0.f;
 #pragma unroll
         for (int q = 0; q < CLUSTER; ++q)
         {
-            T xq = __shfl_sync(0xffffffffu, xj, seg0 + q);
-            T yq = __shfl_sync(0xffffffffu, yj, seg0 + q);
-            T zq = __shfl_sync(0xffffffffu, zj, seg0 + q);
-            T mq = __shfl_sync(0xffffffffu, mj, seg0 + q);
+            const float xq = __shfl_sync(0xffffffffu, fxj, seg0 + q);
+            const float yq = __shfl_sync(0xffffffffu, fyj, seg0 + q);
+            const float zq = __shfl_sync(0xffffffffu, fzj, seg0 + q);
             const size_t j = J * CLUSTER + q;
-            if (activeI && segOn && j < n && j != i)
+            bool cand      = activeI && segOn && j < n && j != i;
+            if constexpr (kExactScreen)
             {
-                T dx = R::sub(xi, xq), dy = R::sub(yi, yq), dz = R::sub(zi, zq);
-                T d2 = R::add(R::add(R::mul(dx, dx), R::mul(dy, dy)), R::mul(dz, dz));
-                if (d2 < r2) sum = R::add(sum, R::mul(mq, densityW<T>(d2, hinv)));
+                const float dx = __fsub_rn(fxi, xq), dy = __fsub_rn(fyi, yq), dz = __fsub_rn(fzi, zq);
+                const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                cand           = cand && d2 < float(r2);
             }
+            else
+            {
+                const float ux = screenAxis(fxi, axi, xq), uy = screenAxis(fyi, ayi, yq);
+                const float uz = screenAxis(fzi, azi, zq);
+                const float lb = __fmaf_rn(uz, uz, __fmaf_rn(uy, uy, __fmul_rn(ux, ux)));
+                cand           = cand && !(lb > thr);
+            }
+            if (cand) queue[qn++][lane] = uint32_t(j);
         }
+        if (__reduce_max_sync(0xffffffffu, qn) > DC_QCAP - CLUSTER) flush();
     }
+    flush();
     if (activeI) rho[i] = R::mul(sum, R::mul(R::mul(hinv, hinv), hinv));
 }
 
@@ -363,15 +434,15 @@ using namespace csg;
                                                    const uint32_t* counts, unsigned ncmax, T* rho)                     \
     {                                                                                                                  \
         if (n == 0) return CS_OK;                                                                                      \
-        if (!x || !y || !z || !h || !m || !lists || !counts || !rho || ncmax == 0)                                     \
+        if (!x || !y || !z || !h || !m || !lists || !counts || !rho || ncmax == 0 || n >= (size_t(1) << 32))          \
         {                                                                                                              \
             setLastError("ijloop density (clusters): invalid argument");                                              \
             return CS_ERR_INVALID;                                                                                     \
         }                                                                                                              \
         size_t nic   = (n + CLUSTER - 1) / CLUSTER;                                                                    \
         size_t warps = (nic + 3) / 4;                                                                                  \
-        densityClusterKernel<T><<<iceil(warps * 32, 128), 128, 0, cudaStream_t(stream)>>>(x, y, z, h, m, n, nic,      \
-                                                                                          lists, counts, ncmax, rho); \
+        densityClusterKernel<T><<<iceil(warps, DC_WARPS), DC_WARPS * 32, 0, cudaStream_t(stream)>>>(                  \
+            x, y, z, h, m, n, nic, lists, counts, ncmax, rho);                                                         \
         CSG_CHECK_LAUNCH();                                                                                            \
         return CS_OK;                                                                                                  \
     }

@@ -162,8 +162,22 @@ __global__ void __launch_bounds__(256) copyListKernel(const uint32_t* __restrict
     }
     const uint4* s4 = reinterpret_cast<const uint4*>(src + head);
     uint4* d4       = reinterpret_cast<uint4*>(dst + head);
+    // four loads in flight per thread before their stores: the host link needs about 1 MB of stores in flight, and
+    // the loads' latency grows while other kernels share the device
+    constexpr int U     = 4;
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nv; i += stride)
+    size_t i            = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * stride < nv; i += U * stride)
+    {
+        uint4 r[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            r[u] = __ldcs(s4 + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            d4[i + u * stride] = r[u];
+    }
+    for (; i < nv; i += stride)
         d4[i] = __ldcs(s4 + i);
 }
 

@@ -73,13 +73,17 @@ struct Pipeline final : PipelineBase
     cudaEvent_t copyEv[kCopyChunks]  = {};
     cudaEvent_t inUsed[2]            = {}; // on the compute stream after the keys of the last run that read the set
     bool inUsedRec[2]                = {false, false};
-    // results to host: a stream of their own; the error words first (errCopied), then counts, flags and the list
-    // compaction (reuseReady: the next run may overwrite its outputs), then the lists themselves (outDone)
-    cudaStream_t d2hStream = nullptr;
+    // results to host: the error words first (errCopied), then counts, flags and the list compaction (reuseReady:
+    // the next run may overwrite its outputs) on d2hStream; the compacted lists then go to the host on listStream
+    // (outDone), from one of two device buffers in turn, so that the next run's compaction need not wait for them
+    cudaStream_t d2hStream = nullptr, listStream = nullptr;
     cudaEvent_t outReady = nullptr, errCopied = nullptr, reuseReady = nullptr, outDone = nullptr;
-    uint32_t* herrHost   = nullptr; // pinned, the last copied error words
-    uint32_t* listOverflowHost = nullptr; // pinned, set by the list compaction when a list buffer was too small
-    DevBuf csrWs, csrOff, csrList; // the compacted lists on the device, copied to the caller's host buffers
+    cudaEvent_t listCopied[2]  = {};  // on listStream after the copy out of compaction buffer b
+    bool listCopiedRec[2]      = {false, false};
+    int csrCur                 = 0;
+    uint32_t* herrHost         = nullptr; // pinned, the last copied error words
+    uint32_t* listOverflowHost = nullptr; // pinned, set by the list copy when a list buffer was too small
+    DevBuf csrWs, csrOff[2], csrList[2]; // the compacted lists on the device, copied to the caller's host buffers
     bool outPending      = false;   // a copy-back whose errors are not yet reported
     int stickyRc         = CS_OK;   // an earlier run's device error, reported by the next wait
     char stickyMsg[160]  = {};
@@ -109,7 +113,8 @@ struct Pipeline final : PipelineBase
         for (auto& e : inUsed)
             if (e) cudaEventDestroy(e);
         if (d2hStream) cudaStreamDestroy(d2hStream);
-        for (cudaEvent_t e : {outReady, errCopied, reuseReady, outDone})
+        if (listStream) cudaStreamDestroy(listStream);
+        for (cudaEvent_t e : {outReady, errCopied, reuseReady, outDone, listCopied[0], listCopied[1]})
             if (e) cudaEventDestroy(e);
         if (herrHost) cudaFreeHost(herrHost);
         if (listOverflowHost) cudaFreeHost(listOverflowHost);
@@ -782,7 +787,8 @@ struct Pipeline final : PipelineBase
         if (!d2hStream)
         {
             CSG_CUDA_TRY(cudaStreamCreateWithFlags(&d2hStream, cudaStreamNonBlocking));
-            for (cudaEvent_t* e : {&outReady, &errCopied, &reuseReady, &outDone})
+            CSG_CUDA_TRY(cudaStreamCreateWithFlags(&listStream, cudaStreamNonBlocking));
+            for (cudaEvent_t* e : {&outReady, &errCopied, &reuseReady, &outDone, &listCopied[0], &listCopied[1]})
                 CSG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
             CSG_CUDA_TRY(cudaHostAlloc(&herrHost, 4 * sizeof(uint32_t), cudaHostAllocDefault));
             CSG_CUDA_TRY(cudaHostAlloc(&listOverflowHost, sizeof(uint32_t), cudaHostAllocMapped));
@@ -809,32 +815,46 @@ struct Pipeline final : PipelineBase
             CSG_CUDA_TRY(
                 cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, d2hStream));
         const size_t devCap = listOffsets ? std::min(listCap, n * size_t(cfg.ngmax)) : 0;
+        const int b         = csrCur;
         if (listOffsets)
         {
-            // the stored neighbour indices compacted on the device (the next run may then overwrite the rows)
-            int rc = csrWs.ensure(neighborCsrWorkspaceBytes(n));
-            if (!rc) rc = csrOff.ensure((n + 1) * sizeof(uint64_t));
-            if (!rc) rc = csrList.ensure(std::max<size_t>(devCap, 4) * sizeof(uint32_t));
+            // the stored neighbour indices compacted on the device (the next run may then overwrite the rows), into
+            // buffer b once the copy out of it two calls ago has finished
+            // a buffer that grows is freed first: wait on the host for its last user
+            const size_t wsNeed = neighborCsrWorkspaceBytes(n), offNeed = (n + 1) * sizeof(uint64_t);
+            const size_t listNeed = std::max<size_t>(devCap, 4) * sizeof(uint32_t);
+            if (wsNeed > csrWs.bytes) CSG_CUDA_TRY(cudaStreamSynchronize(d2hStream));
+            if (listCopiedRec[b] && (offNeed > csrOff[b].bytes || listNeed > csrList[b].bytes))
+                CSG_CUDA_TRY(cudaEventSynchronize(listCopied[b]));
+            int rc = csrWs.ensure(wsNeed);
+            if (!rc) rc = csrOff[b].ensure(offNeed);
+            if (!rc) rc = csrList[b].ensure(listNeed);
             if (rc) return rc;
+            if (listCopiedRec[b]) CSG_CUDA_TRY(cudaStreamWaitEvent(d2hStream, listCopied[b], 0));
             if ((rc = neighborCsr(d2hStream, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax,
-                                  csrOff.as<uint64_t>(), csrList.as<uint32_t>(), devCap, csrWs.p, csrWs.bytes,
+                                  csrOff[b].as<uint64_t>(), csrList[b].as<uint32_t>(), devCap, csrWs.p, csrWs.bytes,
                                   nullptr)))
                 return rc;
         }
         CSG_CUDA_TRY(cudaEventRecord(reuseReady, d2hStream));
+        // everything after the compaction runs on listStream, in call order
+        CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, reuseReady, 0));
         if (listOffsets)
         {
-            // then to the caller's pinned buffers: the offsets by the copy engine, the list by 16-byte stores whose
+            // to the caller's pinned buffers: the offsets by the copy engine, the list by 16-byte stores whose
             // length the compaction left in device memory
-            CSG_CUDA_TRY(cudaMemcpyAsync(listOffsets, csrOff.p, (n + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost,
-                                         d2hStream));
+            CSG_CUDA_TRY(cudaMemcpyAsync(listOffsets, csrOff[b].p, (n + 1) * sizeof(uint64_t),
+                                         cudaMemcpyDeviceToHost, listStream));
             uint32_t* flag = nullptr;
             CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&flag), listOverflowHost, 0));
-            int rc = copyListToHost(d2hStream, csrList.as<uint32_t>(), listHost, csrOff.as<uint64_t>() + n,
+            int rc = copyListToHost(listStream, csrList[b].as<uint32_t>(), listHost, csrOff[b].as<uint64_t>() + n,
                                     listHost ? listCap : 0, flag);
             if (rc) return rc;
+            CSG_CUDA_TRY(cudaEventRecord(listCopied[b], listStream));
+            listCopiedRec[b] = true;
+            csrCur           = 1 - b;
         }
-        CSG_CUDA_TRY(cudaEventRecord(outDone, d2hStream));
+        CSG_CUDA_TRY(cudaEventRecord(outDone, listStream));
         outPending = true;
         return CS_OK;
     }

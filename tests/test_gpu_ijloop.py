@@ -88,3 +88,31 @@ def test_cluster_lists_reject_periodic_boxes(cs, O):
         cs.cluster_nblist(out["x"], out["y"], out["z"], out["h"], cs.make_box(0.0, 1.0, cs.PERIODIC), tree,
                           out["layout"], out["centers"].reshape(-1), out["sizes"].reshape(-1))
     assert e.value.code == cs.CS_ERR_INVALID
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+def test_cluster_density_screen_edge_cases(cs, O, dt):
+    """Pairs at 2 h_i to within a few ulps, far from the origin (where float coordinates carry an error of a tenth of
+    the lattice spacing): the loop's float screen may keep extra pairs but drops none that the exact test keeps."""
+    rng = np.random.default_rng(77)
+    s, off = 0.01, 3000.0
+    g = np.stack(np.meshgrid(np.arange(16), np.arange(16), np.arange(32), indexing="ij"), -1).reshape(-1, 3)
+    n = g.shape[0]
+    pos = off + s * g + rng.normal(0.0, 1e-13, g.shape)
+    x, y, z = (np.ascontiguousarray(pos[:, k]).astype(dt) for k in range(3))
+    # 2 h at a lattice distance (1, sqrt 2, sqrt 3, 2 spacings), nudged by a few ulps either way
+    base = s * np.sqrt(rng.choice([1.0, 2.0, 3.0, 4.0], n)) / 2
+    ulp = np.spacing(base.astype(dt)).astype(np.float64)
+    h = (base + rng.integers(-3, 4, n) * ulp).astype(dt)
+    m = rng.uniform(0.5, 1.5, n).astype(dt)
+    lo = (float(x.min()), float(y.min()), float(z.min()))
+    hi = (float(x.max()), float(y.max()), float(z.max()))
+    out, tree = _gpu_tree(cs, x, y, z, h, cs.make_box(lo, hi), 16, 0, 64 if dt == np.float64 else 32)
+    box = cs.make_box(lo, hi)
+    lists, counts = cs.cluster_nblist(out["x"], out["y"], out["z"], out["h"], box, tree, out["layout"],
+                                      out["centers"].reshape(-1), out["sizes"].reshape(-1), 64, 64)
+    tm = torch.from_numpy(m).cuda()[out["order"].long()]
+    rho = cs.ijloop_density_clusters(out["x"], out["y"], out["z"], out["h"], tm, lists, counts)
+    ref = O.ijloop_density_all(*(out[c].cpu().numpy() for c in ("x", "y", "z", "h")), tm.cpu().numpy(),
+                               O.make_box(lo, hi))
+    assert np.array_equal(rho.cpu().numpy(), ref)
