@@ -763,12 +763,13 @@ def main():
     pipe = cs.Pipeline(64, 64, cs.HILBERT, BUCKET, NGMAX, 1.0, 1.0, True, True)
     for _ in range(args.warmup):
         pipe.run(tx, ty, tz, th, box, FOCUS)
-    # the autotuner (part of the warm-up): each traversal tuning on the warm-up's inputs, the fastest kept
+    # the autotuner (part of the warm-up): each traversal tuning on the warm-up's inputs (scored by the neighbour
+    # stage), then each sort tile shape (scored by the sort stage), the fastest kept
     autotune = None
     if not args.no_autotune:
         pipe.run(tx, ty, tz, th, box, FOCUS)
         r = pipe.autotune(2)
-        autotune = {f"{c['nb_group']}/{c['nb_by_target_cost']}": round(ms, 3) for c, ms in r["tried"]}
+        autotune = {cs.tuning_label(c): round(ms, 3) for c, ms in r["tried"]}
     torch.cuda.synchronize()
 
     # ---- device-resident timed region ----
@@ -903,7 +904,7 @@ def main():
                 "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks.summary(),
                 "gpu_launches": None,
                 "stages_ms": {k: round(v, 4) for k, v in stages.items()},
-                "tuning": pipe.get_tuning(), "autotune_neighbors_ms": autotune,
+                "tuning": pipe.get_tuning(), "autotune_stage_ms": autotune,
                 "tree": {"leaves": res.num_leaves, "nodes": res.num_nodes, "iterations": res.iterations,
                          "max_depth": res.max_depth, "focus_leaves": res.focus_last - res.focus_first},
                 "mean_neighbors": round(mean_nc, 2), "h_converged_frac": float((hnc == K_NEIGHBORS).double().mean())}

@@ -64,7 +64,7 @@ __global__ void setRootsKernel(const uint64_t* __restrict__ prefixes, const int3
 struct BatchBase
 {
     cs_batch_config cfg{};
-    cs_tuning tuning{32, 7};
+    cs_tuning tuning{32, 7, 16};
     virtual ~BatchBase() = default;
     virtual int run(cudaStream_t s, const void* x, const void* y, const void* z, const void* h, const uint32_t* off,
                     int S, const cs_box* boxes, const uint32_t* buckets, cs_batch_result* res) = 0;
@@ -171,7 +171,7 @@ struct Batch final : BatchBase
         bool inAlt = false;
         rc = radixSortPairs<uint64_t>(s, keys.as<uint64_t>(), order.as<uint32_t>(), keysAlt.as<uint64_t>(),
                                       orderAlt.as<uint32_t>(), n, 0, keyBits, true, sortWs.p, sortWs.bytes, err,
-                                      &inAlt);
+                                      &inAlt, tuning.sort_items);
         if (rc) return rc;
         sortedKeys  = inAlt ? keysAlt.as<uint64_t>() : keys.as<uint64_t>();
         sortedOrder = inAlt ? orderAlt.as<uint32_t>() : order.as<uint32_t>();
@@ -377,9 +377,9 @@ extern "C" int cs_batch_destroy(cs_batch b)
 extern "C" int cs_batch_set_tuning(cs_batch b, const cs_tuning* t)
 {
     if (!b || !t || !(t->nb_group == 8 || t->nb_group == 16 || t->nb_group == 32) || t->nb_by_target_cost < 0 ||
-        t->nb_by_target_cost > 64)
+        t->nb_by_target_cost > 64 || !(t->sort_items == 0 || t->sort_items == 12 || t->sort_items == 16))
     {
-        setLastError("batch set tuning: nb_group must be 8, 16 or 32 and nb_by_target_cost in [0, 64]");
+        setLastError("batch set tuning: nb_group must be 8, 16 or 32, nb_by_target_cost in [0, 64], sort_items 0, 12 or 16");
         return CS_ERR_INVALID;
     }
     b->impl->tuning = *t;

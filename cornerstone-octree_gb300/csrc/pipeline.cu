@@ -153,7 +153,9 @@ struct Pipeline final : PipelineBase
             setLastError("autotune: needs a previous run with neighbours");
             return CS_ERR_INVALID;
         }
-        static constexpr cs_tuning candidates[] = {{32, 7}, {32, 0}, {32, 5}, {32, 10}, {16, 7}, {8, 7}};
+        static constexpr cs_tuning candidates[] = {{32, 7, 0}, {32, 0, 0}, {32, 5, 0}, {32, 10, 0}, {16, 7, 0},
+                                                   {8, 7, 0}};
+        static constexpr int sortCandidates[] = {16, 12};
         const void* in[4] = {lastIn[0], lastIn[1], lastIn[2], lastIn[3]};
         const size_t n0   = lastNIn;
         const cs_box box0 = lastBox;
@@ -162,31 +164,51 @@ struct Pipeline final : PipelineBase
         cs_tuning win        = keep;
         float winMs          = 0.f;
         int k                = 0;
-        for (const cs_tuning& c : candidates)
-        {
+        // mean device time of one stage [first, last) over reps runs with tuning c
+        auto score = [&](const cs_tuning& c, int first, int last, float& mean) -> int {
             tuning    = c;
             float acc = 0.f;
             for (int r = 0; r < std::max(1, reps); ++r)
             {
                 int rc = run(s, in[0], in[1], in[2], in[3], n0, box0, f0, f1, nullptr, false);
-                if (rc)
-                {
-                    tuning = keep;
-                    return rc;
-                }
+                if (rc) return rc;
                 float t = 0.f;
                 CSG_CUDA_TRY(cudaEventSynchronize(ev[ST_COUNT]));
-                CSG_CUDA_TRY(cudaEventElapsedTime(&t, ev[ST_NEIGHBORS], ev[ST_COUNT]));
+                CSG_CUDA_TRY(cudaEventElapsedTime(&t, ev[first], ev[last]));
                 acc += t;
             }
-            acc /= float(std::max(1, reps));
+            mean = acc / float(std::max(1, reps));
             if (k < capacity)
             {
                 if (tried) tried[k] = c;
-                if (ms) ms[k] = acc;
+                if (ms) ms[k] = mean;
             }
             ++k;
-            if (k == 1 || acc < winMs) win = c, winMs = acc;
+            return CS_OK;
+        };
+        for (cs_tuning c : candidates)
+        {
+            c.sort_items = keep.sort_items;
+            float t      = 0.f;
+            if (int rc = score(c, ST_NEIGHBORS, ST_COUNT, t))
+            {
+                tuning = keep;
+                return rc;
+            }
+            if (k == 1 || t < winMs) win = c, winMs = t;
+        }
+        float sortWin = 0.f;
+        for (int items : sortCandidates)
+        {
+            cs_tuning c  = win;
+            c.sort_items = items;
+            float t      = 0.f;
+            if (int rc = score(c, ST_SORT, ST_GATHER, t))
+            {
+                tuning = keep;
+                return rc;
+            }
+            if (items == sortCandidates[0] || t < sortWin) sortWin = t, win.sort_items = items;
         }
         tuning = win;
         if (best) *best = win;
@@ -282,7 +304,7 @@ struct Pipeline final : PipelineBase
         CSG_CUDA_TRY(rec(ev[ST_SORT]));
         bool inAlt = false;
         rc = radixSortPairs<K>(s, keys.as<K>(), order.as<uint32_t>(), keysAlt.as<K>(), orderAlt.as<uint32_t>(), nIn,
-                               0, keyBits, true, sortWs.p, sortWs.bytes, err, &inAlt);
+                               0, keyBits, true, sortWs.p, sortWs.bytes, err, &inAlt, tuning.sort_items);
         if (rc) return rc;
         sortedKeys  = inAlt ? keysAlt.as<K>() : keys.as<K>();
         sortedOrder = inAlt ? orderAlt.as<uint32_t>() : order.as<uint32_t>();
@@ -577,7 +599,7 @@ struct Pipeline final : PipelineBase
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_SORT], s));
         bool inAlt = false;
         rc = radixSortPairs<K>(s, keys.as<K>(), order.as<uint32_t>(), keysAlt.as<K>(), orderAlt.as<uint32_t>(), n, 0,
-                               keyBits, true, sortWs.p, sortWs.bytes, err, &inAlt);
+                               keyBits, true, sortWs.p, sortWs.bytes, err, &inAlt, tuning.sort_items);
         if (rc) return rc;
         sortedKeys  = inAlt ? keysAlt.as<K>() : keys.as<K>();
         sortedOrder = inAlt ? orderAlt.as<uint32_t>() : order.as<uint32_t>();
@@ -786,8 +808,12 @@ struct Pipeline final : PipelineBase
         }
         if (!d2hStream)
         {
-            CSG_CUDA_TRY(cudaStreamCreateWithFlags(&d2hStream, cudaStreamNonBlocking));
-            CSG_CUDA_TRY(cudaStreamCreateWithFlags(&listStream, cudaStreamNonBlocking));
+            // the highest priority: the block scheduler then places the compaction's and the list copy's blocks as
+            // soon as blocks of the next run's kernels retire, instead of after those kernels' last blocks
+            int lowPrio = 0, highPrio = 0;
+            CSG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lowPrio, &highPrio));
+            CSG_CUDA_TRY(cudaStreamCreateWithPriority(&d2hStream, cudaStreamNonBlocking, highPrio));
+            CSG_CUDA_TRY(cudaStreamCreateWithPriority(&listStream, cudaStreamNonBlocking, highPrio));
             for (cudaEvent_t* e : {&outReady, &errCopied, &reuseReady, &outDone, &listCopied[0], &listCopied[1]})
                 CSG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
             CSG_CUDA_TRY(cudaHostAlloc(&herrHost, 4 * sizeof(uint32_t), cudaHostAllocDefault));
@@ -1073,9 +1099,9 @@ extern "C" int cs_pipeline_wait(cs_pipeline p)
 extern "C" int cs_pipeline_set_tuning(cs_pipeline p, const cs_tuning* t)
 {
     if (!p || !t || !(t->nb_group == 8 || t->nb_group == 16 || t->nb_group == 32) || t->nb_by_target_cost < 0 ||
-        t->nb_by_target_cost > 64)
+        t->nb_by_target_cost > 64 || !(t->sort_items == 0 || t->sort_items == 12 || t->sort_items == 16))
     {
-        setLastError("set tuning: nb_group must be 8, 16 or 32 and nb_by_target_cost in [0, 64]");
+        setLastError("set tuning: nb_group must be 8, 16 or 32, nb_by_target_cost in [0, 64], sort_items 0, 12 or 16");
         return CS_ERR_INVALID;
     }
     p->impl->tuning = *t;

@@ -42,7 +42,7 @@ struct PipelineBase
     virtual int autotune(cudaStream_t s, int reps, cs_tuning* best, cs_tuning* tried, float* ms, int capacity,
                          int* count) = 0;
     int graphReplays = 0; // steps of the last step sequence that were replayed from a captured graph
-    cs_tuning tuning{32, 7};
+    cs_tuning tuning{32, 7, 16};
     cudaEvent_t ev[ST_COUNT + 1] = {};
     float stageMs[ST_COUNT]      = {};
     int lastN                    = 0;

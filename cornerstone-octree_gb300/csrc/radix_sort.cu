@@ -1,6 +1,7 @@
 // Stable LSD radix sort of (key, uint32 value) pairs: one histogram kernel for all digit positions, then one
 // "onesweep" kernel per 8-bit digit (Adinets & Merrill, "Onesweep: a faster least significant digit radix sort for
-// GPUs", 2022). Each block takes the next 4096-key tile from an atomic counter, ranks its keys by digit in input
+// GPUs", 2022). Each block takes the next tile (256 threads x 16 or 12 keys: a runtime choice, SortShape) from an
+// atomic counter, ranks its keys by digit in input
 // order (warp match + per-warp counters), publishes its per-digit counts and obtains the counts of all earlier tiles
 // by decoupled look-back, then scatters through shared memory so that global writes are runs of consecutive
 // addresses. Traffic per pass: 2 * (sizeof(K) + 4) bytes per pair; the histogram reads the keys once.
@@ -16,9 +17,8 @@ namespace csg
 {
 
 constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS   = 16;
-constexpr int RS_TILE    = RS_THREADS * RS_ITEMS;
 constexpr int RS_WARPS   = RS_THREADS / 32;
+constexpr int RS_MIN_TILE = RS_THREADS * 12; // the smaller of the two tile shapes sizes the workspace
 constexpr int RS_BINS    = 256;
 constexpr int RS_MAXPASS = 8;
 
@@ -40,11 +40,11 @@ struct SortLayout
 static inline int numPasses(int beginBit, int endBit) { return (endBit - beginBit + 7) / 8; }
 
 template<class K>
-static SortLayout sortLayout(Arena& a, size_t n, int beginBit, int endBit)
+static SortLayout sortLayout(Arena& a, size_t n, int beginBit, int endBit, int tile)
 {
     SortLayout L;
     L.passes      = numPasses(beginBit, endBit);
-    L.tiles       = (n + RS_TILE - 1) / RS_TILE;
+    L.tiles       = (n + tile - 1) / tile;
     L.hist        = a.take<uint32_t>(size_t(RS_MAXPASS) * RS_BINS);
     L.tileCounter = a.take<uint32_t>(RS_MAXPASS);
     L.status      = a.take<uint32_t>(size_t(L.passes) * L.tiles * RS_BINS + 1);
@@ -55,7 +55,7 @@ template<class K>
 size_t radixSortWorkspaceBytes(size_t n, int beginBit, int endBit)
 {
     Arena a;
-    sortLayout<K>(a, n, beginBit, endBit);
+    sortLayout<K>(a, n, beginBit, endBit, RS_MIN_TILE);
     return a.size + 256;
 }
 
@@ -136,8 +136,8 @@ __device__ __forceinline__ uint32_t blockExclusiveScan256(uint32_t v, uint32_t* 
     return warpPrefix + x - v;
 }
 
-template<class K, bool Iota>
-__global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restrict__ keysIn,
+template<class K, bool Iota, int Items, int MinBlocks>
+__global__ void __launch_bounds__(RS_THREADS, MinBlocks) onesweepKernel(const K* __restrict__ keysIn,
                                                              const uint32_t* __restrict__ valsIn,
                                                              K* __restrict__ keysOut, uint32_t* __restrict__ valsOut,
                                                              size_t n, int shift, uint32_t mask,
@@ -145,9 +145,10 @@ __global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restr
                                                              uint32_t* status, uint32_t* tileCounter,
                                                              uint32_t* errWord, uint32_t spinLimit, int stallTile1)
 {
+    constexpr int Tile = RS_THREADS * Items;
     extern __shared__ __align__(16) unsigned char smem[];
     K* sKeys        = reinterpret_cast<K*>(smem);
-    uint32_t* sVals = reinterpret_cast<uint32_t*>(smem + RS_TILE * sizeof(K));
+    uint32_t* sVals = reinterpret_cast<uint32_t*>(smem + Tile * sizeof(K));
 
     __shared__ uint32_t sWarpHist[RS_WARPS][RS_BINS];
     __shared__ uint32_t sTileOff[RS_BINS];
@@ -162,13 +163,13 @@ __global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restr
     __syncthreads();
 
     const uint32_t tile   = sTile;
-    const size_t tileBase = size_t(tile) * RS_TILE;
-    const size_t warpBase = tileBase + size_t(warp) * RS_ITEMS * 32;
+    const size_t tileBase = size_t(tile) * Tile;
+    const size_t warpBase = tileBase + size_t(warp) * Items * 32;
 
-    K k[RS_ITEMS];
-    uint32_t v[RS_ITEMS];
+    K k[Items];
+    uint32_t v[Items];
 #pragma unroll
-    for (int j = 0; j < RS_ITEMS; ++j)
+    for (int j = 0; j < Items; ++j)
     {
         size_t idx = warpBase + j * 32 + lane;
         if (idx < n)
@@ -184,10 +185,10 @@ __global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restr
     }
 
     // rank within the warp's 512-key sub-tile, in input order
-    uint32_t rank[RS_ITEMS];
+    uint32_t rank[Items];
     const unsigned ltMask = (1u << lane) - 1u;
 #pragma unroll
-    for (int j = 0; j < RS_ITEMS; ++j)
+    for (int j = 0; j < Items; ++j)
     {
         uint32_t d      = digitOf(k[j], shift, mask);
         unsigned peers  = __match_any_sync(0xffffffffu, d);
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restr
 
     // scatter into shared memory in (digit, input order) order
 #pragma unroll
-    for (int j = 0; j < RS_ITEMS; ++j)
+    for (int j = 0; j < Items; ++j)
     {
         uint32_t d   = digitOf(k[j], shift, mask);
         uint32_t pos = sTileOff[d] + sWarpHist[warp][d] + rank[j];
@@ -283,7 +284,7 @@ __global__ void __launch_bounds__(RS_THREADS, 3) onesweepKernel(const K* __restr
 
     // coalesced write-out: consecutive shared slots of one digit go to consecutive global positions
 #pragma unroll 4
-    for (int i = tid; i < RS_TILE; i += RS_THREADS)
+    for (int i = tid; i < Tile; i += RS_THREADS)
     {
         K key      = sKeys[i];
         uint32_t d = digitOf(key, shift, mask);
@@ -312,9 +313,46 @@ __global__ void histScanKernel(uint32_t* hist)
     h[threadIdx.x] = e;
 }
 
+// the onesweep passes with one tile shape (Items keys per thread, MinBlocks resident blocks per SM); on return kin /
+// vin point at the buffers holding the result
+template<class K, int Items, int MinBlocks>
+static int onesweepPasses(cudaStream_t s, K*& kin, uint32_t*& vin, K* keysAlt, uint32_t* valsAlt, size_t n,
+                          int beginBit, int endBit, bool iota, const SortLayout& L, uint32_t* err)
+{
+    const size_t smemBytes = size_t(RS_THREADS) * Items * (sizeof(K) + sizeof(uint32_t));
+    CSG_CUDA_TRY(cudaFuncSetAttribute(onesweepKernel<K, true, Items, MinBlocks>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smemBytes)));
+    CSG_CUDA_TRY(cudaFuncSetAttribute(onesweepKernel<K, false, Items, MinBlocks>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, int(smemBytes)));
+    const WaitLimits wl = waitLimits();
+    const int stall     = (wl.stall & CS_WAIT_STALL_SORT) ? 1 : 0;
+    K* kout             = keysAlt;
+    uint32_t* vout      = valsAlt;
+    for (int p = 0; p < L.passes; ++p)
+    {
+        int shift     = beginBit + 8 * p;
+        int bitsHere  = std::min(8, endBit - shift);
+        uint32_t mask = (1u << bitsHere) - 1u;
+        uint32_t* st  = L.status + size_t(p) * L.tiles * RS_BINS;
+        if (p == 0 && iota)
+            onesweepKernel<K, true, Items, MinBlocks><<<unsigned(L.tiles), RS_THREADS, smemBytes, s>>>(
+                kin, vin, kout, vout, n, shift, mask, L.hist + p * RS_BINS, st, L.tileCounter + p, err, wl.sortSpins,
+                stall);
+        else
+            onesweepKernel<K, false, Items, MinBlocks><<<unsigned(L.tiles), RS_THREADS, smemBytes, s>>>(
+                kin, vin, kout, vout, n, shift, mask, L.hist + p * RS_BINS, st, L.tileCounter + p, err, wl.sortSpins,
+                stall);
+        CSG_CHECK_LAUNCH();
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    return CS_OK;
+}
+
 template<class K>
 int radixSortPairs(cudaStream_t s, K* keys, uint32_t* vals, K* keysAlt, uint32_t* valsAlt, size_t n, int beginBit,
-                   int endBit, bool iota, void* ws, size_t wsBytes, uint32_t* errWord, bool* resultInAlt)
+                   int endBit, bool iota, void* ws, size_t wsBytes, uint32_t* errWord, bool* resultInAlt,
+                   int sortItems)
 {
     constexpr int KB = 8 * sizeof(K);
     if (beginBit < 0 || endBit > KB || beginBit > endBit)
@@ -341,8 +379,13 @@ int radixSortPairs(cudaStream_t s, K* keys, uint32_t* vals, K* keysAlt, uint32_t
         return CS_OK;
     }
 
+    if (sortItems != 0 && sortItems != 12 && sortItems != 16)
+    {
+        setLastError("sort: keys per thread must be 12 or 16 (0: the default, 16)");
+        return CS_ERR_INVALID;
+    }
     Arena a{static_cast<char*>(ws), 0, wsBytes};
-    SortLayout L = sortLayout<K>(a, n, beginBit, endBit);
+    SortLayout L = sortLayout<K>(a, n, beginBit, endBit, RS_THREADS * (sortItems == 12 ? 12 : 16));
     if (!a.ok())
     {
         setLastError("sort: workspace too small");
@@ -367,36 +410,12 @@ int radixSortPairs(cudaStream_t s, K* keys, uint32_t* vals, K* keysAlt, uint32_t
         CSG_CHECK_LAUNCH();
     }
 
-    size_t smemBytes = RS_TILE * (sizeof(K) + sizeof(uint32_t));
-    CSG_CUDA_TRY(cudaFuncSetAttribute(onesweepKernel<K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(smemBytes)));
-    CSG_CUDA_TRY(cudaFuncSetAttribute(onesweepKernel<K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      int(smemBytes)));
-
-    const WaitLimits wl = waitLimits();
-    const int stall     = (wl.stall & CS_WAIT_STALL_SORT) ? 1 : 0;
     K* kin        = keys;
     uint32_t* vin = vals;
-    K* kout       = keysAlt;
-    uint32_t* vout = valsAlt;
-    for (int p = 0; p < passes; ++p)
-    {
-        int shift     = beginBit + 8 * p;
-        int bitsHere  = std::min(8, endBit - shift);
-        uint32_t mask = (1u << bitsHere) - 1u;
-        uint32_t* st  = L.status + size_t(p) * L.tiles * RS_BINS;
-        if (p == 0 && iota)
-            onesweepKernel<K, true><<<unsigned(L.tiles), RS_THREADS, smemBytes, s>>>(
-                kin, vin, kout, vout, n, shift, mask, L.hist + p * RS_BINS, st, L.tileCounter + p, err, wl.sortSpins,
-                stall);
-        else
-            onesweepKernel<K, false><<<unsigned(L.tiles), RS_THREADS, smemBytes, s>>>(
-                kin, vin, kout, vout, n, shift, mask, L.hist + p * RS_BINS, st, L.tileCounter + p, err, wl.sortSpins,
-                stall);
-        CSG_CHECK_LAUNCH();
-        std::swap(kin, kout);
-        std::swap(vin, vout);
-    }
+    int rc        = sortItems == 12
+                        ? onesweepPasses<K, 12, 4>(s, kin, vin, keysAlt, valsAlt, n, beginBit, endBit, iota, L, err)
+                        : onesweepPasses<K, 16, 3>(s, kin, vin, keysAlt, valsAlt, n, beginBit, endBit, iota, L, err);
+    if (rc) return rc;
     bool inAlt = (kin == keysAlt);
     if (resultInAlt) { *resultInAlt = inAlt; }
     else if (inAlt)
@@ -414,8 +433,10 @@ int radixSortPreload()
     CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, radixHistogramKernel<K>));
     CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, histScanKernel));
     CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, iotaKernel));
-    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, onesweepKernel<K, true>));
-    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, onesweepKernel<K, false>));
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, onesweepKernel<K, true, 16, 3>));
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, onesweepKernel<K, false, 16, 3>));
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, onesweepKernel<K, true, 12, 4>));
+    CSG_CUDA_TRY(cudaFuncGetAttributes(&fa, onesweepKernel<K, false, 12, 4>));
     return CS_OK;
 }
 
@@ -424,9 +445,9 @@ template int radixSortPreload<uint64_t>();
 template size_t radixSortWorkspaceBytes<uint32_t>(size_t, int, int);
 template size_t radixSortWorkspaceBytes<uint64_t>(size_t, int, int);
 template int radixSortPairs<uint32_t>(cudaStream_t, uint32_t*, uint32_t*, uint32_t*, uint32_t*, size_t, int, int, bool,
-                                      void*, size_t, uint32_t*, bool*);
+                                      void*, size_t, uint32_t*, bool*, int);
 template int radixSortPairs<uint64_t>(cudaStream_t, uint64_t*, uint32_t*, uint64_t*, uint32_t*, size_t, int, int, bool,
-                                      void*, size_t, uint32_t*, bool*);
+                                      void*, size_t, uint32_t*, bool*, int);
 
 } // namespace csg
 

@@ -362,12 +362,18 @@ lib.cs_pipeline_device_bytes.argtypes = [C.c_void_p]
 
 
 class Tuning(C.Structure):
-    """speed knobs of the neighbour traversal (results do not depend on them): targets per warp (32, 16, 8) and the
-    by-target switch cost (0: never)"""
-    _fields_ = [("nb_group", C.c_int), ("nb_by_target_cost", C.c_int)]
+    """speed knobs (results do not depend on them): targets per warp of the neighbour traversal (32, 16, 8), its
+    by-target switch cost (0: never), and the key sort's keys per thread (16 or 12)"""
+    _fields_ = [("nb_group", C.c_int), ("nb_by_target_cost", C.c_int), ("sort_items", C.c_int)]
 
     def as_dict(self):
-        return {"nb_group": self.nb_group, "nb_by_target_cost": self.nb_by_target_cost}
+        return {"nb_group": self.nb_group, "nb_by_target_cost": self.nb_by_target_cost,
+                "sort_items": self.sort_items or 16}
+
+
+def tuning_label(t):
+    """'32/7/s16': targets per warp / by-target cost / sort keys per thread"""
+    return f"{t['nb_group']}/{t['nb_by_target_cost']}/s{t.get('sort_items', 16)}"
 
 
 lib.cs_pipeline_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
@@ -452,8 +458,8 @@ class Pipeline:
         _check(lib.cs_pipeline_stage_times(self.handle, ms, len(STAGES)))
         return dict(zip(STAGES, list(ms)))
 
-    def set_tuning(self, nb_group=32, nb_by_target_cost=7):
-        t = Tuning(nb_group, nb_by_target_cost)
+    def set_tuning(self, nb_group=32, nb_by_target_cost=7, sort_items=16):
+        t = Tuning(nb_group, nb_by_target_cost, sort_items)
         _check(lib.cs_pipeline_set_tuning(self.handle, C.byref(t)))
 
     def get_tuning(self):
@@ -462,8 +468,9 @@ class Pipeline:
         return t.as_dict()
 
     def autotune(self, reps=2):
-        """times the neighbour stage of the last run's inputs for each candidate tuning and keeps the fastest;
-        returns {"best": tuning, "tried": [(tuning, ms), ...]}"""
+        """reruns the last run's inputs for each candidate tuning (traversal candidates timed on the neighbour stage,
+        then sort tile shapes on the sort stage) and keeps the fastest; returns
+        {"best": tuning, "tried": [(tuning, ms), ...]}"""
         cap = 16
         best, tried, ms, count = Tuning(), (Tuning * cap)(), (C.c_float * cap)(), C.c_int()
         _check(lib.cs_pipeline_autotune(self.handle, _stream(), int(reps), C.byref(best), tried, ms, cap,
@@ -540,8 +547,8 @@ class Batch:
             lib.cs_batch_destroy(self.handle)
             self.handle = None
 
-    def set_tuning(self, nb_group=32, nb_by_target_cost=7):
-        t = Tuning(nb_group, nb_by_target_cost)
+    def set_tuning(self, nb_group=32, nb_by_target_cost=7, sort_items=16):
+        t = Tuning(nb_group, nb_by_target_cost, sort_items)
         _check(lib.cs_batch_set_tuning(self.handle, C.byref(t)))
 
     def run(self, x, y, z, h, offsets, boxes, buckets):

@@ -1,11 +1,12 @@
-"""Tuning table of the neighbour traversal: the autotuner's choices (``Pipeline.autotune``) keyed by coordinate
+"""Tuning table of the neighbour traversal and the key sort: the autotuner's choices (``Pipeline.autotune``) keyed by coordinate
 width, key width, particle count (power of two, rounded) and device name, stored as JSON. A tuning only changes the
 speed of a pipeline, never its results."""
 import json
 import math
 import os
 
-DEFAULT = {"nb_group": 32, "nb_by_target_cost": 7}
+DEFAULT = {"nb_group": 32, "nb_by_target_cost": 7, "sort_items": 16}
+FIELDS = ("nb_group", "nb_by_target_cost", "sort_items")
 
 
 def tuning_key(coord_bits, key_bits, n, device):
@@ -21,16 +22,17 @@ class TuningTable:
             with open(path) as f:
                 data = json.load(f)
             for key, e in data.get("entries", {}).items():
-                self.entries[key] = {"nb_group": int(e["nb_group"]), "nb_by_target_cost": int(e["nb_by_target_cost"]),
-                                     "ms": e.get("ms")}
+                # entries written before the sort shape was a knob take the default shape
+                self.entries[key] = {f: int(e.get(f, DEFAULT[f])) for f in FIELDS}
+                self.entries[key]["ms"] = e.get("ms")
 
     def lookup(self, key):
         e = self.entries.get(key)
-        return None if e is None else {"nb_group": e["nb_group"], "nb_by_target_cost": e["nb_by_target_cost"]}
+        return None if e is None else {f: e[f] for f in FIELDS}
 
     def store(self, key, tuning, ms=None):
-        self.entries[key] = {"nb_group": int(tuning["nb_group"]), "nb_by_target_cost": int(tuning["nb_by_target_cost"]),
-                             "ms": ms}
+        self.entries[key] = {f: int(tuning.get(f, DEFAULT[f])) for f in FIELDS}
+        self.entries[key]["ms"] = ms
 
     def save(self, path=None):
         path = path or self.path
@@ -48,6 +50,6 @@ def tune_pipeline(pipe, table, key, reps=2):
         pipe.set_tuning(**t)
         return t, None
     r = pipe.autotune(reps)
-    ms = dict((f"{c['nb_group']}/{c['nb_by_target_cost']}", m) for c, m in r["tried"])
+    ms = dict((f"{c['nb_group']}/{c['nb_by_target_cost']}/s{c['sort_items']}", m) for c, m in r["tried"])
     table.store(key, r["best"], ms)
     return r["best"], r["tried"]

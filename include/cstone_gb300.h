@@ -582,22 +582,28 @@ int cs_pipeline_graph_replays(cs_pipeline p);
  * nb_group: targets per warp of the neighbour traversal (32, 16 or 8; 1, 2 or 4 lanes per target).
  * nb_by_target_cost: with one target per lane, a candidate batch that few lanes need runs the by-target loop (lanes
  * hold the candidates, the warp loops over the needing targets) when 19 x (needing lanes) < nb_by_target_cost x (the
- * per-lane loop's candidate steps); 0 never. Default {32, 7}. Setting a tuning ends a step sequence (the next
- * cs_pipeline_step builds from the root). The reference has no counterpart: its traversal shape is the compile-time
- * TravConfig (traversal/find_neighbors.cuh:29-58). */
+ * per-lane loop's candidate steps); 0 never.
+ * sort_items: the key sort's tile shape, keys per thread (16 with 3 blocks of 256 threads per SM, or 12 with 4; 0
+ * means 16). Default {32, 7, 16}. Setting a tuning ends a step sequence (the next cs_pipeline_step builds from the
+ * root). The reference has no counterpart: its traversal shape is the compile-time TravConfig
+ * (traversal/find_neighbors.cuh:29-58), and its sort's tiles are CUB's compile-time policy
+ * (primitives/primitives_gpu.cu:322-356). */
 typedef struct
 {
     int nb_group;
     int nb_by_target_cost;
+    int sort_items;
 } cs_tuning;
 
 int cs_pipeline_set_tuning(cs_pipeline p, const cs_tuning* tuning);
 int cs_pipeline_get_tuning(cs_pipeline p, cs_tuning* tuning);
 /* Autotuner: reruns the inputs of the last cs_pipeline_run / cs_pipeline_run_host, when no cs_pipeline_step came
- * after it (device input arrays must still be valid), reps times for each candidate tuning ({32, 7}, {32, 0}, {32, 5}, {32, 10}, {16, 7}, {8, 7}), scores each by
- * the mean device time of the neighbour stage, and keeps the fastest as the pipeline's tuning. Writes the best, and
- * up to capacity candidates with their mean ms (tried / ms may be NULL); *count = candidates run. The outputs
- * afterwards are those of the last candidate's run (identical for every tuning). */
+ * after it (device input arrays must still be valid), reps times for each candidate tuning: first the traversal
+ * ({32, 7}, {32, 0}, {32, 5}, {32, 10}, {16, 7}, {8, 7}, scored by the mean device time of the neighbour stage), then,
+ * with the fastest of those, the sort's tile shapes (16 and 12 keys per thread, scored by the sort stage). Keeps the
+ * fastest as the pipeline's tuning. Writes the best, and up to capacity candidates with their mean ms of the stage
+ * that scored them (tried / ms may be NULL); *count = candidates run (8). The outputs afterwards are those of the
+ * last candidate's run (identical for every tuning). */
 int cs_pipeline_autotune(cs_pipeline p, cs_stream_t stream, int reps, cs_tuning* best, cs_tuning* tried, float* ms,
                          int capacity, int* count);
 

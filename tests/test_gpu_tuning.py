@@ -1,16 +1,17 @@
-"""GPU: the traversal tunings change the speed, never the results. Every candidate of the autotuner (targets per
-warp 32 / 16 / 8, by-target switch cost 0 / 5 / 7 / 10) gives neighbour counts and lists identical to the default,
-which equal the oracle's; the autotuner keeps one of its candidates; invalid tunings are refused; the batched path
-with another tuning gives the same results."""
+"""GPU: the tunings change the speed, never the results. Every candidate of the autotuner (targets per warp 32 / 16 /
+8, by-target switch cost 0 / 5 / 7 / 10, sort tiles of 16 or 12 keys per thread) gives sorted keys, neighbour counts
+and lists identical to the default, which equal the oracle's; the autotuner keeps one of its candidates; invalid
+tunings are refused; the batched path with another tuning gives the same results."""
 import numpy as np
 import pytest
 import torch
 
-from gpu_util import neighbor_lists_equal, to_dev, u32
+from gpu_util import keys_u, neighbor_lists_equal, to_dev, u32
 
 pytestmark = pytest.mark.gpu
 
 CANDIDATES = [(32, 7), (32, 0), (32, 5), (32, 10), (16, 7), (8, 7)]
+SORT_ITEMS = [16, 12]
 
 
 def _inputs(O, case):
@@ -45,10 +46,17 @@ def test_every_tuning_gives_the_same_neighbours(cs, O, case):
     neighbor_lists_equal(nb0.reshape(-1, ngmax), nc0, ref["nb"], ref["nc"], ngmax)
     for g, c in CANDIDATES:
         pipe.set_tuning(g, c)
-        assert pipe.get_tuning() == {"nb_group": g, "nb_by_target_cost": c}
+        assert pipe.get_tuning() == {"nb_group": g, "nb_by_target_cost": c, "sort_items": 16}
         nc, nb = _run(cs, pipe, t, box)
         assert np.array_equal(nc, nc0), (g, c)
         neighbor_lists_equal(nb.reshape(-1, ngmax), nc, nb0.reshape(-1, ngmax), nc0, ngmax)
+    pipe.set_tuning(32, 7, 12)
+    nc, nb = _run(cs, pipe, t, box)
+    out = pipe.outputs()
+    assert np.array_equal(keys_u(out["sorted_keys"]), np.asarray(ref["sorted_keys"], np.uint64))
+    assert np.array_equal(u32(out["order"]), ref["perm"])
+    assert np.array_equal(nc, nc0)
+    neighbor_lists_equal(nb.reshape(-1, ngmax), nc, nb0.reshape(-1, ngmax), nc0, ngmax)
 
 
 def test_autotune_keeps_a_candidate_and_the_results(cs, O):
@@ -60,10 +68,16 @@ def test_autotune_keeps_a_candidate_and_the_results(cs, O):
     nc0, nb0 = _run(cs, pipe, t, box)
     r = pipe.autotune(2)
     tried = [(c["nb_group"], c["nb_by_target_cost"]) for c, _ in r["tried"]]
-    assert tried == CANDIDATES and all(ms > 0 for _, ms in r["tried"])
+    nbt = len(CANDIDATES)
+    # the traversal candidates with the default sort shape, then the sort shapes with the fastest traversal
+    assert tried[:nbt] == CANDIDATES and all(ms > 0 for _, ms in r["tried"])
+    assert [c["sort_items"] for c, _ in r["tried"][:nbt]] == [16] * nbt
+    assert [c["sort_items"] for c, _ in r["tried"][nbt:]] == SORT_ITEMS
     assert r["best"] in [c for c, _ in r["tried"]] and pipe.get_tuning() == r["best"]
-    assert min(ms for _, ms in r["tried"]) == dict((tuple(c.values()), ms) for c, ms in r["tried"])[
-        (r["best"]["nb_group"], r["best"]["nb_by_target_cost"])]
+    fastest_nb = min(r["tried"][:nbt], key=lambda cm: cm[1])[0]
+    assert (r["best"]["nb_group"], r["best"]["nb_by_target_cost"]) == (fastest_nb["nb_group"],
+                                                                      fastest_nb["nb_by_target_cost"])
+    assert r["best"]["sort_items"] == min(r["tried"][nbt:], key=lambda cm: cm[1])[0]["sort_items"]
     out = pipe.outputs()
     torch.cuda.synchronize()
     assert np.array_equal(u32(out["neighbor_counts"]), nc0)
@@ -74,10 +88,10 @@ def test_autotune_keeps_a_candidate_and_the_results(cs, O):
 
 def test_invalid_tunings_are_refused(cs):
     pipe = cs.Pipeline(64, 64, cs.HILBERT, 64, 100, 1.0, 1.0, False, True)
-    for g, c in [(4, 7), (64, 7), (32, -1), (32, 65)]:
+    for g, c, s in [(4, 7, 16), (64, 7, 16), (32, -1, 16), (32, 65, 16), (32, 7, 8), (32, 7, 24)]:
         with pytest.raises(cs.CsError):
-            pipe.set_tuning(g, c)
-    assert pipe.get_tuning() == {"nb_group": 32, "nb_by_target_cost": 7}
+            pipe.set_tuning(g, c, s)
+    assert pipe.get_tuning() == {"nb_group": 32, "nb_by_target_cost": 7, "sort_items": 16}
     with pytest.raises(cs.CsError):
         pipe.autotune(1)  # no previous run
 
@@ -91,7 +105,7 @@ def test_batch_with_another_tuning_gives_the_same_results(cs, O):
     tx, ty, tz, th = to_dev(x, y, z, h)
     boxes = [cs.make_box(0.0, 1.0) for _ in sets]
     outs = []
-    for tuning in [(32, 7), (16, 7), (32, 0)]:
+    for tuning in [(32, 7, 16), (16, 7, 16), (32, 0, 12)]:
         b = cs.Batch(32, cs.MORTON, 64)
         b.set_tuning(*tuning)
         b.run(tx, ty, tz, th, offsets, boxes, [16] * len(sets))
