@@ -280,9 +280,9 @@ __global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuild
 // within the lane's 8-lane segment):
 //  - screen: every candidate j of the lane's target is tested in FP32; the ones that may lie within 2 h_i go, in
 //    ascending j, into the lane's queue in shared memory;
-//  - flush (when a queue may not take another j-cluster, and at the end): every lane runs its own queue through the
-//    exact test and the interaction, so the lanes of a warp do the expensive arithmetic on their own pairs instead of
-//    all lanes following the few that accept each candidate.
+//  - flush (when a queue may not take another j-cluster, and at the end): the queued pairs of all 32 lanes are dealt
+//    out 32 at a time, each lane evaluating the exact test and the interaction term of one pair (of any target), so
+//    that no lane idles in the expensive arithmetic; then each target adds its own terms in queue order.
 // For float coordinates the screen is the exact test itself. For double coordinates it is a proven lower bound:
 // with xf = float(x) (round to nearest), a = |float(xi_f - xj_f)| and S = |xi_f| + |xj_f|,
 //   |xi - xj| >= a (1 - 2^-24) - 2^-24 S - 2^-149,
@@ -293,6 +293,19 @@ __global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuild
 // raised to 2^-100 so that subnormal roundings cannot matter. The sums are those of the one-phase loop, bit for bit.
 constexpr int DC_WARPS = 4;
 constexpr int DC_QCAP  = 32; // queued candidates per target; a j-cluster adds at most CLUSTER
+
+template<class T>
+__device__ __forceinline__ unsigned long long toBits(T v)
+{
+    if constexpr (std::is_same_v<T, double>) return static_cast<unsigned long long>(__double_as_longlong(v));
+    else return __float_as_uint(v);
+}
+template<class T>
+__device__ __forceinline__ T fromBits(unsigned long long b)
+{
+    if constexpr (std::is_same_v<T, double>) return __longlong_as_double(static_cast<long long>(b));
+    else return __uint_as_float(uint32_t(b));
+}
 
 template<class T>
 __device__ __forceinline__ float toFloatRn(T v)
@@ -318,7 +331,7 @@ __global__ void __launch_bounds__(DC_WARPS * 32) densityClusterKernel(const T* _
                                                                       unsigned ncmax, T* __restrict__ rho)
 {
     constexpr bool kExactScreen = std::is_same_v<T, float>;
-    __shared__ uint32_t sQueue[DC_WARPS][DC_QCAP][32];
+    __shared__ unsigned long long sQueue[DC_WARPS][DC_QCAP][32]; // a queued j, then its term
     using R            = RN<T>;
     const int lane     = threadIdx.x & 31;
     const int warp     = threadIdx.x >> 5;
@@ -339,21 +352,48 @@ __global__ void __launch_bounds__(DC_WARPS * 32) densityClusterKernel(const T* _
     float thr = 0.f;
     if constexpr (!kExactScreen) thr = fmaxf(__fmul_ru(__double2float_ru(r2), 1.f + 0x1p-20f), 0x1p-100f);
 
-    uint32_t(*queue)[32] = sQueue[warp];
-    unsigned qn          = 0;
-    auto flush           = [&]() {
-        const unsigned qmax = __reduce_max_sync(0xffffffffu, qn);
-        __syncwarp();
-        for (unsigned s = 0; s < qmax; ++s)
+    unsigned long long(*queue)[32] = sQueue[warp];
+    unsigned qn                    = 0;
+    auto flush                     = [&]() {
+        // (1) every queued pair's term, the warp's queues taken 32 pairs at a time in lane-major order, so that all
+        //     lanes evaluate the expensive part; a term replaces its j in the queue (-0 where d2 >= r2: adding -0
+        //     leaves every sum unchanged)
+        unsigned incl = qn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
         {
-            if (s < qn)
+            const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+        const unsigned excl  = incl - qn;
+        __syncwarp();
+        for (unsigned e0 = 0; e0 < total; e0 += 32)
+        {
+            const unsigned e = e0 + lane;
+            // the pair's owner: the last lane whose queue starts at or before e (its queue is not empty)
+            int owner = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (__shfl_sync(0xffffffffu, excl, owner + step) <= e) owner += step;
+            const unsigned slot = e - __shfl_sync(0xffffffffu, excl, owner);
+            const T oxi = __shfl_sync(0xffffffffu, xi, owner), oyi = __shfl_sync(0xffffffffu, yi, owner);
+            const T ozi = __shfl_sync(0xffffffffu, zi, owner), ohinv = __shfl_sync(0xffffffffu, hinv, owner);
+            const T or2 = __shfl_sync(0xffffffffu, r2, owner);
+            if (e < total)
             {
-                const uint32_t j = queue[s][lane];
-                T dx = R::sub(xi, __ldg(x + j)), dy = R::sub(yi, __ldg(y + j)), dz = R::sub(zi, __ldg(z + j));
+                const uint32_t j = uint32_t(queue[slot][owner]);
+                T dx = R::sub(oxi, __ldg(x + j)), dy = R::sub(oyi, __ldg(y + j)), dz = R::sub(ozi, __ldg(z + j));
                 T d2 = R::add(R::add(R::mul(dx, dx), R::mul(dy, dy)), R::mul(dz, dz));
-                if (d2 < r2) sum = R::add(sum, R::mul(__ldg(m + j), densityW<T>(d2, hinv)));
+                T term = d2 < or2 ? R::mul(__ldg(m + j), densityW<T>(d2, ohinv)) : T(-0.0);
+                queue[slot][owner] = toBits<T>(term);
             }
         }
+        __syncwarp();
+        // (2) each target adds its own terms in queue order (ascending j)
+        const unsigned qmax = __reduce_max_sync(0xffffffffu, qn);
+        for (unsigned k = 0; k < qmax; ++k)
+            if (k < qn) sum = R::add(sum, fromBits<T>(queue[k][lane]));
         __syncwarp();
         qn = 0;
     };

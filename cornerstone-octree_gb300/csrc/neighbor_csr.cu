@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(CSR_THREADS) csrWriteKernel(const uint32_t* __
 // link runs at its copy-engine rate this way; 4-byte stores at unaligned row offsets reach about half of it). The
 // length comes from device memory, so the copy needs no host synchronisation. src is 16-byte aligned; the first few
 // entries bring dst to a 16-byte boundary. A total above the capacity sets *overflow (when given).
-__global__ void __launch_bounds__(256) copyListKernel(const uint32_t* __restrict__ src, uint32_t* dst,
+__global__ void __launch_bounds__(256, 5) copyListKernel(const uint32_t* __restrict__ src, uint32_t* dst,
                                                       const uint64_t* __restrict__ total, size_t capacity,
                                                       uint32_t* overflow)
 {
@@ -160,25 +160,28 @@ __global__ void __launch_bounds__(256) copyListKernel(const uint32_t* __restrict
         const size_t tail0 = head + 4 * nv;
         if (tail0 + threadIdx.x < m) dst[tail0 + threadIdx.x] = src[tail0 + threadIdx.x];
     }
-    const uint4* s4 = reinterpret_cast<const uint4*>(src + head);
-    uint4* d4       = reinterpret_cast<uint4*>(dst + head);
     // four loads in flight per thread before their stores: the host link needs about 1 MB of stores in flight, and
     // the loads' latency grows while other kernels share the device
-    constexpr int U     = 4;
-    const size_t stride = size_t(gridDim.x) * blockDim.x;
-    size_t i            = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    for (; i + (U - 1) * stride < nv; i += U * stride)
+    constexpr int U        = 4;
+    const unsigned stride  = gridDim.x * blockDim.x;
+    const unsigned tid     = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint4* sp        = reinterpret_cast<const uint4*>(src + head) + tid;
+    uint4* dp              = reinterpret_cast<uint4*>(dst + head) + tid;
+    size_t left            = nv > tid ? (nv - tid + stride - 1) / stride : 0; // this thread's 16-byte words
+    for (; left >= U; left -= U)
     {
         uint4 r[U];
 #pragma unroll
         for (int u = 0; u < U; ++u)
-            r[u] = __ldcs(s4 + i + u * stride);
+            r[u] = __ldcs(sp + u * stride);
 #pragma unroll
         for (int u = 0; u < U; ++u)
-            d4[i + u * stride] = r[u];
+            dp[u * stride] = r[u];
+        sp += U * stride;
+        dp += U * stride;
     }
-    for (; i < nv; i += stride)
-        d4[i] = __ldcs(s4 + i);
+    for (; left > 0; --left, sp += stride, dp += stride)
+        *dp = __ldcs(sp);
 }
 
 int copyListToHost(cudaStream_t s, const uint32_t* src, uint32_t* dst, const uint64_t* totalDev, size_t capacity,
@@ -190,7 +193,9 @@ int copyListToHost(cudaStream_t s, const uint32_t* src, uint32_t* dst, const uin
         setLastError("list copy: null or misaligned pointer");
         return CS_ERR_INVALID;
     }
-    // 64 blocks saturate the host link (measured) while leaving the SMs to the next run's kernels
+    // 64 blocks saturate the host link (measured) while leaving the SMs to the next run's kernels. Each block is
+    // small (256 threads, at most 51 registers each): it fits beside a full share of the cooperative build's blocks,
+    // whose launch waits until all of its blocks can be resident
     copyListKernel<<<64, 256, 0, s>>>(src, dst, totalDev, capacity, overflow);
     CSG_CHECK_LAUNCH();
     return CS_OK;
