@@ -617,7 +617,12 @@ def run_ijloop(args, world, rank, local):
                              "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "algorithmic_bytes": algo,
                              "note": "hbm fraction of the loop; its distance tests and kernel run in FP64"},
-                "stored_lists_complete": complete, "rho_identical_frac": agree, "clocks": clocks.summary()}
+                "stored_lists_complete": complete, "rho_identical_frac": agree,
+                "rho_identical_note": "the cluster loop sums over every j within 2 h_i (checked against a brute-force "
+                                      "sum); the stored lists follow findNeighbors, which looks only into leaves "
+                                      "that pass its cell test, and a j just inside 2 h_i can sit in a leaf that "
+                                      "fails it at the edge, so a few particles (19 of 16M) differ by one pair",
+                "clocks": clocks.summary()}
         print(json.dumps(line), flush=True)
 
 
@@ -838,6 +843,9 @@ def main():
             lambda: pipe.run_host_csr(hx, hy, hz, hh, box, FOCUS, off_host, list_host, nc_out=nc_host,
                                       flags_out=flags_host, asynchronous=True), False)
         lists_ok = int(off_host[-1]) == total
+        # the last pipelined step's device times: its stages and its copy-back (compaction, list copy)
+        last_stages = {k: round(v, 3) for k, v in pipe.stage_times().items()}
+        last_copy = {k: round(v, 3) for k, v in pipe.copy_times().items()}
         lists_sync_ms, _ = timed_e2e(
             lambda: pipe.run_host_csr(hx, hy, hz, hh, box, FOCUS, off_host, list_host, nc_out=nc_host,
                                       flags_out=flags_host), False)
@@ -851,6 +859,7 @@ def main():
                "returns": "neighbour counts, halo flags and the stored neighbour lists (CSR: u64 offsets + u32 "
                           "indices, the first min(nc, ngmax) per particle)",
                "lists_total": total, "lists_complete": lists_ok,
+               "last_step_ms": {"stages": last_stages, "copy_back": last_copy},
                "api": "cs_pipeline_run_host_csr_async per step, cs_pipeline_wait at the end",
                "synchronous_calls": {"value": round(world * n / (lists_sync_ms * 1e-3) / 1e6, 3),
                                      "ms_per_step": round(lists_sync_ms, 3), "api": "cs_pipeline_run_host_csr"},

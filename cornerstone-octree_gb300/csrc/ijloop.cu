@@ -9,10 +9,11 @@
 //
 // 2. Over cluster-pair lists (the role of the reference's supercluster lists, traversal/ijloop/
 //    gpu_superclusternblist.cuh and gpu_superclusternblist/{build,loop}.cuh, built differently here). Particles are
-//    cut into clusters of 8 consecutive (SFC-ordered) particles. For each i-cluster a warp walks the octree with the
-//    cluster's search box (the union of its particles' 2h boxes, rounded outwards to float and widened by one finest
-//    cell, which covers particles that lie slightly outside their leaf's box) and lists, in ascending order and
-//    without repeats, every j-cluster whose float bounding box meets it; capacity ncmax j-clusters per i-cluster.
+//    cut into clusters of 8 consecutive (SFC-ordered) particles. An i-cluster's search box is the union of its
+//    particles' 2h boxes, rounded outwards to float and widened by one finest cell (which covers particles that lie
+//    slightly outside their leaf's box). A warp walks the octree once for 4 consecutive i-clusters, with the union of
+//    their search boxes, and lists for each, in ascending order and without repeats, every j-cluster whose float
+//    bounding box meets its own search box; capacity ncmax j-clusters per i-cluster.
 //    The loop then runs 4 i-clusters per warp, one target per lane: each j-cluster's 8 particles are loaded by the 8
 //    lanes of the segment and broadcast with shuffles, so every target adds its neighbours in ascending j. The list is
 //    a superset of the neighbours of every target, so the sum equals the brute-force sum over all j with
@@ -143,6 +144,7 @@ __global__ void jClusterBoxKernel(const T* __restrict__ x, const T* __restrict__
 }
 
 constexpr int CB_WARPS = 4;
+constexpr int CB_GROUP = 4; // i-clusters per warp
 constexpr int CB_STACK = 192;
 
 template<class T>
@@ -162,18 +164,21 @@ struct ClusterBuildArgs
     uint32_t* err; // bit 0: a list overflowed ncmax; bit 1: traversal stack overflow
 };
 
+// One warp builds the lists of CB_GROUP consecutive i-clusters (lane 8 g + k holds particle k of i-cluster g): one
+// tree walk with the union of their search boxes, and at each reached leaf every j-cluster box tested against each
+// i-cluster's own box.
 template<class T>
 __global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuildArgs<T> a)
 {
     __shared__ int sStack[CB_WARPS][CB_STACK];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const size_t ic = size_t(blockIdx.x) * CB_WARPS + warp;
-    if (ic >= a.numIClusters) return;
+    const int lane   = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t ic0 = (size_t(blockIdx.x) * CB_WARPS + warp) * CB_GROUP;
+    if (ic0 >= a.numIClusters) return;
 
-    // the cluster's search box: union over its particles of [x - 2h, x + 2h], rounded outwards, plus the margin
+    // each i-cluster's search box: union over its particles of [x - 2h, x + 2h], rounded outwards, plus the margin
     float blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    const size_t i = ic * CLUSTER + lane;
-    if (lane < CLUSTER && i < a.n)
+    const size_t i = ic0 * CLUSTER + lane;
+    if (i < a.n)
     {
         T p[3]  = {a.x[i], a.y[i], a.z[i]};
         float r = toFloatRu<T>(RN<T>::mul(T(2), a.h[i]));
@@ -184,16 +189,26 @@ __global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuild
             bhi[k] = __fadd_ru(toFloatRu<T>(p[k]), r);
         }
     }
+    float glo[CB_GROUP][3], ghi[CB_GROUP][3], ulo[3], uhi[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
     {
-        for (int o = 16; o > 0; o >>= 1)
+        for (int o = CLUSTER / 2; o > 0; o >>= 1)
         {
             blo[k] = fminf(blo[k], __shfl_xor_sync(0xffffffffu, blo[k], o));
             bhi[k] = fmaxf(bhi[k], __shfl_xor_sync(0xffffffffu, bhi[k], o));
         }
         blo[k] = __fsub_rd(blo[k], a.margin[k]);
         bhi[k] = __fadd_ru(bhi[k], a.margin[k]);
+        ulo[k] = INFINITY, uhi[k] = -INFINITY;
+#pragma unroll
+        for (int g = 0; g < CB_GROUP; ++g)
+        {
+            glo[g][k] = __shfl_sync(0xffffffffu, blo[k], g * CLUSTER);
+            ghi[g][k] = __shfl_sync(0xffffffffu, bhi[k], g * CLUSTER);
+            ulo[k]    = fminf(ulo[k], glo[g][k]);
+            uhi[k]    = fmaxf(uhi[k], ghi[g][k]);
+        }
     }
 
     auto nodeMeets = [&](int node) {
@@ -202,19 +217,21 @@ __global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuild
         for (int k = 0; k < 3; ++k)
         {
             T c      = a.centers[3 * size_t(node) + k];
-            T s      = a.sizes[3 * size_t(node) + k];
-            float lo = __fsub_rd(__fsub_rd(toFloatRd<T>(c), toFloatRu<T>(s)), a.margin[k]);
-            float hi = __fadd_ru(__fadd_ru(toFloatRu<T>(c), toFloatRu<T>(s)), a.margin[k]);
-            meet     = meet && lo <= bhi[k] && blo[k] <= hi;
+            T sz     = a.sizes[3 * size_t(node) + k];
+            float lo = __fsub_rd(__fsub_rd(toFloatRd<T>(c), toFloatRu<T>(sz)), a.margin[k]);
+            float hi = __fadd_ru(__fadd_ru(toFloatRu<T>(c), toFloatRu<T>(sz)), a.margin[k]);
+            meet     = meet && lo <= uhi[k] && ulo[k] <= hi;
         }
         return meet;
     };
 
-    uint32_t* list = a.lists + ic * size_t(a.ncmax);
-    unsigned count = 0;
-    long long lastJ = -1;
-    int* stack      = sStack[warp];
-    int top         = 0;
+    unsigned count[CB_GROUP] = {};
+    long long lastJ[CB_GROUP];
+#pragma unroll
+    for (int g = 0; g < CB_GROUP; ++g)
+        lastJ[g] = -1;
+    int* stack = sStack[warp];
+    int top    = 0;
     if (nodeMeets(0))
     {
         if (lane == 0) stack[0] = 0;
@@ -229,29 +246,33 @@ __global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuild
         if (c0 == 0)
         {
             // a leaf: its particles' j-clusters, tested 32 at a time, appended in ascending order without repeats
-            const int leaf     = a.internalToLeaf[node];
-            const uint32_t pf  = a.layout[leaf], pl = a.layout[leaf + 1];
+            const int leaf    = a.internalToLeaf[node];
+            const uint32_t pf = a.layout[leaf], pl = a.layout[leaf + 1];
             if (pl > pf)
             {
                 const long long J0 = pf / CLUSTER, J1 = (pl - 1) / CLUSTER;
                 for (long long Jb = J0; Jb <= J1; Jb += 32)
                 {
                     const long long J = Jb + lane;
-                    bool hit          = false;
-                    if (J <= J1 && J != lastJ)
+                    float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0.f), hi = make_float4(-INFINITY, -INFINITY,
+                                                                                                -INFINITY, 0.f);
+                    if (J <= J1) lo = a.jBoxes[2 * J], hi = a.jBoxes[2 * J + 1];
+#pragma unroll
+                    for (int g = 0; g < CB_GROUP; ++g)
                     {
-                        float4 lo = a.jBoxes[2 * J], hi = a.jBoxes[2 * J + 1];
-                        hit = lo.x <= bhi[0] && blo[0] <= hi.x && lo.y <= bhi[1] && blo[1] <= hi.y &&
-                              lo.z <= bhi[2] && blo[2] <= hi.z;
+                        const bool hit = J != lastJ[g] && lo.x <= ghi[g][0] && glo[g][0] <= hi.x &&
+                                         lo.y <= ghi[g][1] && glo[g][1] <= hi.y && lo.z <= ghi[g][2] &&
+                                         glo[g][2] <= hi.z;
+                        const unsigned m = __ballot_sync(0xffffffffu, hit);
+                        if (hit)
+                        {
+                            const unsigned pos = count[g] + __popc(m & ((1u << lane) - 1u));
+                            if (pos < a.ncmax && ic0 + g < a.numIClusters)
+                                a.lists[(ic0 + g) * size_t(a.ncmax) + pos] = uint32_t(J);
+                        }
+                        count[g] += __popc(m);
+                        if (m) lastJ[g] = Jb + 31 - __clz(m);
                     }
-                    const unsigned m = __ballot_sync(0xffffffffu, hit);
-                    if (hit)
-                    {
-                        unsigned pos = count + __popc(m & ((1u << lane) - 1u));
-                        if (pos < a.ncmax) list[pos] = uint32_t(J);
-                    }
-                    count += __popc(m);
-                    if (m) lastJ = Jb + 31 - __clz(m);
                 }
             }
             continue;
@@ -269,11 +290,13 @@ __global__ void __launch_bounds__(CB_WARPS * 32) clusterBuildKernel(ClusterBuild
         top += __popc(m);
         __syncwarp();
     }
-    if (lane == 0)
-    {
-        a.counts[ic] = count;
-        if (count > a.ncmax) atomicOr(a.err, 1u);
-    }
+#pragma unroll
+    for (int g = 0; g < CB_GROUP; ++g)
+        if (lane == g && ic0 + g < a.numIClusters)
+        {
+            a.counts[ic0 + g] = count[g];
+            if (count[g] > a.ncmax) atomicOr(a.err, 1u);
+        }
 }
 
 // The cluster loop in two phases per warp (4 i-clusters, one target per lane; each j-cluster's particles are broadcast
@@ -542,7 +565,7 @@ int clusterBuild(cudaStream_t s, const T* x, const T* y, const T* z, const T* h,
     a.lists  = lists;
     a.counts = counts;
     a.err    = err;
-    clusterBuildKernel<T><<<iceil(nic, CB_WARPS), CB_WARPS * 32, 0, s>>>(a);
+    clusterBuildKernel<T><<<iceil(nic, CB_WARPS * CB_GROUP), CB_WARPS * 32, 0, s>>>(a);
     CSG_CHECK_LAUNCH();
     uint32_t herr = 0;
     CSG_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));

@@ -79,6 +79,8 @@ struct Pipeline final : PipelineBase
     cudaStream_t d2hStream = nullptr, listStream = nullptr;
     cudaEvent_t outReady = nullptr, errCopied = nullptr, reuseReady = nullptr, outDone = nullptr;
     cudaEvent_t listCopied[2]  = {};  // on listStream after the copy out of compaction buffer b
+    cudaEvent_t cbEv[4]        = {};  // timing: compaction start / end, list copy start / end (cs_pipeline_copy_times)
+    bool cbTimed               = false;
     bool listCopiedRec[2]      = {false, false};
     int csrCur                 = 0;
     uint32_t* herrHost         = nullptr; // pinned, the last copied error words
@@ -114,7 +116,8 @@ struct Pipeline final : PipelineBase
             if (e) cudaEventDestroy(e);
         if (d2hStream) cudaStreamDestroy(d2hStream);
         if (listStream) cudaStreamDestroy(listStream);
-        for (cudaEvent_t e : {outReady, errCopied, reuseReady, outDone, listCopied[0], listCopied[1]})
+        for (cudaEvent_t e : {outReady, errCopied, reuseReady, outDone, listCopied[0], listCopied[1], cbEv[0], cbEv[1],
+                              cbEv[2], cbEv[3]})
             if (e) cudaEventDestroy(e);
         if (herrHost) cudaFreeHost(herrHost);
         if (listOverflowHost) cudaFreeHost(listOverflowHost);
@@ -816,6 +819,8 @@ struct Pipeline final : PipelineBase
             CSG_CUDA_TRY(cudaStreamCreateWithPriority(&listStream, cudaStreamNonBlocking, highPrio));
             for (cudaEvent_t* e : {&outReady, &errCopied, &reuseReady, &outDone, &listCopied[0], &listCopied[1]})
                 CSG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+            for (cudaEvent_t& e : cbEv)
+                CSG_CUDA_TRY(cudaEventCreate(&e));
             CSG_CUDA_TRY(cudaHostAlloc(&herrHost, 4 * sizeof(uint32_t), cudaHostAllocDefault));
             CSG_CUDA_TRY(cudaHostAlloc(&listOverflowHost, sizeof(uint32_t), cudaHostAllocMapped));
             *listOverflowHost = 0;
@@ -857,16 +862,19 @@ struct Pipeline final : PipelineBase
             if (!rc) rc = csrList[b].ensure(listNeed);
             if (rc) return rc;
             if (listCopiedRec[b]) CSG_CUDA_TRY(cudaStreamWaitEvent(d2hStream, listCopied[b], 0));
+            CSG_CUDA_TRY(cudaEventRecord(cbEv[0], d2hStream));
             if ((rc = neighborCsr(d2hStream, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax,
                                   csrOff[b].as<uint64_t>(), csrList[b].as<uint32_t>(), devCap, csrWs.p, csrWs.bytes,
                                   nullptr)))
                 return rc;
         }
+        if (listOffsets) CSG_CUDA_TRY(cudaEventRecord(cbEv[1], d2hStream));
         CSG_CUDA_TRY(cudaEventRecord(reuseReady, d2hStream));
         // everything after the compaction runs on listStream, in call order
         CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, reuseReady, 0));
         if (listOffsets)
         {
+            CSG_CUDA_TRY(cudaEventRecord(cbEv[2], listStream));
             // to the caller's pinned buffers: the offsets by the copy engine, the list by 16-byte stores whose
             // length the compaction left in device memory
             CSG_CUDA_TRY(cudaMemcpyAsync(listOffsets, csrOff[b].p, (n + 1) * sizeof(uint64_t),
@@ -876,12 +884,29 @@ struct Pipeline final : PipelineBase
             int rc = copyListToHost(listStream, csrList[b].as<uint32_t>(), listHost, csrOff[b].as<uint64_t>() + n,
                                     listHost ? listCap : 0, flag);
             if (rc) return rc;
+            CSG_CUDA_TRY(cudaEventRecord(cbEv[3], listStream));
             CSG_CUDA_TRY(cudaEventRecord(listCopied[b], listStream));
             listCopiedRec[b] = true;
+            cbTimed          = true;
             csrCur           = 1 - b;
         }
         CSG_CUDA_TRY(cudaEventRecord(outDone, listStream));
         outPending = true;
+        return CS_OK;
+    }
+
+    int copyTimes(float* ms, int count) override
+    {
+        if (!cbTimed)
+        {
+            setLastError("copy times: no copy-back with neighbour lists yet");
+            return CS_ERR_INVALID;
+        }
+        CSG_CUDA_TRY(cudaEventSynchronize(cbEv[3]));
+        const cudaEvent_t from[4] = {cbEv[0], cbEv[2], cbEv[1], ev[ST_KEYS]};
+        const cudaEvent_t to[4]   = {cbEv[1], cbEv[3], cbEv[2], cbEv[3]};
+        for (int i = 0; i < count && i < 4; ++i)
+            CSG_CUDA_TRY(cudaEventElapsedTime(&ms[i], from[i], to[i]));
         return CS_OK;
     }
 
@@ -1171,6 +1196,16 @@ extern "C" int cs_pipeline_get_outputs(cs_pipeline p, cs_pipeline_outputs* out)
 }
 
 extern "C" size_t cs_pipeline_device_bytes(cs_pipeline p) { return p ? p->impl->deviceBytes() : 0; }
+
+extern "C" int cs_pipeline_copy_times(cs_pipeline p, float* ms, int count)
+{
+    if (!p || !ms || count < 0)
+    {
+        setLastError("pipeline copy times: invalid argument");
+        return CS_ERR_INVALID;
+    }
+    return p->impl->copyTimes(ms, count);
+}
 
 /* per-stage device time of the last run in ms (keys, sort, gather, build, link, geometry, node prep, halos,
  * neighbours) */

@@ -41,6 +41,9 @@ struct PipelineBase
     //! times the neighbour search of the last run's inputs for each candidate tuning and keeps the fastest
     virtual int autotune(cudaStream_t s, int reps, cs_tuning* best, cs_tuning* tried, float* ms, int capacity,
                          int* count) = 0;
+    //! device times of the last copy-back that returned neighbour lists (waits for it): compaction, list copy, the
+    //! list copy's wait for its stream, and the run's start to the end of its list copy
+    virtual int copyTimes(float* ms, int count) = 0;
     int graphReplays = 0; // steps of the last step sequence that were replayed from a captured graph
     cs_tuning tuning{32, 7, 16};
     cudaEvent_t ev[ST_COUNT + 1] = {};

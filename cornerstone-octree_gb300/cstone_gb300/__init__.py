@@ -380,6 +380,7 @@ lib.cs_pipeline_autotune.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p
                                      C.c_void_p]
 
 STAGES = ("keys", "sort", "gather", "build", "link", "geometry", "nbprep", "halos", "neighbors")
+COPY_TIMES = ("compaction", "list_copy", "list_copy_wait", "run_start_to_lists_on_host")
 
 
 class Pipeline:
@@ -457,6 +458,13 @@ class Pipeline:
         ms = (C.c_float * len(STAGES))()
         _check(lib.cs_pipeline_stage_times(self.handle, ms, len(STAGES)))
         return dict(zip(STAGES, list(ms)))
+
+    def copy_times(self):
+        """device ms of the last copy-back that returned neighbour lists: the compaction, the list copy to host
+        memory, the copy's wait for the previous call's copy, and the run's start to the end of its list copy"""
+        ms = (C.c_float * len(COPY_TIMES))()
+        _check(lib.cs_pipeline_copy_times(self.handle, ms, len(COPY_TIMES)))
+        return dict(zip(COPY_TIMES, list(ms)))
 
     def set_tuning(self, nb_group=32, nb_by_target_cost=7, sort_items=16):
         t = Tuning(nb_group, nb_by_target_cost, sort_items)

@@ -611,6 +611,10 @@ int cs_pipeline_autotune(cs_pipeline p, cs_stream_t stream, int reps, cs_tuning*
  * (node preparation of the halo and neighbour searches), halos, neighbours (count <= 9 values); waits for the last
  * run to finish */
 int cs_pipeline_stage_times(cs_pipeline p, float* ms, int count);
+/* device times in ms of the last copy-back that returned neighbour lists (cs_pipeline_run_host_csr*), waiting for it:
+ * the list compaction, the list's copy to host memory, how long the compacted list waited for the previous call's
+ * copy, and the time from the start of the run (its keys) to the end of its list copy (count <= 4 values) */
+int cs_pipeline_copy_times(cs_pipeline p, float* ms, int count);
 
 /* ---- batched independent sets ----------------------------------------------------------------------------------
  * No counterpart call in the reference, which builds one tree per call: many independent particle sets of uneven size
