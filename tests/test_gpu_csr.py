@@ -85,3 +85,50 @@ def test_pipeline_run_host_csr_reports_a_small_list_buffer(cs, O):
     big = torch.empty(int(roff[-1]), dtype=torch.int32).pin_memory()
     pipe.run_host_csr(hx, hy, hz, hh, box, (0, 0), off, big)
     assert np.array_equal(off.numpy(), roff)
+
+
+@pytest.mark.parametrize("shift", [1, 2, 3])
+def test_pipeline_run_host_csr_unaligned_list_buffer(cs, O, shift):
+    """a list buffer that does not start on a 16-byte boundary (the lists are written in 16-byte tiles from the
+    first aligned entry): every entry lands in place, nothing before the buffer is touched"""
+    n, ngmax = 30_000, 48
+    x, y, z, h, ref = _case(O, n, ngmax, 0.05, 6 + shift)
+    roff, rlst = _oracle_csr(ref["nb"], ref["nc"], ngmax)
+    assert roff[-1] > 3 * 4096  # several output tiles
+    hx, hy, hz, hh = (torch.from_numpy(a).pin_memory() for a in (x, y, z, h))
+    off = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+    raw = torch.full((int(roff[-1]) + 16,), -7, dtype=torch.int32).pin_memory()
+    lst = raw[shift:]
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, 16, ngmax, 1.0, 1.0, False, True)
+    pipe.run_host_csr(hx, hy, hz, hh, cs.make_box(-1.0, 60.0), (0, 0), off, lst)
+    assert np.array_equal(off.numpy(), roff)
+    assert np.array_equal(lst.numpy()[: roff[-1]].view(np.uint32), rlst)
+    assert (raw.numpy()[:shift] == -7).all() and (raw.numpy()[shift + roff[-1]:] == -7).all()
+
+
+def test_list_copy_survives_the_next_runs(cs, O):
+    """an asynchronous call's lists are still being copied when the next runs start: the next run writes its
+    neighbour rows elsewhere, and a step waits for the copy, so the host lists are those of the first call"""
+    n, ngmax = 30_000, 48
+    xa, ya, za, ha, refa = _case(O, n, ngmax, 0.05, 11)
+    xb, yb, zb, hb, refb = _case(O, n, ngmax, 0.05, 12)
+    roff, rlst = _oracle_csr(refa["nb"], refa["nc"], ngmax)
+    hx, hy, hz, hh = (torch.from_numpy(a).pin_memory() for a in (xa, ya, za, ha))
+    dx, dy, dz, dh = (torch.from_numpy(a).cuda() for a in (xb, yb, zb, hb))
+    box = cs.make_box(-1.0, 60.0)
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, 16, ngmax, 1.0, 1.0, False, True)
+    for follow in ("run", "run2", "step"):
+        off = torch.empty(n + 1, dtype=torch.int64).pin_memory()
+        lst = torch.empty(int(roff[-1]) + 5, dtype=torch.int32).pin_memory()
+        pipe.run_host_csr(hx, hy, hz, hh, box, (0, 0), off, lst, asynchronous=True)
+        if follow == "step":
+            pipe.step(dx, dy, dz, dh, box)
+        else:
+            for _ in range(1 if follow == "run" else 2):
+                pipe.run(dx, dy, dz, dh, box)
+        pipe.wait()
+        torch.cuda.synchronize()
+        assert np.array_equal(off.numpy(), roff), follow
+        assert np.array_equal(lst.numpy()[: roff[-1]].view(np.uint32), rlst), follow
+        out = pipe.outputs()
+        assert np.array_equal(u32(out["neighbor_counts"]), refb["nc"]), follow
