@@ -184,41 +184,80 @@ __global__ void __launch_bounds__(LT_THREADS) gatherListKernel(const uint32_t* _
                                                                 size_t maxTiles, uint32_t* overflow)
 {
     __shared__ __align__(16) uint32_t sTile[LT_TILE + 8];
+    __shared__ unsigned long long sOff[LT_THREADS + 1];
     const unsigned long long t = offsets[n];
     const size_t m             = t < capacity ? size_t(t) : capacity;
     if (blockIdx.x == 0 && threadIdx.x == 0 && overflow && t > capacity) *overflow = 1u;
     if (m == 0) return;
-    const size_t head   = ltHead(dst);
-    const size_t tiles  = m <= head + LT_TILE ? 1 : 1 + (m - head - 1) / LT_TILE;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t head  = ltHead(dst);
+    const size_t tiles = m <= head + LT_TILE ? 1 : 1 + (m - head - 1) / LT_TILE;
+    const unsigned tid = threadIdx.x;
     for (size_t k = blockIdx.x; k < tiles && k < maxTiles; k += gridDim.x)
     {
         const size_t s = ltTileStart(k, head);
         const size_t e = min(m, head + (k + 1) * LT_TILE);
         // shared index of entry q: q - s + pad (tile 0's aligned part starts at index 4)
         const size_t pad = k == 0 ? 4 - head : 0;
-        // gather: warp w takes rows r0 + w, r0 + w + 8, ... until a row starts at or after e
-        const size_t r0 = tileRows[k];
-        for (size_t r = r0 + warp; r < n; r += LT_THREADS / 32)
+        // gather, in chunks of up to LT_THREADS rows: the chunk's row offsets staged in shared memory, then each
+        // thread takes every LT_THREADS-th entry (consecutive threads read consecutive entries of a row), keeping up
+        // to four loads in flight
+        size_t r0 = tileRows[k], q0 = s;
+        while (q0 < e)
         {
-            const unsigned long long lo = offsets[r], hi = offsets[r + 1];
-            if (lo >= e) break;
-            const size_t a = lo > s ? size_t(lo) : s, b = hi < e ? size_t(hi) : e;
-            const uint32_t* row = nb + r * size_t(ngmax);
-            for (size_t q = a + lane; q < b; q += 32)
-                sTile[q - s + pad] = __ldcs(row + (q - lo));
+            const unsigned R = unsigned(min(size_t(LT_THREADS), n - r0));
+            if (tid <= R) sOff[tid] = offsets[r0 + tid];
+            if (tid == 0 && R == LT_THREADS) sOff[LT_THREADS] = offsets[r0 + LT_THREADS];
+            __syncthreads();
+            const size_t qEnd = min(e, size_t(sOff[R]));
+            size_t q          = q0 + tid;
+            unsigned row      = 0;
+            if (q < qEnd)
+            {
+                // the last row that starts at or before q (rows that start later are past it)
+                unsigned lo = 0, hi = R;
+                while (hi - lo > 1)
+                {
+                    const unsigned mid = (lo + hi) / 2;
+                    if (sOff[mid] <= q) lo = mid;
+                    else hi = mid;
+                }
+                row = lo;
+            }
+            for (; q < qEnd; q += 4 * LT_THREADS)
+            {
+                uint32_t v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                {
+                    const size_t qq = q + u * LT_THREADS;
+                    if (qq < qEnd)
+                    {
+                        while (sOff[row + 1] <= qq)
+                            ++row;
+                        v[u] = __ldcs(nb + (r0 + row) * size_t(ngmax) + (qq - sOff[row]));
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                {
+                    const size_t qq = q + u * LT_THREADS;
+                    if (qq < qEnd) sTile[qq - s + pad] = v[u];
+                }
+            }
+            __syncthreads();
+            r0 += R;
+            q0 = qEnd;
         }
-        __syncthreads();
         // write: the unaligned entries of tile 0 one by one, then 16-byte stores, then the ragged end
         const size_t a0 = k == 0 ? min(head, e) : s;
-        for (size_t q = s + threadIdx.x; q < a0; q += LT_THREADS)
+        for (size_t q = s + tid; q < a0; q += LT_THREADS)
             dst[q] = sTile[q - s + pad];
         const size_t nv = (e - a0) / 4;
         const uint4* sv = reinterpret_cast<const uint4*>(sTile + (a0 - s + pad));
         uint4* dv       = reinterpret_cast<uint4*>(dst + a0);
-        for (size_t v = threadIdx.x; v < nv; v += LT_THREADS)
+        for (size_t v = tid; v < nv; v += LT_THREADS)
             dv[v] = sv[v];
-        for (size_t q = a0 + 4 * nv + threadIdx.x; q < e; q += LT_THREADS)
+        for (size_t q = a0 + 4 * nv + tid; q < e; q += LT_THREADS)
             dst[q] = sTile[q - s + pad];
         __syncthreads();
     }
