@@ -142,156 +142,62 @@ __global__ void __launch_bounds__(CSR_THREADS) csrWriteKernel(const uint32_t* __
     }
 }
 
-// ---------------------------------------------------------------------------------------------------------------
-// The stored entries straight from the ngmax-strided rows to host memory, once the offsets are known (no compacted
-// copy in device memory). The output [0, m), m = min(total, capacity), is cut into tiles at the 16-byte boundaries of
-// the destination: tile 0 = [0, head + LT_TILE), tile k >= 1 = [head + k LT_TILE, head + (k + 1) LT_TILE), where
-// dst + head is the first 16-byte aligned entry. A block gathers a tile's entries from its rows into shared memory
-// and writes them with 16-byte stores (the host link runs at its copy-engine rate this way; 4-byte stores at the
-// rows' unaligned offsets reach about half of it). tileRows[k] (one pass over the offsets) is the row that holds the
-// tile's first entry. The length comes from device memory: no host synchronisation. HBM traffic: the stored
-// entries read once (plus the offsets), against a compaction's read + write + read.
-// ---------------------------------------------------------------------------------------------------------------
-constexpr int LT_TILE    = 4096; // entries per tile (16 KB)
-constexpr int LT_THREADS = 256;
-
-__device__ __forceinline__ size_t ltTileStart(size_t k, size_t head) { return k == 0 ? 0 : head + k * LT_TILE; }
-
-__device__ __forceinline__ size_t ltHead(const uint32_t* dst)
+// Copies min(*total, capacity) list entries from device memory to pinned host memory with 16-byte stores (the host
+// link runs at its copy-engine rate this way; 4-byte stores at unaligned row offsets reach about half of it). The
+// length comes from device memory, so the copy needs no host synchronisation. src is 16-byte aligned; the first few
+// entries bring dst to a 16-byte boundary. A total above the capacity sets *overflow (when given).
+__global__ void __launch_bounds__(256, 5) copyListKernel(const uint32_t* __restrict__ src, uint32_t* dst,
+                                                      const uint64_t* __restrict__ total, size_t capacity,
+                                                      uint32_t* overflow)
 {
-    return ((16u - (reinterpret_cast<uintptr_t>(dst) & 15u)) / 4u) & 3u;
-}
-
-__global__ void listTileRowsKernel(const uint64_t* __restrict__ offsets, size_t n, const uint32_t* dst,
-                                   size_t maxTiles, uint32_t* __restrict__ tileRows)
-{
-    const size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (r >= n) return;
-    const unsigned long long lo = offsets[r], hi = offsets[r + 1];
-    if (hi <= lo) return;
-    const size_t head = ltHead(dst);
-    // the first tile whose start is at or after lo
-    size_t k = lo == 0 ? 0 : (lo <= head ? 1 : (lo - head + LT_TILE - 1) / LT_TILE);
-    if (k == 0 && lo > 0) k = 1;
-    for (; k < maxTiles && ltTileStart(k, head) < hi; ++k)
-        tileRows[k] = uint32_t(r);
-}
-
-__global__ void __launch_bounds__(LT_THREADS) gatherListKernel(const uint32_t* __restrict__ nb, unsigned ngmax,
-                                                                const uint64_t* __restrict__ offsets, size_t n,
-                                                                uint32_t* dst, size_t capacity,
-                                                                const uint32_t* __restrict__ tileRows,
-                                                                size_t maxTiles, uint32_t* overflow)
-{
-    __shared__ __align__(16) uint32_t sTile[LT_TILE + 8];
-    __shared__ unsigned long long sOff[LT_THREADS + 1];
-    const unsigned long long t = offsets[n];
+    const unsigned long long t = *total;
     const size_t m             = t < capacity ? size_t(t) : capacity;
     if (blockIdx.x == 0 && threadIdx.x == 0 && overflow && t > capacity) *overflow = 1u;
-    if (m == 0) return;
-    const size_t head  = ltHead(dst);
-    const size_t tiles = m <= head + LT_TILE ? 1 : 1 + (m - head - 1) / LT_TILE;
-    const unsigned tid = threadIdx.x;
-    for (size_t k = blockIdx.x; k < tiles && k < maxTiles; k += gridDim.x)
+    const size_t head = min(size_t((16u - (reinterpret_cast<uintptr_t>(dst) & 15u)) / 4u & 3u), m);
+    const size_t nv   = (m - head) / 4;
+    if (blockIdx.x == 0)
     {
-        const size_t s = ltTileStart(k, head);
-        const size_t e = min(m, head + (k + 1) * LT_TILE);
-        // shared index of entry q: q - s + pad (tile 0's aligned part starts at index 4)
-        const size_t pad = k == 0 ? 4 - head : 0;
-        // gather, in chunks of up to LT_THREADS rows: the chunk's row offsets staged in shared memory, then each
-        // thread takes every LT_THREADS-th entry (consecutive threads read consecutive entries of a row), keeping up
-        // to four loads in flight
-        size_t r0 = tileRows[k], q0 = s;
-        while (q0 < e)
-        {
-            const unsigned R = unsigned(min(size_t(LT_THREADS), n - r0));
-            if (tid <= R) sOff[tid] = offsets[r0 + tid];
-            if (tid == 0 && R == LT_THREADS) sOff[LT_THREADS] = offsets[r0 + LT_THREADS];
-            __syncthreads();
-            const size_t qEnd = min(e, size_t(sOff[R]));
-            size_t q          = q0 + tid;
-            unsigned row      = 0;
-            if (q < qEnd)
-            {
-                // the last row that starts at or before q (rows that start later are past it)
-                unsigned lo = 0, hi = R;
-                while (hi - lo > 1)
-                {
-                    const unsigned mid = (lo + hi) / 2;
-                    if (sOff[mid] <= q) lo = mid;
-                    else hi = mid;
-                }
-                row = lo;
-            }
-            for (; q < qEnd; q += 4 * LT_THREADS)
-            {
-                uint32_t v[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                {
-                    const size_t qq = q + u * LT_THREADS;
-                    if (qq < qEnd)
-                    {
-                        while (sOff[row + 1] <= qq)
-                            ++row;
-                        v[u] = __ldcs(nb + (r0 + row) * size_t(ngmax) + (qq - sOff[row]));
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                {
-                    const size_t qq = q + u * LT_THREADS;
-                    if (qq < qEnd) sTile[qq - s + pad] = v[u];
-                }
-            }
-            __syncthreads();
-            r0 += R;
-            q0 = qEnd;
-        }
-        // write: the unaligned entries of tile 0 one by one, then 16-byte stores, then the ragged end
-        const size_t a0 = k == 0 ? min(head, e) : s;
-        for (size_t q = s + tid; q < a0; q += LT_THREADS)
-            dst[q] = sTile[q - s + pad];
-        const size_t nv = (e - a0) / 4;
-        const uint4* sv = reinterpret_cast<const uint4*>(sTile + (a0 - s + pad));
-        uint4* dv       = reinterpret_cast<uint4*>(dst + a0);
-        for (size_t v = tid; v < nv; v += LT_THREADS)
-            dv[v] = sv[v];
-        for (size_t q = a0 + 4 * nv + tid; q < e; q += LT_THREADS)
-            dst[q] = sTile[q - s + pad];
-        __syncthreads();
+        if (threadIdx.x < head) dst[threadIdx.x] = src[threadIdx.x];
+        const size_t tail0 = head + 4 * nv;
+        if (tail0 + threadIdx.x < m) dst[tail0 + threadIdx.x] = src[tail0 + threadIdx.x];
     }
+    // four loads in flight per thread before their stores: the host link needs about 1 MB of stores in flight, and
+    // the loads' latency grows while other kernels share the device
+    constexpr int U        = 4;
+    const unsigned stride  = gridDim.x * blockDim.x;
+    const unsigned tid     = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint4* sp        = reinterpret_cast<const uint4*>(src + head) + tid;
+    uint4* dp              = reinterpret_cast<uint4*>(dst + head) + tid;
+    size_t left            = nv > tid ? (nv - tid + stride - 1) / stride : 0; // this thread's 16-byte words
+    for (; left >= U; left -= U)
+    {
+        uint4 r[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            r[u] = __ldcs(sp + u * stride);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            dp[u * stride] = r[u];
+        sp += U * stride;
+        dp += U * stride;
+    }
+    for (; left > 0; --left, sp += stride, dp += stride)
+        *dp = __ldcs(sp);
 }
 
-size_t listTileCount(size_t capacity) { return capacity / LT_TILE + 2; }
-
-int listTileRows(cudaStream_t s, const uint64_t* offsets, size_t n, const uint32_t* dst, uint32_t* tileRows,
-                 size_t maxTiles)
+int copyListToHost(cudaStream_t s, const uint32_t* src, uint32_t* dst, const uint64_t* totalDev, size_t capacity,
+                   uint32_t* overflow)
 {
-    if (n == 0 || maxTiles == 0) return CS_OK;
-    listTileRowsKernel<<<iceil(n, 256), 256, 0, s>>>(offsets, n, dst, maxTiles, tileRows);
-    CSG_CHECK_LAUNCH();
-    return CS_OK;
-}
-
-int gatherListToHost(cudaStream_t s, const uint32_t* nb, unsigned ngmax, const uint64_t* offsets, size_t n,
-                     uint32_t* dst, size_t capacity, const uint32_t* tileRows, size_t maxTiles, uint32_t* overflow)
-{
-    if (!nb || !offsets || !tileRows || (capacity && !dst) || (reinterpret_cast<uintptr_t>(dst) & 3u))
+    if (!src || !totalDev || (capacity && !dst) || (reinterpret_cast<uintptr_t>(dst) & 3u) ||
+        (reinterpret_cast<uintptr_t>(src) & 15u))
     {
-        setLastError("list gather: null or misaligned pointer");
+        setLastError("list copy: null or misaligned pointer");
         return CS_ERR_INVALID;
     }
-    if (maxTiles < listTileCount(capacity))
-    {
-        setLastError("list gather: tile table too small");
-        return CS_ERR_INVALID;
-    }
-    if (n == 0) return CS_OK;
-    // 64 blocks saturate the host link while leaving most SM slots to the next run's kernels; 16 KB of shared
-    // memory and 256 threads each, they fit beside the cooperative build's blocks, whose launch waits until all of
-    // its blocks can be resident
-    gatherListKernel<<<64, LT_THREADS, 0, s>>>(nb, ngmax, offsets, n, dst, capacity, tileRows, maxTiles, overflow);
+    // 64 blocks saturate the host link (measured) while leaving the SMs to the next run's kernels. Each block is
+    // small (256 threads, at most 51 registers each): it fits beside a full share of the cooperative build's blocks,
+    // whose launch waits until all of its blocks can be resident
+    copyListKernel<<<64, 256, 0, s>>>(src, dst, totalDev, capacity, overflow);
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }

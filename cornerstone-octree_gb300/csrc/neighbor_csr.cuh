@@ -13,18 +13,9 @@ size_t neighborCsrWorkspaceBytes(size_t n);
 int neighborCsr(cudaStream_t s, const uint32_t* nb, const uint32_t* nc, size_t n, unsigned ngmax, uint64_t* offsets,
                 uint32_t* list, size_t capacity, void* ws, size_t wsBytes, uint32_t* overflow);
 
-/*! Entries of the tile table that gatherListToHost needs for a list buffer of `capacity` entries. */
-size_t listTileCount(size_t capacity);
-
-/*! tileRows[k] = the row holding the first entry of output tile k (for the destination dst, whose alignment sets
- *  the tiles), from the offsets of neighborCsr (device). No host synchronisation. */
-int listTileRows(cudaStream_t s, const uint64_t* offsets, size_t n, const uint32_t* dst, uint32_t* tileRows,
-                 size_t maxTiles);
-
-/*! dst[q] = the q-th stored entry of the ngmax-strided rows nb, for q < min(offsets[n], capacity) (dst: pinned host
- *  or device memory, 4-byte aligned); *overflow = 1 when offsets[n] > capacity (overflow may be null). Reads the
- *  offsets and tile table from device memory: no host synchronisation. */
-int gatherListToHost(cudaStream_t s, const uint32_t* nb, unsigned ngmax, const uint64_t* offsets, size_t n,
-                     uint32_t* dst, size_t capacity, const uint32_t* tileRows, size_t maxTiles, uint32_t* overflow);
+/*! dst[k] = src[k] for k < min(*totalDev, capacity) (device src, 16-byte aligned; pinned host or device dst, 4-byte
+ *  aligned); *overflow = 1 when *totalDev > capacity (overflow may be null). No host synchronisation. */
+int copyListToHost(cudaStream_t s, const uint32_t* src, uint32_t* dst, const uint64_t* totalDev, size_t capacity,
+                   uint32_t* overflow);
 
 } // namespace csg

@@ -73,9 +73,9 @@ struct Pipeline final : PipelineBase
     cudaEvent_t copyEv[kCopyChunks]  = {};
     cudaEvent_t inUsed[2]            = {}; // on the compute stream after the keys of the last run that read the set
     bool inUsedRec[2]                = {false, false};
-    // results to host: the error words first (errCopied), then counts, flags and the list offsets (reuseReady: the
-    // next run may overwrite its outputs, all but the neighbour rows) on d2hStream; the lists then go to the host on
-    // listStream (outDone), with offsets from one of two buffer sets in turn
+    // results to host: with lists, the compaction first, on the compute stream (outReady after it); then the error
+    // words (errCopied), counts and flags (reuseReady: the next run may overwrite its outputs) on d2hStream, and the
+    // compacted lists (from one of two device buffer sets in turn) on listStream (outDone)
     cudaStream_t d2hStream = nullptr, listStream = nullptr;
     cudaEvent_t outReady = nullptr, errCopied = nullptr, reuseReady = nullptr, outDone = nullptr;
     cudaEvent_t listCopied[2]  = {};  // on listStream after the copy out of compaction buffer b
@@ -85,11 +85,7 @@ struct Pipeline final : PipelineBase
     int csrCur                 = 0;
     uint32_t* herrHost         = nullptr; // pinned, the last copied error words
     uint32_t* listOverflowHost = nullptr; // pinned, set by the list copy when a list buffer was too small
-    DevBuf csrWs, csrOff[2], csrTileRows[2]; // per copy-back with lists: offsets and tile rows (two sets in turn)
-    // neighbour rows: a copy-back with lists reads nb after reuseReady, so the next run writes nbAlt instead (the
-    // two swap); nbInFlight / nbAltGuard: the listCopied index whose copy reads nb / nbAlt (-1: none)
-    DevBuf nbAlt;
-    int nbInFlight = -1, nbAltGuard = -1;
+    DevBuf csrWs, csrOff[2], csrList[2]; // the compacted lists on the device (two sets in turn), copied to the host
     bool outPending      = false;   // a copy-back whose errors are not yet reported
     int stickyRc         = CS_OK;   // an earlier run's device error, reported by the next wait
     char stickyMsg[160]  = {};
@@ -380,12 +376,6 @@ struct Pipeline final : PipelineBase
     {
         int rc;
         if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, reuseReady, 0)); // a copy-back still reads the outputs
-        if (nbInFlight >= 0)
-        {
-            // a list copy still reads the neighbour rows (steps keep one row buffer: their graphs hold its address)
-            CSG_CUDA_TRY(cudaStreamWaitEvent(s, listCopied[nbInFlight], 0));
-            nbInFlight = -1;
-        }
         lastNIn = 0; // autotune reruns plain runs only (a step's inputs need not outlive it)
         if (incCur < 0 || nIn != incN)
         {
@@ -685,22 +675,6 @@ struct Pipeline final : PipelineBase
         if (cfg.do_neighbors)
         {
             const size_t nbNeed = std::max<size_t>(1, n * cfg.ngmax) * sizeof(uint32_t);
-            if (nbInFlight >= 0)
-            {
-                // the last run's rows are still being copied to host memory: write the other row buffer, once the
-                // copy that read it (two copy-backs ago) is done; step graphs hold the old address, so steps restart
-                const int g = nbAltGuard;
-                std::swap(nb.p, nbAlt.p);
-                std::swap(nb.bytes, nbAlt.bytes);
-                nbAltGuard = nbInFlight;
-                nbInFlight = -1;
-                if (g >= 0)
-                {
-                    if (nbNeed > nb.bytes) CSG_CUDA_TRY(cudaEventSynchronize(listCopied[g]));
-                    CSG_CUDA_TRY(cudaStreamWaitEvent(s, listCopied[g], 0));
-                }
-                resetSteps();
-            }
             if ((rc = nb.ensure(nbNeed))) return rc;
             if ((rc = pout.ensure(n))) return rc;
             if ((rc = nbMarkOutside<T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), prep.phi, centers.as<T>(),
@@ -863,6 +837,29 @@ struct Pipeline final : PipelineBase
                 std::snprintf(stickyMsg, sizeof(stickyMsg), "%s", cs_last_error());
             }
         }
+        const size_t devCap = listOffsets ? std::min(listCap, n * size_t(cfg.ngmax)) : 0;
+        const int b         = csrCur;
+        if (listOffsets)
+        {
+            // the stored neighbour indices compacted on the compute stream, right after the run (a full-bandwidth
+            // pass of about 2 ms at 16M; beside the next run it would slow that run's sort and hold up its
+            // cooperative build), into buffer set b once the copy out of it two calls ago has finished (a buffer that
+            // grows is freed first: wait on the host for its last reader)
+            const size_t wsNeed = neighborCsrWorkspaceBytes(n), offNeed = (n + 1) * sizeof(uint64_t);
+            const size_t listNeed = std::max<size_t>(devCap, 4) * sizeof(uint32_t);
+            if (listCopiedRec[b] && (offNeed > csrOff[b].bytes || listNeed > csrList[b].bytes))
+                CSG_CUDA_TRY(cudaEventSynchronize(listCopied[b]));
+            int rc = csrWs.ensure(wsNeed);
+            if (!rc) rc = csrOff[b].ensure(offNeed);
+            if (!rc) rc = csrList[b].ensure(listNeed);
+            if (rc) return rc;
+            if (listCopiedRec[b]) CSG_CUDA_TRY(cudaStreamWaitEvent(s, listCopied[b], 0));
+            CSG_CUDA_TRY(cudaEventRecord(cbEv[0], s));
+            if ((rc = neighborCsr(s, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax, csrOff[b].as<uint64_t>(),
+                                  csrList[b].as<uint32_t>(), devCap, csrWs.p, csrWs.bytes, nullptr)))
+                return rc;
+            CSG_CUDA_TRY(cudaEventRecord(cbEv[1], s));
+        }
         CSG_CUDA_TRY(cudaEventRecord(outReady, s));
         CSG_CUDA_TRY(cudaStreamWaitEvent(d2hStream, outReady, 0));
         CSG_CUDA_TRY(cudaMemcpyAsync(herrHost, errWords.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d2hStream));
@@ -872,54 +869,28 @@ struct Pipeline final : PipelineBase
         if (flagsHost)
             CSG_CUDA_TRY(
                 cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, d2hStream));
-        const size_t cap = listHost ? listCap : 0;
-        const int b      = csrCur;
-        if (listOffsets)
-        {
-            // the offsets, and the row that holds each output tile's first entry, into buffer set b once the copy
-            // out of it two calls ago has finished (a buffer that grows is freed first: wait on the host for it)
-            const size_t wsNeed = neighborCsrWorkspaceBytes(n), offNeed = (n + 1) * sizeof(uint64_t);
-            const size_t tiles = listTileCount(cap), rowsNeed = tiles * sizeof(uint32_t);
-            if (wsNeed > csrWs.bytes) CSG_CUDA_TRY(cudaStreamSynchronize(d2hStream));
-            if (listCopiedRec[b] && (offNeed > csrOff[b].bytes || rowsNeed > csrTileRows[b].bytes))
-                CSG_CUDA_TRY(cudaEventSynchronize(listCopied[b]));
-            int rc = csrWs.ensure(wsNeed);
-            if (!rc) rc = csrOff[b].ensure(offNeed);
-            if (!rc) rc = csrTileRows[b].ensure(rowsNeed);
-            if (rc) return rc;
-            if (listCopiedRec[b]) CSG_CUDA_TRY(cudaStreamWaitEvent(d2hStream, listCopied[b], 0));
-            CSG_CUDA_TRY(cudaEventRecord(cbEv[0], d2hStream));
-            if ((rc = neighborCsr(d2hStream, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax,
-                                  csrOff[b].as<uint64_t>(), nullptr, 0, csrWs.p, csrWs.bytes, nullptr)))
-                return rc;
-            if (cap && (rc = listTileRows(d2hStream, csrOff[b].as<uint64_t>(), n, listHost,
-                                          csrTileRows[b].as<uint32_t>(), tiles)))
-                return rc;
-            CSG_CUDA_TRY(cudaEventRecord(cbEv[1], d2hStream));
-        }
         CSG_CUDA_TRY(cudaEventRecord(reuseReady, d2hStream));
-        // everything after the offsets runs on listStream, in call order
-        CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, reuseReady, 0));
+        // everything after the compaction runs on listStream, in call order
+        CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, outReady, 0));
         if (listOffsets)
         {
             CSG_CUDA_TRY(cudaEventRecord(cbEv[2], listStream));
-            // to the caller's pinned buffers: the offsets by the copy engine, the stored entries gathered from the
-            // rows and written with 16-byte stores. The rows stay readable until then: the next run writes its
-            // neighbours into the other row buffer (nbInFlight), and a step waits for this copy
+            // to the caller's pinned buffers: the offsets by the copy engine, the list by 16-byte stores whose
+            // length the compaction left in device memory
             CSG_CUDA_TRY(cudaMemcpyAsync(listOffsets, csrOff[b].p, (n + 1) * sizeof(uint64_t),
                                          cudaMemcpyDeviceToHost, listStream));
             uint32_t* flag = nullptr;
             CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&flag), listOverflowHost, 0));
-            int rc = gatherListToHost(listStream, nb.as<uint32_t>(), cfg.ngmax, csrOff[b].as<uint64_t>(), n, listHost,
-                                      cap, csrTileRows[b].as<uint32_t>(), listTileCount(cap), flag);
+            int rc = copyListToHost(listStream, csrList[b].as<uint32_t>(), listHost, csrOff[b].as<uint64_t>() + n,
+                                    listHost ? listCap : 0, flag);
             if (rc) return rc;
             CSG_CUDA_TRY(cudaEventRecord(cbEv[3], listStream));
             CSG_CUDA_TRY(cudaEventRecord(listCopied[b], listStream));
             listCopiedRec[b] = true;
             cbTimed          = true;
-            nbInFlight       = b;
             csrCur           = 1 - b;
         }
+        CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, reuseReady, 0)); // outDone: the counts and flags too
         CSG_CUDA_TRY(cudaEventRecord(outDone, listStream));
         outPending = true;
         return CS_OK;

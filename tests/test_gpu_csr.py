@@ -89,12 +89,12 @@ def test_pipeline_run_host_csr_reports_a_small_list_buffer(cs, O):
 
 @pytest.mark.parametrize("shift", [1, 2, 3])
 def test_pipeline_run_host_csr_unaligned_list_buffer(cs, O, shift):
-    """a list buffer that does not start on a 16-byte boundary (the lists are written in 16-byte tiles from the
-    first aligned entry): every entry lands in place, nothing before the buffer is touched"""
+    """a list buffer that does not start on a 16-byte boundary (the lists are written with 16-byte stores from the
+    first aligned entry): every entry lands in place, nothing outside the buffer is touched"""
     n, ngmax = 30_000, 48
     x, y, z, h, ref = _case(O, n, ngmax, 0.05, 6 + shift)
     roff, rlst = _oracle_csr(ref["nb"], ref["nc"], ngmax)
-    assert roff[-1] > 3 * 4096  # several output tiles
+    assert roff[-1] > 3 * 4096
     hx, hy, hz, hh = (torch.from_numpy(a).pin_memory() for a in (x, y, z, h))
     off = torch.empty(n + 1, dtype=torch.int64).pin_memory()
     raw = torch.full((int(roff[-1]) + 16,), -7, dtype=torch.int32).pin_memory()
@@ -107,8 +107,8 @@ def test_pipeline_run_host_csr_unaligned_list_buffer(cs, O, shift):
 
 
 def test_list_copy_survives_the_next_runs(cs, O):
-    """an asynchronous call's lists are still being copied when the next runs start: the next run writes its
-    neighbour rows elsewhere, and a step waits for the copy, so the host lists are those of the first call"""
+    """an asynchronous call's lists are still being copied to host memory when the next runs (or a step) start: the
+    copy reads the compacted lists, in buffers of their own, so the host lists are those of the first call"""
     n, ngmax = 30_000, 48
     xa, ya, za, ha, refa = _case(O, n, ngmax, 0.05, 11)
     xb, yb, zb, hb, refb = _case(O, n, ngmax, 0.05, 12)
