@@ -144,8 +144,9 @@ __global__ void __launch_bounds__(CSR_THREADS) csrWriteKernel(const uint32_t* __
 
 // Copies min(*total, capacity) list entries from device memory to pinned host memory with 16-byte stores (the host
 // link runs at its copy-engine rate this way; 4-byte stores at unaligned row offsets reach about half of it). The
-// length comes from device memory, so the copy needs no host synchronisation. src is 16-byte aligned; the first few
-// entries bring dst to a 16-byte boundary. A total above the capacity sets *overflow (when given).
+// length comes from device memory, so the copy needs no host synchronisation. src and dst lie at the same offset
+// within 16 bytes: the first head entries are copied one by one, then src + head and dst + head are both 16-byte
+// aligned. A total above the capacity sets *overflow (when given).
 __global__ void __launch_bounds__(256, 5) copyListKernel(const uint32_t* __restrict__ src, uint32_t* dst,
                                                       const uint64_t* __restrict__ total, size_t capacity,
                                                       uint32_t* overflow)
@@ -188,10 +189,12 @@ __global__ void __launch_bounds__(256, 5) copyListKernel(const uint32_t* __restr
 int copyListToHost(cudaStream_t s, const uint32_t* src, uint32_t* dst, const uint64_t* totalDev, size_t capacity,
                    uint32_t* overflow)
 {
-    if (!src || !totalDev || (capacity && !dst) || (reinterpret_cast<uintptr_t>(dst) & 3u) ||
-        (reinterpret_cast<uintptr_t>(src) & 15u))
+    // the 16-byte loads and stores start at the same entry of src and dst: both must sit at the same place within
+    // 16 bytes (and on 4-byte boundaries)
+    const uintptr_t sa = reinterpret_cast<uintptr_t>(src), da = reinterpret_cast<uintptr_t>(dst);
+    if (!src || !totalDev || (capacity && !dst) || (sa & 3u) || (capacity && ((da & 3u) || (sa & 15u) != (da & 15u))))
     {
-        setLastError("list copy: null or misaligned pointer");
+        setLastError("list copy: null pointer, or source and destination not aligned alike");
         return CS_ERR_INVALID;
     }
     // 64 blocks saturate the host link (measured) while leaving the SMs to the next run's kernels. Each block is

@@ -839,6 +839,14 @@ struct Pipeline final : PipelineBase
         }
         const size_t devCap = listOffsets ? std::min(listCap, n * size_t(cfg.ngmax)) : 0;
         const int b         = csrCur;
+        if (listHost && (reinterpret_cast<uintptr_t>(listHost) & 3u))
+        {
+            setLastError("pipeline: the neighbour list buffer must be 4-byte aligned");
+            return CS_ERR_INVALID;
+        }
+        // the compacted list starts at the host buffer's offset within 16 bytes, so that the copy's 16-byte loads and
+        // stores are aligned on both sides
+        const size_t phase = (reinterpret_cast<uintptr_t>(listHost) & 15u) / 4u;
         if (listOffsets)
         {
             // the stored neighbour indices compacted on the compute stream, right after the run (a full-bandwidth
@@ -846,7 +854,7 @@ struct Pipeline final : PipelineBase
             // cooperative build), into buffer set b once the copy out of it two calls ago has finished (a buffer that
             // grows is freed first: wait on the host for its last reader)
             const size_t wsNeed = neighborCsrWorkspaceBytes(n), offNeed = (n + 1) * sizeof(uint64_t);
-            const size_t listNeed = std::max<size_t>(devCap, 4) * sizeof(uint32_t);
+            const size_t listNeed = (devCap + 4) * sizeof(uint32_t);
             if (listCopiedRec[b] && (offNeed > csrOff[b].bytes || listNeed > csrList[b].bytes))
                 CSG_CUDA_TRY(cudaEventSynchronize(listCopied[b]));
             int rc = csrWs.ensure(wsNeed);
@@ -856,7 +864,7 @@ struct Pipeline final : PipelineBase
             if (listCopiedRec[b]) CSG_CUDA_TRY(cudaStreamWaitEvent(s, listCopied[b], 0));
             CSG_CUDA_TRY(cudaEventRecord(cbEv[0], s));
             if ((rc = neighborCsr(s, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax, csrOff[b].as<uint64_t>(),
-                                  csrList[b].as<uint32_t>(), devCap, csrWs.p, csrWs.bytes, nullptr)))
+                                  csrList[b].as<uint32_t>() + phase, devCap, csrWs.p, csrWs.bytes, nullptr)))
                 return rc;
             CSG_CUDA_TRY(cudaEventRecord(cbEv[1], s));
         }
@@ -881,8 +889,8 @@ struct Pipeline final : PipelineBase
                                          cudaMemcpyDeviceToHost, listStream));
             uint32_t* flag = nullptr;
             CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&flag), listOverflowHost, 0));
-            int rc = copyListToHost(listStream, csrList[b].as<uint32_t>(), listHost, csrOff[b].as<uint64_t>() + n,
-                                    listHost ? listCap : 0, flag);
+            int rc = copyListToHost(listStream, csrList[b].as<uint32_t>() + phase, listHost,
+                                    csrOff[b].as<uint64_t>() + n, listHost ? listCap : 0, flag);
             if (rc) return rc;
             CSG_CUDA_TRY(cudaEventRecord(cbEv[3], listStream));
             CSG_CUDA_TRY(cudaEventRecord(listCopied[b], listStream));
