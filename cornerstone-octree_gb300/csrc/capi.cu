@@ -4,6 +4,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 
 namespace csg
 {
@@ -32,6 +33,36 @@ int smCount()
         cachedDevice = dev;
     }
     return cachedCount;
+}
+
+__global__ void copyWordsKernel(const uint32_t* src, uint32_t* dst, unsigned words)
+{
+    for (unsigned k = threadIdx.x; k < words; k += blockDim.x)
+        dst[k] = src[k];
+}
+
+int readSmallToHost(cudaStream_t s, void* hostDst, const void* devSrc, size_t bytes)
+{
+    constexpr size_t kMax = 4096;
+    if (bytes % 4 || bytes > kMax)
+    {
+        setLastError("internal: small read of %zu bytes", bytes);
+        return CS_ERR_INVALID;
+    }
+    // one staging buffer per host thread (calls on a thread are sequential: each ends with a synchronisation);
+    // portable + mapped, so that kernels of any device reach it through its device address
+    static thread_local uint32_t* staging = nullptr;
+    static thread_local uint32_t* stagingDev = nullptr;
+    if (!staging)
+    {
+        CSG_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&staging), kMax, cudaHostAllocPortable | cudaHostAllocMapped));
+        CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&stagingDev), staging, 0));
+    }
+    copyWordsKernel<<<1, 32, 0, s>>>(static_cast<const uint32_t*>(devSrc), stagingDev, unsigned(bytes / 4));
+    CSG_CHECK_LAUNCH();
+    CSG_CUDA_TRY(cudaStreamSynchronize(s));
+    std::memcpy(hostDst, staging, bytes);
+    return CS_OK;
 }
 
 static std::atomic<uint32_t> gSortSpins{WaitLimits{}.sortSpins};

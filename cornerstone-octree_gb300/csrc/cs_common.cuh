@@ -432,6 +432,14 @@ inline unsigned iceil(size_t a, size_t b) { return unsigned((a + b - 1) / b); }
 // number of SMs of the current device (cached per device)
 int smCount();
 
+// Reads `bytes` (a multiple of 4, at most 4096) of device memory to host memory after the work already on stream s:
+// a one-warp kernel copies them into mapped pinned memory, then the stream is synchronised. No copy engine takes
+// part, so the read never waits behind large device-to-host copies queued on other streams.
+int readSmallToHost(cudaStream_t s, void* hostDst, const void* devSrc, size_t bytes);
+
+// dst[k] = src[k], k < words: one warp; dst may be mapped pinned host memory
+__global__ void copyWordsKernel(const uint32_t* src, uint32_t* dst, unsigned words);
+
 // Bounds of the device-side waits, read by the host at each launch and passed as kernel arguments. The defaults
 // give up after about a second; cs_set_wait_limits lowers them and can make one wait stall on purpose (a flag that
 // nothing sets), so that tests reach the timeout path on ordinary inputs.

@@ -142,69 +142,6 @@ __global__ void __launch_bounds__(CSR_THREADS) csrWriteKernel(const uint32_t* __
     }
 }
 
-// Copies min(*total, capacity) list entries from device memory to pinned host memory with 16-byte stores (the host
-// link runs at its copy-engine rate this way; 4-byte stores at unaligned row offsets reach about half of it). The
-// length comes from device memory, so the copy needs no host synchronisation. src and dst lie at the same offset
-// within 16 bytes: the first head entries are copied one by one, then src + head and dst + head are both 16-byte
-// aligned. A total above the capacity sets *overflow (when given).
-__global__ void __launch_bounds__(256, 5) copyListKernel(const uint32_t* __restrict__ src, uint32_t* dst,
-                                                      const uint64_t* __restrict__ total, size_t capacity,
-                                                      uint32_t* overflow)
-{
-    const unsigned long long t = *total;
-    const size_t m             = t < capacity ? size_t(t) : capacity;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && overflow && t > capacity) *overflow = 1u;
-    const size_t head = min(size_t((16u - (reinterpret_cast<uintptr_t>(dst) & 15u)) / 4u & 3u), m);
-    const size_t nv   = (m - head) / 4;
-    if (blockIdx.x == 0)
-    {
-        if (threadIdx.x < head) dst[threadIdx.x] = src[threadIdx.x];
-        const size_t tail0 = head + 4 * nv;
-        if (tail0 + threadIdx.x < m) dst[tail0 + threadIdx.x] = src[tail0 + threadIdx.x];
-    }
-    // four loads in flight per thread before their stores: the host link needs about 1 MB of stores in flight, and
-    // the loads' latency grows while other kernels share the device
-    constexpr int U        = 4;
-    const unsigned stride  = gridDim.x * blockDim.x;
-    const unsigned tid     = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint4* sp        = reinterpret_cast<const uint4*>(src + head) + tid;
-    uint4* dp              = reinterpret_cast<uint4*>(dst + head) + tid;
-    size_t left            = nv > tid ? (nv - tid + stride - 1) / stride : 0; // this thread's 16-byte words
-    for (; left >= U; left -= U)
-    {
-        uint4 r[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            r[u] = __ldcs(sp + u * stride);
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            dp[u * stride] = r[u];
-        sp += U * stride;
-        dp += U * stride;
-    }
-    for (; left > 0; --left, sp += stride, dp += stride)
-        *dp = __ldcs(sp);
-}
-
-int copyListToHost(cudaStream_t s, const uint32_t* src, uint32_t* dst, const uint64_t* totalDev, size_t capacity,
-                   uint32_t* overflow)
-{
-    // the 16-byte loads and stores start at the same entry of src and dst: both must sit at the same place within
-    // 16 bytes (and on 4-byte boundaries)
-    const uintptr_t sa = reinterpret_cast<uintptr_t>(src), da = reinterpret_cast<uintptr_t>(dst);
-    if (!src || !totalDev || (capacity && !dst) || (sa & 3u) || (capacity && ((da & 3u) || (sa & 15u) != (da & 15u))))
-    {
-        setLastError("list copy: null pointer, or source and destination not aligned alike");
-        return CS_ERR_INVALID;
-    }
-    // 64 blocks saturate the host link (measured) while leaving the SMs to the next run's kernels. Each block is
-    // small (256 threads, at most 51 registers each): it fits beside a full share of the cooperative build's blocks,
-    // whose launch waits until all of its blocks can be resident
-    copyListKernel<<<64, 256, 0, s>>>(src, dst, totalDev, capacity, overflow);
-    CSG_CHECK_LAUNCH();
-    return CS_OK;
-}
-
 size_t neighborCsrWorkspaceBytes(size_t n) { return ((n + CSR_TILE - 1) / CSR_TILE + 1) * 8 + 256; }
 
 int neighborCsr(cudaStream_t s, const uint32_t* nb, const uint32_t* nc, size_t n, unsigned ngmax, uint64_t* offsets,

@@ -13,10 +13,4 @@ size_t neighborCsrWorkspaceBytes(size_t n);
 int neighborCsr(cudaStream_t s, const uint32_t* nb, const uint32_t* nc, size_t n, unsigned ngmax, uint64_t* offsets,
                 uint32_t* list, size_t capacity, void* ws, size_t wsBytes, uint32_t* overflow);
 
-/*! dst[k] = src[k] for k < min(*totalDev, capacity) (device src; pinned host or device dst; both 4-byte aligned and
- *  at the same offset within 16 bytes, else CS_ERR_INVALID); *overflow = 1 when *totalDev > capacity (overflow may
- *  be null). No host synchronisation. */
-int copyListToHost(cudaStream_t s, const uint32_t* src, uint32_t* dst, const uint64_t* totalDev, size_t capacity,
-                   uint32_t* overflow);
-
 } // namespace csg

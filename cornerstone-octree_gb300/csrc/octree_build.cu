@@ -722,8 +722,8 @@ int octreeBuildFinish(cudaStream_t s, void* ws, size_t wsBytes, int capacity, bo
         return CS_ERR_INVALID;
     }
     BuildState h;
-    CSG_CUDA_TRY(cudaMemcpyAsync(&h, l.st, sizeof(BuildState), cudaMemcpyDeviceToHost, s));
-    CSG_CUDA_TRY(cudaStreamSynchronize(s));
+    static_assert(sizeof(BuildState) % 4 == 0 && sizeof(BuildState) <= 4096, "read as at most 4 KB of 32-bit words");
+    if (int rc = readSmallToHost(s, &h, l.st, sizeof(BuildState))) return rc;
     if (res)
     {
         res->numLeaves  = h.L;

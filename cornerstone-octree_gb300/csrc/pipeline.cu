@@ -75,7 +75,7 @@ struct Pipeline final : PipelineBase
     bool inUsedRec[2]                = {false, false};
     // results to host: with lists, the compaction first, on the compute stream (outReady after it); then the error
     // words (errCopied), counts and flags (reuseReady: the next run may overwrite its outputs) on d2hStream, and the
-    // compacted lists (from one of two device buffer sets in turn) on listStream (outDone)
+    // offsets and compacted lists (from one of two device buffer sets in turn) on listStream (outDone)
     cudaStream_t d2hStream = nullptr, listStream = nullptr;
     cudaEvent_t outReady = nullptr, errCopied = nullptr, reuseReady = nullptr, outDone = nullptr;
     cudaEvent_t listCopied[2]  = {};  // on listStream after the copy out of compaction buffer b
@@ -83,8 +83,18 @@ struct Pipeline final : PipelineBase
     bool cbTimed               = false;
     bool listCopiedRec[2]      = {false, false};
     int csrCur                 = 0;
-    uint32_t* herrHost         = nullptr; // pinned, the last copied error words
-    uint32_t* listOverflowHost = nullptr; // pinned, set by the list copy when a list buffer was too small
+    uint32_t* herrHost         = nullptr; // pinned and mapped, the last copied error words (herrDev: device view)
+    uint32_t* herrDev          = nullptr;
+    uint32_t* listTotalHost    = nullptr; // pinned and mapped: the list total of compaction buffer set b at [2 b]
+    uint32_t* listTotalDev     = nullptr;
+    uint32_t* listOverflowHost = nullptr; // pinned, set when a list buffer was too small
+    struct PendingList
+    {
+        bool on      = false;
+        int b        = 0;
+        uint32_t* dst = nullptr;
+        size_t cap   = 0;
+    } pendingList; // a copy-back whose list copy is not yet enqueued
     DevBuf csrWs, csrOff[2], csrList[2]; // the compacted lists on the device (two sets in turn), copied to the host
     bool outPending      = false;   // a copy-back whose errors are not yet reported
     int stickyRc         = CS_OK;   // an earlier run's device error, reported by the next wait
@@ -120,6 +130,7 @@ struct Pipeline final : PipelineBase
                               cbEv[2], cbEv[3]})
             if (e) cudaEventDestroy(e);
         if (herrHost) cudaFreeHost(herrHost);
+        if (listTotalHost) cudaFreeHost(listTotalHost);
         if (listOverflowHost) cudaFreeHost(listOverflowHost);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
@@ -375,6 +386,7 @@ struct Pipeline final : PipelineBase
              const cs_box& box, bool useGraph, cs_pipeline_result* res) override
     {
         int rc;
+        if ((rc = flushListCopy())) return rc;
         if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, reuseReady, 0)); // a copy-back still reads the outputs
         lastNIn = 0; // autotune reruns plain runs only (a step's inputs need not outlive it)
         if (incCur < 0 || nIn != incN)
@@ -636,6 +648,9 @@ struct Pipeline final : PipelineBase
             break;
         }
         const int L = br.numLeaves, I = (L - 1) / 7, N = L + I;
+        // the build's result was read on the host: everything before it on this stream is done, the previous call's
+        // list compaction included, so its list copy can be sized and enqueued now
+        if ((rc = flushListCopy())) return rc;
 
         // ---- internal tree ----
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_LINK], s));
@@ -812,8 +827,7 @@ struct Pipeline final : PipelineBase
         }
         if (!d2hStream)
         {
-            // the highest priority: the block scheduler then places the compaction's and the list copy's blocks as
-            // soon as blocks of the next run's kernels retire, instead of after those kernels' last blocks
+            // the highest priority: the one-warp copies of error words run as soon as a slot frees
             int lowPrio = 0, highPrio = 0;
             CSG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lowPrio, &highPrio));
             CSG_CUDA_TRY(cudaStreamCreateWithPriority(&d2hStream, cudaStreamNonBlocking, highPrio));
@@ -822,8 +836,12 @@ struct Pipeline final : PipelineBase
                 CSG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
             for (cudaEvent_t& e : cbEv)
                 CSG_CUDA_TRY(cudaEventCreate(&e));
-            CSG_CUDA_TRY(cudaHostAlloc(&herrHost, 4 * sizeof(uint32_t), cudaHostAllocDefault));
-            CSG_CUDA_TRY(cudaHostAlloc(&listOverflowHost, sizeof(uint32_t), cudaHostAllocMapped));
+            CSG_CUDA_TRY(cudaHostAlloc(&herrHost, 4 * sizeof(uint32_t), cudaHostAllocPortable | cudaHostAllocMapped));
+            CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&herrDev), herrHost, 0));
+            CSG_CUDA_TRY(
+                cudaHostAlloc(&listTotalHost, 4 * sizeof(uint32_t), cudaHostAllocPortable | cudaHostAllocMapped));
+            CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&listTotalDev), listTotalHost, 0));
+            CSG_CUDA_TRY(cudaHostAlloc(&listOverflowHost, sizeof(uint32_t), cudaHostAllocDefault));
             *listOverflowHost = 0;
         }
         if (outPending)
@@ -837,24 +855,17 @@ struct Pipeline final : PipelineBase
                 std::snprintf(stickyMsg, sizeof(stickyMsg), "%s", cs_last_error());
             }
         }
+        if (int rc = flushListCopy()) return rc; // a previous call's list (normally already enqueued by run)
         const size_t devCap = listOffsets ? std::min(listCap, n * size_t(cfg.ngmax)) : 0;
         const int b         = csrCur;
-        if (listHost && (reinterpret_cast<uintptr_t>(listHost) & 3u))
-        {
-            setLastError("pipeline: the neighbour list buffer must be 4-byte aligned");
-            return CS_ERR_INVALID;
-        }
-        // the compacted list starts at the host buffer's offset within 16 bytes, so that the copy's 16-byte loads and
-        // stores are aligned on both sides
-        const size_t phase = (reinterpret_cast<uintptr_t>(listHost) & 15u) / 4u;
         if (listOffsets)
         {
             // the stored neighbour indices compacted on the compute stream, right after the run (a full-bandwidth
-            // pass of about 2 ms at 16M; beside the next run it would slow that run's sort and hold up its
-            // cooperative build), into buffer set b once the copy out of it two calls ago has finished (a buffer that
-            // grows is freed first: wait on the host for its last reader)
+            // pass of about 2 ms at 16M; beside the next run it would slow that run's sort), into buffer set b once
+            // the copy out of it two calls ago has finished (a buffer that grows is freed first: wait on the host for
+            // its last reader); the total goes to mapped host memory for the list copy's size
             const size_t wsNeed = neighborCsrWorkspaceBytes(n), offNeed = (n + 1) * sizeof(uint64_t);
-            const size_t listNeed = (devCap + 4) * sizeof(uint32_t);
+            const size_t listNeed = std::max<size_t>(devCap, 1) * sizeof(uint32_t);
             if (listCopiedRec[b] && (offNeed > csrOff[b].bytes || listNeed > csrList[b].bytes))
                 CSG_CUDA_TRY(cudaEventSynchronize(listCopied[b]));
             int rc = csrWs.ensure(wsNeed);
@@ -864,13 +875,18 @@ struct Pipeline final : PipelineBase
             if (listCopiedRec[b]) CSG_CUDA_TRY(cudaStreamWaitEvent(s, listCopied[b], 0));
             CSG_CUDA_TRY(cudaEventRecord(cbEv[0], s));
             if ((rc = neighborCsr(s, nb.as<uint32_t>(), nc.as<uint32_t>(), n, cfg.ngmax, csrOff[b].as<uint64_t>(),
-                                  csrList[b].as<uint32_t>() + phase, devCap, csrWs.p, csrWs.bytes, nullptr)))
+                                  csrList[b].as<uint32_t>(), devCap, csrWs.p, csrWs.bytes, nullptr)))
                 return rc;
+            copyWordsKernel<<<1, 32, 0, s>>>(reinterpret_cast<const uint32_t*>(csrOff[b].as<uint64_t>() + n),
+                                             listTotalDev + 2 * b, 2);
+            CSG_CHECK_LAUNCH();
             CSG_CUDA_TRY(cudaEventRecord(cbEv[1], s));
         }
         CSG_CUDA_TRY(cudaEventRecord(outReady, s));
         CSG_CUDA_TRY(cudaStreamWaitEvent(d2hStream, outReady, 0));
-        CSG_CUDA_TRY(cudaMemcpyAsync(herrHost, errWords.p, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, d2hStream));
+        // the error words by a one-warp kernel into mapped memory: no copy engine, so they never queue behind lists
+        copyWordsKernel<<<1, 32, 0, d2hStream>>>(errWords.as<uint32_t>(), herrDev, 4);
+        CSG_CHECK_LAUNCH();
         CSG_CUDA_TRY(cudaEventRecord(errCopied, d2hStream));
         if (ncHost)
             CSG_CUDA_TRY(cudaMemcpyAsync(ncHost, nc.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, d2hStream));
@@ -878,25 +894,15 @@ struct Pipeline final : PipelineBase
             CSG_CUDA_TRY(
                 cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, d2hStream));
         CSG_CUDA_TRY(cudaEventRecord(reuseReady, d2hStream));
-        // everything after the compaction runs on listStream, in call order
         CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, outReady, 0));
         if (listOffsets)
         {
-            CSG_CUDA_TRY(cudaEventRecord(cbEv[2], listStream));
-            // to the caller's pinned buffers: the offsets by the copy engine, the list by 16-byte stores whose
-            // length the compaction left in device memory
+            // the offsets now; the list itself by the copy engine once its length is known on the host, which is
+            // when the next call (run, step or wait) has seen this compaction finish (flushListCopy)
             CSG_CUDA_TRY(cudaMemcpyAsync(listOffsets, csrOff[b].p, (n + 1) * sizeof(uint64_t),
                                          cudaMemcpyDeviceToHost, listStream));
-            uint32_t* flag = nullptr;
-            CSG_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&flag), listOverflowHost, 0));
-            int rc = copyListToHost(listStream, csrList[b].as<uint32_t>() + phase, listHost,
-                                    csrOff[b].as<uint64_t>() + n, listHost ? listCap : 0, flag);
-            if (rc) return rc;
-            CSG_CUDA_TRY(cudaEventRecord(cbEv[3], listStream));
-            CSG_CUDA_TRY(cudaEventRecord(listCopied[b], listStream));
-            listCopiedRec[b] = true;
-            cbTimed          = true;
-            csrCur           = 1 - b;
+            pendingList = PendingList{true, b, listHost, listHost ? listCap : 0};
+            csrCur      = 1 - b;
         }
         CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, reuseReady, 0)); // outDone: the counts and flags too
         CSG_CUDA_TRY(cudaEventRecord(outDone, listStream));
@@ -904,8 +910,33 @@ struct Pipeline final : PipelineBase
         return CS_OK;
     }
 
+    // Enqueue the list copy of the last copy-back that returned lists, if not done yet: waits (on the host) for that
+    // run's compaction, reads the total from mapped memory and copies min(total, capacity) entries on listStream.
+    int flushListCopy()
+    {
+        if (!pendingList.on) return CS_OK;
+        const PendingList pl = pendingList;
+        pendingList.on       = false;
+        CSG_CUDA_TRY(cudaEventSynchronize(cbEv[1]));
+        uint64_t total = 0;
+        std::memcpy(&total, const_cast<const uint32_t*>(listTotalHost) + 2 * pl.b, sizeof(total));
+        const size_t m = size_t(std::min<uint64_t>(total, pl.cap));
+        if (total > pl.cap) *listOverflowHost = 1;
+        CSG_CUDA_TRY(cudaEventRecord(cbEv[2], listStream));
+        if (m)
+            CSG_CUDA_TRY(cudaMemcpyAsync(pl.dst, csrList[pl.b].p, m * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                         listStream));
+        CSG_CUDA_TRY(cudaEventRecord(cbEv[3], listStream));
+        CSG_CUDA_TRY(cudaEventRecord(listCopied[pl.b], listStream));
+        listCopiedRec[pl.b] = true;
+        cbTimed             = true;
+        CSG_CUDA_TRY(cudaEventRecord(outDone, listStream));
+        return CS_OK;
+    }
+
     int copyTimes(float* ms, int count) override
     {
+        if (int rc = flushListCopy()) return rc;
         if (!cbTimed)
         {
             setLastError("copy times: no copy-back with neighbour lists yet");
@@ -922,7 +953,8 @@ struct Pipeline final : PipelineBase
     // Wait for the last copy-back; report the first device error of the runs since the previous wait.
     int wait() override
     {
-        int rc = CS_OK;
+        int rc = flushListCopy();
+        if (rc) return rc;
         if (outPending)
         {
             CSG_CUDA_TRY(cudaEventSynchronize(outDone));
