@@ -59,6 +59,10 @@ def parse():
                         "the neighbour-list consumers on the 16M Plummer particles (cluster-pair lists built and an "
                         "SPH density summed over them, and the same sum over the stored neighbour lists)")
     p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--ijloop-dist", default="plummer", choices=["plummer", "uniform"],
+                   help="particles of the ijloop workload: the Plummer sphere (the benchmark), or uniform in the unit "
+                        "cube (small profiling cases: the Plummer sphere's sparse outskirts need long cluster lists "
+                        "at small n)")
     p.add_argument("--cpu-sample", type=int, default=1 << 20, help="particles of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -556,7 +560,10 @@ def run_ijloop(args, world, rank, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     n = args.n or 16 * 1024 * 1024
-    x, y, z = W.plummer(n, args.seed + rank)
+    if args.ijloop_dist == "plummer":
+        x, y, z = W.plummer(n, args.seed + rank)
+    else:
+        x, y, z = W.uniform(n, 0.0, 1.0, args.seed + rank)
     lo, hi = W.tight_box(x, y, z)
     box = cs.make_box(lo, hi)
     tx, ty, tz = (torch.from_numpy(a).to(dev) for a in (x, y, z))
@@ -602,14 +609,19 @@ def run_ijloop(args, world, rank, local):
     algo = n * 48 + 4 * listed
     achieved = algo / (loop_ms * 1e-3) / 1e9
     if rank == 0:
-        line = {"metric": "Mparticles/s neighbour-list consumers: cluster-pair lists + SPH density (16M Plummer, FP64)",
+        dist = "Plummer" if args.ijloop_dist == "plummer" else "uniform"
+        line = {"metric": f"Mparticles/s neighbour-list consumers: cluster-pair lists + SPH density "
+                          f"({n / 2 ** 20:g}M {dist}, FP64)",
                 "value": round(world * n / (step_ms * 1e-3) / 1e6, 3), "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic",
-                "config": {"workload": "ijloop-density", "n_particles_per_gpu": n, "neighbours_target": K_NEIGHBORS,
+                "config": {"workload": "ijloop-density", "particles": args.ijloop_dist, "n_particles_per_gpu": n,
+                           "neighbours_target": K_NEIGHBORS,
                            "cluster": 8, "ncmax": ncmax, "keys": "hilbert64", "bucket_size": BUCKET,
-                           "l2": "inputs (640 MB) larger than L2", "parallelism": f"replicas x{world}"},
+                           "l2": f"inputs ({n * 40 / 1e6:.0f} MB) "
+                                 f"{'larger' if n * 40 > 129e6 else 'smaller'} than L2",
+                           "parallelism": f"replicas x{world}"},
                 "stages_ms": {"cluster_lists": round(build_ms, 4), "density_over_clusters": round(loop_ms, 4),
                               "density_over_stored_lists": round(list_ms, 4)},
                 "pair_tests_per_neighbour": round(8 * listed * 8 / max(1.0, float(nc.double().sum())), 3),

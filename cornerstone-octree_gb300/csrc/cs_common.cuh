@@ -440,6 +440,11 @@ int readSmallToHost(cudaStream_t s, void* hostDst, const void* devSrc, size_t by
 // dst[k] = src[k], k < words: one warp; dst may be mapped pinned host memory
 __global__ void copyWordsKernel(const uint32_t* src, uint32_t* dst, unsigned words);
 
+// Device memory to host memory on stream s. Pinned (page-locked) destinations are written by a small kernel through
+// their device mapping (16-byte stores where source and destination are aligned alike): the copy does not queue
+// behind other streams' copies on the copy engines. Other destinations go through cudaMemcpyAsync.
+int copyToHostAsync(cudaStream_t s, void* hostDst, const void* devSrc, size_t bytes);
+
 // Bounds of the device-side waits, read by the host at each launch and passed as kernel arguments. The defaults
 // give up after about a second; cs_set_wait_limits lowers them and can make one wait stall on purpose (a flag that
 // nothing sets), so that tests reach the timeout path on ordinary inputs.

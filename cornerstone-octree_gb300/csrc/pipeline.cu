@@ -888,11 +888,12 @@ struct Pipeline final : PipelineBase
         copyWordsKernel<<<1, 32, 0, d2hStream>>>(errWords.as<uint32_t>(), herrDev, 4);
         CSG_CHECK_LAUNCH();
         CSG_CUDA_TRY(cudaEventRecord(errCopied, d2hStream));
+        // counts and flags: the next run waits for them (reuseReady), so they must not queue behind a list copy on
+        // the copy engines; pinned destinations are written by a small kernel instead
         if (ncHost)
-            CSG_CUDA_TRY(cudaMemcpyAsync(ncHost, nc.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, d2hStream));
+            if (int rc = copyToHostAsync(d2hStream, ncHost, nc.p, n * sizeof(uint32_t))) return rc;
         if (flagsHost)
-            CSG_CUDA_TRY(
-                cudaMemcpyAsync(flagsHost, flags.p, size_t(last.num_nodes), cudaMemcpyDeviceToHost, d2hStream));
+            if (int rc = copyToHostAsync(d2hStream, flagsHost, flags.p, size_t(last.num_nodes))) return rc;
         CSG_CUDA_TRY(cudaEventRecord(reuseReady, d2hStream));
         CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, outReady, 0));
         if (listOffsets)
