@@ -191,6 +191,21 @@ def profile_figures(n):
     return fig
 
 
+def density_profile_figures():
+    """the cluster density loop's FP64 pipe activity from its committed ncu summary (None where absent)"""
+    path = os.path.join(ROOT, "profiles", "ijloop_density_uniform4m.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("fp64_pipe_active_fraction:"):
+                    return {"fp64_pipe_active": float(line.split(":")[1]),
+                            "source": "ncu capture of the 4194304-particle uniform case "
+                                      "(profiles/ijloop_density_uniform4m.md)"}
+    except OSError:
+        pass
+    return None
+
+
 # ---------------------------------------------------------------------------------------------------------------
 # CPU side (oracle): bounded sample of the workload
 # ---------------------------------------------------------------------------------------------------------------
@@ -628,7 +643,9 @@ def run_ijloop(args, world, rank, local):
                 "roofline": {"kernel": "densityClusterKernel<double>", "bound": "fp64",
                              "achieved": round(achieved, 1), "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "algorithmic_bytes": algo,
-                             "note": "hbm fraction of the loop; its distance tests and kernel run in FP64"},
+                             "note": "the hbm fraction above is small by construction: the loop's exact tests and "
+                                     "interaction terms run on the FP64 pipe, whose activity is below",
+                             "fp64_pipe": density_profile_figures()},
                 "stored_lists_complete": complete, "rho_identical_frac": agree,
                 "rho_identical_note": "the cluster loop sums over every j within 2 h_i (checked against a brute-force "
                                       "sum); the stored lists follow findNeighbors, which looks only into leaves "

@@ -544,10 +544,12 @@ int cs_pipeline_wait(cs_pipeline p);
 /* The host-buffer runs above with the neighbour lists returned as well, in compressed sparse row form: row i's first
  * min(nc_i, ngmax) neighbours (ascending, as findNeighbors stores them into its ngmax-strided `neighbors` argument,
  * findneighbors.hpp:156-177) are list_host[offsets_host[i] .. offsets_host[i+1]), offsets_host has n + 1 entries and
- * offsets_host[n] is the total. Both buffers must be pinned host memory (cudaHostAlloc / cudaHostRegister): the
- * lists are compacted on the device and written straight into them over the host link, on the copy-back stream.
- * Entries past list_capacity are not written and the wait reports CS_ERR_CAPACITY (offsets_host[n] = entries
- * needed). The _async form follows cs_pipeline_run_host_async (results valid after cs_pipeline_wait). */
+ * offsets_host[n] is the total. Pinned host buffers (cudaHostAlloc / cudaHostRegister) give the full host-link rate.
+ * The lists are compacted on the device right after the run (on `stream`); the offsets, counts and flags are copied
+ * at once, and the list itself by the copy engine once its length is known on the host: at the pipeline's next call
+ * (run, step or wait), which has already waited for that compaction. Entries past list_capacity are not written and
+ * the wait reports CS_ERR_CAPACITY (offsets_host[n] = entries needed). The _async form follows
+ * cs_pipeline_run_host_async (results valid after cs_pipeline_wait). */
 int cs_pipeline_run_host_csr(cs_pipeline p, cs_stream_t stream, const void* x, const void* y, const void* z,
                              const void* h, size_t n, const cs_box* box, uint64_t focus_start, uint64_t focus_end,
                              uint32_t* neighbor_counts_host, uint8_t* halo_flags_host, size_t halo_flags_capacity,
