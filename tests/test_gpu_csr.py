@@ -132,3 +132,21 @@ def test_list_copy_survives_the_next_runs(cs, O):
         assert np.array_equal(lst.numpy()[: roff[-1]].view(np.uint32), rlst), follow
         out = pipe.outputs()
         assert np.array_equal(u32(out["neighbor_counts"]), refb["nc"]), follow
+
+
+def test_pipeline_run_host_with_pageable_outputs(cs, O):
+    """counts, flags and lists into ordinary (pageable) host memory: the copies that a kernel makes into pinned buffers
+    go through the copy engine instead, with the same results"""
+    n, ngmax = 30_000, 48
+    x, y, z, h, ref = _case(O, n, ngmax, 0.05, 21)
+    roff, rlst = _oracle_csr(ref["nb"], ref["nc"], ngmax)
+    hx, hy, hz, hh = (torch.from_numpy(a).pin_memory() for a in (x, y, z, h))
+    off = torch.empty(n + 1, dtype=torch.int64)
+    lst = torch.empty(int(roff[-1]) + 3, dtype=torch.int32)
+    nc = torch.empty(n, dtype=torch.int32)
+    assert not (off.is_pinned() or lst.is_pinned() or nc.is_pinned())
+    pipe = cs.Pipeline(64, 64, cs.HILBERT, 16, ngmax, 1.0, 1.0, False, True)
+    pipe.run_host_csr(hx, hy, hz, hh, cs.make_box(-1.0, 60.0), (0, 0), off, lst, nc_out=nc)
+    assert np.array_equal(nc.numpy().view(np.uint32), ref["nc"])
+    assert np.array_equal(off.numpy(), roff)
+    assert np.array_equal(lst.numpy()[: roff[-1]].view(np.uint32), rlst)
