@@ -886,6 +886,12 @@ def cluster_nblist(x, y, z, h, box, tree, layout, centers, sizes, key_bits=64, n
                 C.c_uint(ncmax), _p(lists), _p(counts), None, C.c_size_t(0), C.byref(mx))
         if rc == CS_ERR_CAPACITY:
             ncmax = mx.value
+            need = nic * ncmax * 4
+            free, _ = torch.cuda.mem_get_info(x.device)
+            if need > free:
+                raise CsError(CS_ERR_CAPACITY, f"cluster lists: the longest list needs ncmax = {ncmax}, "
+                                               f"{need / 2 ** 30:.1f} GiB for {nic} i-clusters ({free / 2 ** 30:.1f} "
+                                               f"GiB free)")
             continue
         _check(rc)
         return lists, counts
