@@ -6,9 +6,10 @@
 // sum_{k<i} min(nc_k, ngmax) (u64, n + 1 entries, offsets[n] = total) and list[offsets[i] .. offsets[i+1]) = row i.
 //
 // Three kernels: per tile of rows the sum of the stored counts; one block scans the tile sums; per tile a block scan
-// gives each row's offset and the block's warps copy their rows. Outputs may be device memory or pinned host memory
-// (the kernels write it directly over the host link, so no separate copy and no host-side knowledge of the total is
-// needed). Entries past list_capacity are not written; offsets[n] always holds the total, so the caller can tell.
+// gives each row's offset and the block's warps copy their rows (a null list: offsets only). Outputs may be device
+// memory or pinned host memory (the kernels then write over the host link, with no host-side knowledge of the total).
+// Entries past list_capacity are not written; offsets[n] always holds the total, so the caller can tell. The
+// pipeline's host-buffer runs compact into device memory and copy the list to the host with the copy engine.
 //
 // Algorithmic bytes: reads 4 n (counts) + 4 total (stored entries), writes 8 (n + 1) + 4 total.
 #include "cs_common.cuh"
