@@ -28,7 +28,11 @@
 // d2 < min(r2, Tsafe) are accepted outright; the rare ones in [Tsafe, r2) (only when ext < 1 + O(kappa)) walk the
 // ancestor chain explicitly through parents[] with the reference's cell test.
 //
-// Arithmetic. T = float evaluates the reference's expressions with round-to-nearest intrinsics (no contraction).
+// Arithmetic. T = float decides with the reference's expressions in round-to-nearest intrinsics (no contraction). The
+// one-target-per-lane loops first evaluate the squared distance of the reference's own differences with packed FMAs,
+// fma(dz, dz, fma(dy, dy, dx dx)); it and the reference's RN(RN(RN(dx dx) + RN(dy dy)) + RN(dz dz)) are each within
+// 3 u d2 + 3 2^-150 of the exact sum (u = 2^-24), so below min(r2, Tsafe) (1 - 8 u) - 2^-146 the pair is a path-safe
+// neighbour, from r2 (1 + 8 u) + 2^-146 on it is not, and only the band between is evaluated again unfused.
 // T = double (GB300 has little FP64 throughput) first evaluates each test in FP32 on coordinates relative to a
 // per-warp reference point P, with a proven bound on the difference to the FP64 result:
 //   candidate  a_j = fl((xhi_j - P) + xlo_j)  (x = xhi + xlo, two floats),  target b_i = fl(x_i - P)
@@ -426,6 +430,10 @@ constexpr int NBG_STACK = 192;
 #ifndef NBG_MIN_BLOCKS
 #define NBG_MIN_BLOCKS 8
 #endif
+// leaves merged into one candidate range at most (one target per lane)
+#ifndef NBG_MERGE
+#define NBG_MERGE 4
+#endif
 
 // exact decision of a pair in the ambiguous band (T = double): d2 < r2 and the reference's path condition
 __device__ __noinline__ bool pairDecideF64(double xi, double yi, double zi, double r2, double cellR2, double kappa,
@@ -500,10 +508,13 @@ __device__ __forceinline__ void loadTarget(const TargetRef<T>& t, T& xi, T& yi, 
     targetRadii<T>(t.h, t.hf, t.i, t.ext, r2, cellR2, twoh);
 }
 
-// a candidate in the FP32 band (T = double) or past Tsafe (T = float): the pair and path decision
+// a candidate in the band of the FP32 filter: the pair decision in the reference's arithmetic (T = double: FP64;
+// T = float: the unfused FP32 distance) and the path condition (path-safe below tsafe when the candidate lies inside
+// its leaf's box, else the ancestor walk)
 template<class T>
-__device__ __noinline__ bool slowPairAt(TargetRef<T> t, float kappa, uint32_t j, int leafNode, const int32_t* parents,
-                                        const T* centers, const T* sizes, bool contained, int rootNode)
+__device__ __noinline__ bool slowPairAt(TargetRef<T> t, float kappa, float tsafe, uint32_t j, int leafNode,
+                                        const int32_t* parents, const T* centers, const T* sizes, bool contained,
+                                        int rootNode)
 {
     T xi, yi, zi, r2, cellR2;
     loadTarget(t, xi, yi, zi, r2, cellR2);
@@ -511,8 +522,13 @@ __device__ __noinline__ bool slowPairAt(TargetRef<T> t, float kappa, uint32_t j,
         return pairDecideF64(xi, yi, zi, r2, cellR2, double(kappa), t.x, t.y, t.z, j, leafNode, parents, centers,
                              sizes, contained, rootNode);
     else
-        return pathCheckF32(float(xi), float(yi), float(zi), float(cellR2), leafNode, parents,
-                            reinterpret_cast<const float*>(centers), reinterpret_cast<const float*>(sizes), rootNode);
+    {
+        const float dx = __fsub_rn(t.x[j], xi), dy = __fsub_rn(t.y[j], yi), dz = __fsub_rn(t.z[j], zi);
+        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        if (!(d2 < r2)) return false;
+        if (contained && d2 < tsafe) return true;
+        return pathCheckF32(xi, yi, zi, cellR2, leafNode, parents, centers, sizes, rootNode);
+    }
 }
 
 // the path condition to a leaf (its candidates outside its box have no path-safe shortcut)
@@ -536,6 +552,15 @@ __device__ __noinline__ bool pairWithinAt(TargetRef<double> t, uint32_t j)
     loadTarget(t, xi, yi, zi, r2, cellR2);
     const PbcArgs open{};
     return pairExactF64(xi, yi, zi, false, r2, t.x, t.y, t.z, j, open);
+}
+
+// exact d2 < r2 of a pair in the reference's FP32 arithmetic (T = float, no periodic axis)
+__device__ __noinline__ bool pairWithinAt(TargetRef<float> t, uint32_t j)
+{
+    float xi, yi, zi, r2, cellR2;
+    loadTarget(t, xi, yi, zi, r2, cellR2);
+    const float dx = __fsub_rn(t.x[j], xi), dy = __fsub_rn(t.y[j], yi), dz = __fsub_rn(t.z[j], zi);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)) < r2;
 }
 
 __device__ __forceinline__ float warpMinF(float v)
@@ -566,6 +591,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     // S == 1: each lane's target for the by-target loop: negated frame coordinates and -Tin, and -Tup
     __shared__ float4 sTgtA[NB_WARPS][32];
     __shared__ float sTgtB[NB_WARPS][32];
+    // S == 1: leaves merged into one candidate range (their particle ranges adjoin): end of each range and its node
+    __shared__ int2 sMerge[NB_WARPS][NBG_MERGE];
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int t = lane % G, s = lane / G;
@@ -783,8 +810,11 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     }
     else
     {
-        Tin = fminf(float(r2), tsafe);
-        Tup = float(r2);
+        // the packed FMA distance of the batch loops is within 6 u d2 + 6 2^-150 of the reference's unfused FP32
+        // value (u = 2^-24, three roundings each, subnormal results included): below Tin the pair is a path-safe
+        // neighbour, from Tup on it is not; the band between is decided exactly (decideSlow)
+        Tin = __fsub_rd(__fmul_rd(fminf(float(r2), tsafe), 1.f - 8 * EPS), 0x1p-146f);
+        Tup = __fadd_ru(__fmul_ru(float(r2), 1.f + 8 * EPS), 0x1p-146f);
     }
     // minus the target in the candidates' frame, as float pairs for the packed distance evaluation
     float nbS[3];
@@ -809,7 +839,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     }
     const TargetRef<T> tref{a.x, a.y, a.z, a.h, a.hf, a.ext, i};
     auto decideSlow = [&](uint32_t jj, int node, bool contained) -> bool {
-        return slowPairAt<T>(tref, kappa, jj, node, a.parents, a.centers, a.sizes, contained, rootNode);
+        return slowPairAt<T>(tref, kappa, tsafe, jj, node, a.parents, a.centers, a.sizes, contained, rootNode);
     };
     // first filter: FP32 distance of the staged candidate; returns d2 and whether it can be a neighbour
     auto filter = [&](float4 c, float& d2) -> bool {
@@ -845,13 +875,17 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     };
 
     // a leaf with its record r0..r2: the lanes whose sphere may reach it test its particles, 32 per batch
-    auto processLeaf = [&](int node, unsigned pmask, float4 recA, float4 recB, float4 recC, bool anyOut) {
-        const uint32_t first = __float_as_uint(recB.w), last = __float_as_uint(recC.w);
+    // a leaf with its record r0..r2: the lanes whose sphere may reach it test its particles, 32 per batch. With
+    // nMerged > 1 (S == 1) the following leaves of sMerge are tested with it as one range [first, lastM): needM is
+    // this lane's need of any of them
+    auto processLeaf = [&](int node, unsigned pmask, float4 recA, float4 recB, float4 recC, bool anyOut, int nMerged,
+                           uint32_t lastM, bool needM) {
+        const uint32_t first = __float_as_uint(recB.w), last = nMerged > 1 ? lastM : __float_as_uint(recC.w);
         // the first batch is loaded before the lanes' box test, so that the two latencies overlap
         float4 q0 = stage(first + lane, last);
         float cc[3], sz[3];
         frameOf(recA, recB, recC, cc, sz);
-        bool need     = ((pmask >> lane) & 1u) && mayHitBox(cc, sz);
+        bool need     = (((pmask >> lane) & 1u) && mayHitBox(cc, sz)) || needM;
         unsigned mask = __ballot_sync(0xffffffffu, need);
         if (mask == 0) return;
         // a leaf holding particles outside its box: whether this lane's path to it passes the reference's cell tests.
@@ -935,24 +969,12 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                         float2 dx = __fadd2_rn(cx, n[0]);
                         float2 dy = __fadd2_rn(cy, n[1]);
                         float2 dz = __fadd2_rn(cz, n[2]);
-                        float2 e;
-                        if constexpr (F64)
-                        {
-                            // an FP32 filter with proven margins: any rounding of these FMAs stays inside them
-                            e = __fmul2_rn(dx, dx);
-                            e = __ffma2_rn(dy, dy, e);
-                            e = __ffma2_rn(dz, dz, e);
-                        }
-                        else
-                        {
-                            // the reference's FP32 distance itself, so no product may be fused into the next add:
-                            // scalar __fmul_rn / __fadd_rn (a packed multiply followed by a packed add was measured to
-                            // round once, as a fused multiply-add, even with explicit rounding modifiers)
-                            auto d2 = [](float a, float b, float c) {
-                                return __fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c));
-                            };
-                            e = make_float2(d2(dx.x, dy.x, dz.x), d2(dx.y, dy.y, dz.y));
-                        }
+                        // an FP32 filter with proven margins (the thresholds): any rounding of these FMAs stays
+                        // inside them. T = float: the differences are the reference's own, and the band around r2
+                        // is decided again with its unfused expression
+                        float2 e = __fmul2_rn(dx, dx);
+                        e        = __ffma2_rn(dy, dy, e);
+                        e        = __ffma2_rn(dz, dz, e);
                         const float2 ti = __fadd2_rn(e, nin), tu = __fadd2_rn(e, nup);
                         mi = __funnelshift_l(__float_as_uint(ti.x), mi, 1);
                         mi = __funnelshift_l(__float_as_uint(ti.y), mi, 1);
@@ -980,8 +1002,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                         const float tup = sTgtB[warp][t];
                         const float dx = __fadd_rn(q.x, tg.x), dy = __fadd_rn(q.y, tg.y), dz = __fadd_rn(q.z, tg.z);
                         float e;
-                        if constexpr (F64) e = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                        else e = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        e = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
                         const unsigned mi = __ballot_sync(0xffffffffu, __float_as_int(__fadd_rn(e, tg.w)) < 0);
                         const unsigned ma = __ballot_sync(0xffffffffu, __float_as_int(__fadd_rn(e, tup)) < 0);
                         if (lane == t)
@@ -1015,25 +1036,21 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     const unsigned outR = __brev(outB); // bit 31 - k: candidate k lies outside its leaf's box
                     // candidates outside their leaf's box: no path-safe shortcut; a neighbour iff within r and the
                     // lane's path to the leaf passes. Below Tin the FP32 bound already proves d2 < r2; the band
-                    // [Tin, Tup) is decided exactly (T = float: e < Tup is exactly d2 < r2)
+                    // [Tin, Tup) is decided exactly
                     const unsigned fIn = inM & outR, fAmb = ambM & outR;
                     inM &= ~outR;
                     ambM &= ~outR;
                     if (leafPass)
                     {
                         inM |= fIn;
-                        if constexpr (F64)
+                        // group warps have no periodic sphere
+                        unsigned f = fAmb;
+                        while (f)
                         {
-                            // group warps have no periodic sphere
-                            unsigned f = fAmb;
-                            while (f)
-                            {
-                                int k = __clz(f);
-                                f &= ~(0x80000000u >> k);
-                                if (pairWithinAt(tref, base + k)) inM |= 0x80000000u >> k;
-                            }
+                            int k = __clz(f);
+                            f &= ~(0x80000000u >> k);
+                            if (pairWithinAt(tref, base + k)) inM |= 0x80000000u >> k;
                         }
-                        else { inM |= fAmb; }
                     }
                     if constexpr (Stats)
                     {
@@ -1044,7 +1061,15 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     {
                         int k = __clz(ambM);
                         ambM &= ~(0x80000000u >> k);
-                        if (decideSlow(base + k, node, true)) inM |= 0x80000000u >> k;
+                        int kn = node;
+                        if (nMerged > 1)
+                            for (int m = 0; m < nMerged; ++m)
+                                if (base + k < uint32_t(sMerge[warp][m].x))
+                                {
+                                    kn = sMerge[warp][m].y;
+                                    break;
+                                }
+                        if (decideSlow(base + k, kn, true)) inM |= 0x80000000u >> k;
                     }
                     if (i >= base && i - base < 32u) inM &= ~(0x80000000u >> (i - base));
                     if constexpr (Stats) hitsThis = __popc(inM);
@@ -1151,7 +1176,40 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             float4 recA = rec[0], recB = rec[1], recC = rec[2];
             long long tl0 = Stats ? clock64() : 0;
             unsigned long long before = stLeaves;
-            processLeaf(node, pmask, recA, recB, recC, out);
+            // S == 1: the next leaves on the stack whose particles continue this leaf's range (siblings and cousins
+            // met consecutively in SFC order) join its candidate batch while the range stays within 32 particles; a
+            // lane then tests all of them, which changes no decision (a candidate outside a lane's sphere fails its
+            // distance test), and the batch overhead is paid once. Leaves holding particles outside their box stay alone
+            int nMerged    = 1;
+            uint32_t lastM = __float_as_uint(recC.w);
+            bool needM     = false;
+            if constexpr (S == 1)
+            {
+                const uint32_t first = __float_as_uint(recB.w);
+                while (!out && top > 0 && nMerged < NBG_MERGE && lastM - first < 32u)
+                {
+                    const int2 nx = stack[top - 1];
+                    if (nx.x > 0 || ((-nx.x - 1) & 1)) break; // an internal node, or a leaf with outside particles
+                    const int nnode    = (-nx.x - 1) >> 1;
+                    const float4* nrc  = prep.nrec + 3 * size_t(nnode);
+                    const float4 nB = nrc[1], nC = nrc[2];
+                    if (__float_as_uint(nB.w) != lastM || __float_as_uint(nC.w) - first > 32u) break;
+                    const float4 nA = nrc[0];
+                    float cc[3], sz[3];
+                    frameOf(nA, nB, nC, cc, sz);
+                    needM = needM || (((unsigned(nx.y) >> lane) & 1u) && mayHitBox(cc, sz));
+                    if (lane == 0)
+                    {
+                        if (nMerged == 1) sMerge[warp][0] = make_int2(int(lastM), node);
+                        sMerge[warp][nMerged] = make_int2(int(__float_as_uint(nC.w)), nnode);
+                    }
+                    lastM = __float_as_uint(nC.w);
+                    ++nMerged;
+                    --top;
+                }
+                if (nMerged > 1) __syncwarp();
+            }
+            processLeaf(node, pmask, recA, recB, recC, out, nMerged, lastM, needM);
             if constexpr (Stats)
             {
                 stLeafCyc += (unsigned long long)(clock64() - tl0);
