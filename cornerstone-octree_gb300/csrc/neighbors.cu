@@ -430,9 +430,12 @@ constexpr int NBG_STACK = 192;
 #ifndef NBG_MIN_BLOCKS
 #define NBG_MIN_BLOCKS 8
 #endif
-// leaves merged into one candidate range at most (one target per lane)
+// leaves merged into one candidate range at most (one target per lane), and the longest merged range
 #ifndef NBG_MERGE
 #define NBG_MERGE 4
+#endif
+#ifndef NBG_MERGE_SPAN
+#define NBG_MERGE_SPAN 32
 #endif
 
 // exact decision of a pair in the ambiguous band (T = double): d2 < r2 and the reference's path condition
@@ -1177,7 +1180,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             long long tl0 = Stats ? clock64() : 0;
             unsigned long long before = stLeaves;
             // S == 1: the next leaves on the stack whose particles continue this leaf's range (siblings and cousins
-            // met consecutively in SFC order) join its candidate batch while the range stays within 32 particles; a
+            // met consecutively in SFC order) join its candidate range while it stays within NBG_MERGE_SPAN
+            // particles; a
             // lane then tests all of them, which changes no decision (a candidate outside a lane's sphere fails its
             // distance test), and the batch overhead is paid once. Leaves holding particles outside their box stay alone
             int nMerged    = 1;
@@ -1186,14 +1190,15 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             if constexpr (S == 1)
             {
                 const uint32_t first = __float_as_uint(recB.w);
-                while (!out && top > 0 && nMerged < NBG_MERGE && lastM - first < 32u)
+                while (!out && top > 0 && nMerged < NBG_MERGE && lastM - first < unsigned(NBG_MERGE_SPAN))
                 {
                     const int2 nx = stack[top - 1];
                     if (nx.x > 0 || ((-nx.x - 1) & 1)) break; // an internal node, or a leaf with outside particles
                     const int nnode    = (-nx.x - 1) >> 1;
                     const float4* nrc  = prep.nrec + 3 * size_t(nnode);
                     const float4 nB = nrc[1], nC = nrc[2];
-                    if (__float_as_uint(nB.w) != lastM || __float_as_uint(nC.w) - first > 32u) break;
+                    if (__float_as_uint(nB.w) != lastM || __float_as_uint(nC.w) - first > unsigned(NBG_MERGE_SPAN))
+                        break;
                     const float4 nA = nrc[0];
                     float cc[3], sz[3];
                     frameOf(nA, nB, nC, cc, sz);
@@ -1456,26 +1461,48 @@ __global__ void prepNodesF32Kernel(const float* __restrict__ centers, const floa
     if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m));
 }
 
-// one warp per node: the particles of a leaf that lie outside its box (the exact test in T, as the reference's node
-// boxes are T values), and a marker in the leaf's record (child offset -1) when it holds any. For T = double most
-// particles are decided in FP32 on the float shadows: with u = 2^-24 the FP32 value of |x - c| - s is within
-// 4 u (|x| + |c| + s) of the exact one, so a value below -8 u (|hi| + |c_hi| + s_f) proves the particle inside.
+// eight lanes per node (four nodes per warp; leaves hold about 8 to 30 particles): the particles of a leaf that lie
+// outside its box (the exact test in T, as the reference's node boxes are T values), and a marker in the leaf's record
+// (child offset -1) when it holds any. For T = double most particles are decided in FP32 on the float shadows: with
+// u = 2^-24 the FP32 value of |x - c| - s is within 4 u (|x| + |c| + s) of the exact one, so a value below
+// -8 u (|hi| + |c_hi| + s_f) proves the particle inside.
+constexpr int MARK_LANES = 8;
+
 template<class T>
 __global__ void markOutsideKernel(const T* __restrict__ x, const T* __restrict__ y, const T* __restrict__ z,
                                   const float4* __restrict__ phi, const T* __restrict__ centers,
                                   const T* __restrict__ sizes, int Nhost, const int* Ldev, float4* __restrict__ nrec,
                                   uint8_t* __restrict__ pout)
 {
-    const int node = int((size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (node >= nodeCount(Ldev, Nhost)) return;
-    // the node's record: float box, child offset, particle range (one load round)
-    const float4 ch = nrec[3 * size_t(node)], cl = nrec[3 * size_t(node) + 1], sz = nrec[3 * size_t(node) + 2];
-    if (__float_as_int(ch.w) != 0) return;
-    const uint32_t first = __float_as_uint(cl.w), last = __float_as_uint(sz.w);
-    bool any = false;
-    for (uint32_t j0 = first; j0 < last; j0 += 32)
+    const size_t gtid = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int sub = int(gtid % MARK_LANES), lane = threadIdx.x & 31;
+    const unsigned segMask = 0xFFu << (lane & ~(MARK_LANES - 1));
+    const long long node   = (long long)(gtid / MARK_LANES);
+    // whole warps leave together past the last node; the others keep every lane for the segment votes
+    const int N = nodeCount(Ldev, Nhost);
+    if (__all_sync(0xffffffffu, node >= N)) return;
+    bool leaf      = false;
+    uint32_t first = 0, last = 0;
+    float4 ch = make_float4(0.f, 0.f, 0.f, 0.f), sz = ch;
+    if (node < N)
     {
-        const uint32_t j = j0 + lane;
+        // the node's record: float box, child offset, particle range (one load round)
+        ch = nrec[3 * size_t(node)];
+        const float4 cl = nrec[3 * size_t(node) + 1];
+        sz              = nrec[3 * size_t(node) + 2];
+        leaf            = __float_as_int(ch.w) == 0;
+        first           = __float_as_uint(cl.w);
+        last            = __float_as_uint(sz.w);
+    }
+    if (!leaf) first = last = 0;
+    bool any = false;
+    // rounds over the longest leaf of the warp's four, all eight lanes of a segment voting together
+    uint32_t cnt = last - first;
+    for (int o = MARK_LANES; o < 32; o <<= 1)
+        cnt = max(cnt, __shfl_xor_sync(0xffffffffu, cnt, o));
+    for (uint32_t j0 = 0; j0 < cnt; j0 += MARK_LANES)
+    {
+        const uint32_t j = first + j0 + uint32_t(sub);
         bool o           = false;
         if (j < last)
         {
@@ -1503,9 +1530,9 @@ __global__ void markOutsideKernel(const T* __restrict__ x, const T* __restrict__
             }
             pout[j] = o ? 1 : 0;
         }
-        any |= __any_sync(0xffffffffu, o);
+        any |= (__ballot_sync(0xffffffffu, o) & segMask) != 0u;
     }
-    if (any && lane == 0) nrec[3 * size_t(node)].w = __int_as_float(-1);
+    if (any && sub == 0) nrec[3 * size_t(node)].w = __int_as_float(-1);
 }
 
 template<class T>
@@ -1519,8 +1546,8 @@ int nbMarkOutside(cudaStream_t s, const T* x, const T* y, const T* z, const floa
         setLastError("find neighbors: the outside marks of FP64 particles need the float shadows");
         return CS_ERR_INVALID;
     }
-    markOutsideKernel<T><<<iceil(size_t(numNodes) * 32, 256), 256, 0, s>>>(x, y, z, phi, centers, sizes, numNodes,
-                                                                          Ldev, const_cast<float4*>(prep.nrec), pout);
+    markOutsideKernel<T><<<iceil(size_t(numNodes) * MARK_LANES, 256), 256, 0, s>>>(
+        x, y, z, phi, centers, sizes, numNodes, Ldev, const_cast<float4*>(prep.nrec), pout);
     CSG_CHECK_LAUNCH();
     return CS_OK;
 }

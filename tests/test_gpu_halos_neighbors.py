@@ -185,3 +185,31 @@ def test_fp32_pair_at_the_radius_is_not_a_neighbour(cs, O):
     nb, nc = cs.find_neighbors(tx, ty, tz, th, 0, n, box, o, layout, c, s, ngmax)
     torch.cuda.synchronize()
     neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("bucket", [4, 8])
+def test_neighbors_lattice_at_the_radius_small_leaves(cs, O, dtype, bucket):
+    """A cubic lattice whose face neighbours lie at the search radius up to the rounding of the coordinates (spacing
+    2^-6, origin off the binary grid, h = spacing / 2): nearly every face pair falls in the band of the FP32 filter and
+    is decided exactly, and the small buckets make the traversal merge adjoining leaves into one candidate batch, so
+    the exact decisions also look up the leaf of a candidate inside a merged batch."""
+    a = 1.0 / 64
+    g = np.arange(24, dtype=np.float64)
+    X, Y, Z = (v.ravel() for v in np.meshgrid(g, g, g, indexing="ij"))
+    x = (0.3 + a * X).astype(dtype)
+    y = (0.1 + a * Y).astype(dtype)
+    z = (0.7 + a * Z).astype(dtype)
+    n = x.size
+    h = np.full(n, a / 2, dtype)
+    lo = (0.3 - a, 0.1 - a, 0.7 - a)
+    hi = (0.3 + 25 * a, 0.1 + 25 * a, 0.7 + 25 * a)
+    ngmax = 32
+    ref, obox, box, o, layout, c, s, (tx, ty, tz, th) = _setup(O, cs, x, y, z, h, lo, hi, 0, bucket)
+    rnb, rnc = O.find_neighbors(ref["x"], ref["y"], ref["z"], ref["h"], 0, n, obox, ref["tree"], ref["layout"],
+                                ref["centers"], ref["sizes"], ngmax)
+    nb, nc = cs.find_neighbors(tx, ty, tz, th, 0, n, box, o, layout, c, s, ngmax)
+    torch.cuda.synchronize()
+    neighbor_lists_equal(u32(nb), u32(nc), rnb, rnc, ngmax)
+    # the rounding of the coordinates puts some face pairs inside the radius and some outside
+    assert 0 < rnc.sum() < 6 * n
