@@ -7,9 +7,14 @@
 // results bit for bit.
 #pragma once
 
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <type_traits>
 
 #include "../../include/cstone_gb300.h"
 
@@ -373,12 +378,17 @@ inline BoxParams<T> makeBoxParams(const cs_box& b)
     return p;
 }
 
-// sfc3D (sfc/sfc.hpp:142-179) parameters: mx = 2^L * ilx and xmin * mx, both rounded in T as the reference does
+// sfc3D (sfc/sfc.hpp:142-179) parameters: mx = 2^L * ilx and xmin * mx, both rounded in T as the reference does.
+// T = double also carries the integer form of the quantisation (quantizeAxis): oi = floor(o), ofrac = (o != oi), and
+// intForm when every axis passes the host's exactness checks
 template<class T, class K>
 struct KeyParams
 {
     T m[3];
     T o[3];
+    int oi[3];
+    int ofrac[3];
+    int intForm;
 };
 
 template<class T, class K>
@@ -386,12 +396,113 @@ inline KeyParams<T, K> makeKeyParams(const BoxParams<T>& b)
 {
     KeyParams<T, K> p;
     unsigned cube = 1u << KeyTraits<K>::maxLevel;
+    p.intForm     = std::is_same_v<T, double> ? 1 : 0;
     for (int k = 0; k < 3; ++k)
     {
         p.m[k] = T(cube) * b.ilen[k];
         p.o[k] = b.lo[k] * p.m[k];
+        // integer form (quantizeAxis): |x m| and |o| below 2^29 over the box (so floor(x m) - o is within 2^30 and
+        // its FP64 rounding below 2^-23), and the fraction of o zero or at least 2^-21 from 0 and 1
+        const double o    = double(p.o[k]);
+        const double oi   = std::floor(o);
+        const double frac = o - oi; // exact
+        const double ext  = std::max(std::fabs(double(b.lo[k])), std::fabs(double(b.hi[k]))) * double(p.m[k]);
+        const bool ok     = std::isfinite(ext) && ext < 0x1p29 && std::fabs(o) < 0x1p29 &&
+                        (frac == 0.0 || (frac > 0x1p-21 && 1.0 - frac > 0x1p-21));
+        p.oi[k]    = ok ? int(oi) : 0;
+        p.ofrac[k] = frac != 0.0 ? 1 : 0;
+        if (!ok) p.intForm = 0;
     }
     return p;
+}
+
+// x = hi + lo with hi = RN_float(x) and lo = RN_float(x - hi) (x - hi is exact in FP64), computed from the bits of x
+// with integer and FP32 instructions: GB300 issues FP64 instructions (the conversions and the subtraction) at a small
+// fraction of the FP32 rate. For a normal float result (binary exponent of x in [-70, 100]) hi keeps the top 23 of
+// the 52 mantissa bits, rounded to nearest with ties to even on the other 29 (a carry into the exponent included); x -
+// hi is then rem * 2^(e - 52) with rem the discarded bits minus 2^29 when rounded up (|rem| <= 2^28), and lo is
+// RN_float(rem) * 2^(e - 52), exact scaling by a power of two. Other exponents (zero, tiny or huge values, infinities,
+// NaN) take the FP64 instructions. Both give the same bits.
+__host__ __device__ __forceinline__ void splitDouble(double x, float& hi, float& lo)
+{
+#ifdef __CUDA_ARCH__
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+#else
+    unsigned long long b;
+    std::memcpy(&b, &x, sizeof b);
+#endif
+    const int e = int((b >> 52) & 0x7ffu) - 1023;
+    if (e >= -70 && e <= 100)
+    {
+        const unsigned long long mant = b & 0xfffffffffffffull;
+        unsigned m23                  = unsigned(mant >> 29);
+        const int rem                 = int(mant & 0x1fffffffu);
+        const bool up                 = rem > (1 << 28) || (rem == (1 << 28) && (m23 & 1u));
+        const int diff                = up ? rem - (1 << 29) : rem;
+        unsigned ex                   = unsigned(e + 127);
+        if (up && ++m23 == (1u << 23))
+        {
+            m23 = 0;
+            ++ex;
+        }
+        const unsigned sign = unsigned(b >> 32) & 0x80000000u;
+        const unsigned hb   = sign | (ex << 23) | m23;
+        const unsigned sb   = unsigned(e - 52 + 127) << 23; // 2^(e - 52), a normal float for e >= -74
+#ifdef __CUDA_ARCH__
+        hi = __uint_as_float(hb);
+        lo = __fmul_rn(__int2float_rn(sign ? -diff : diff), __uint_as_float(sb));
+#else
+        std::memcpy(&hi, &hb, sizeof hi);
+        float scale;
+        std::memcpy(&scale, &sb, sizeof scale);
+        lo = float(sign ? -diff : diff) * scale;
+#endif
+        return;
+    }
+#ifdef __CUDA_ARCH__
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(__dsub_rn(x, double(hi)));
+#else
+    hi = float(x);
+    lo = float(x - double(hi));
+#endif
+}
+
+// One axis of sfc3D's quantisation, int(floor(x m) - o) evaluated as the reference does in T (sfc/sfc.hpp:142-160).
+// Integer form (T = double, intForm): with f = floor(x m) (exact, an int while |x m| < 2^30) and o = oi + phi
+// (oi = floor(o), phi in [0, 1)), the exact difference f - o is d - phi with d = f - oi. The reference rounds it to
+// FP64 (an error of at most 2^-24 below 2^30), which keeps it inside (d - 1, d) when phi is 0 or at least 2^-21 from
+// 0 and 1; its truncation is then d - 1 when phi > 0 and d >= 1, and d otherwise. That is two FP64-pipe operations
+// (the product and the rounding-down conversion) instead of four. Products beyond 2^30 (points far outside the box)
+// take the FP64 expression.
+template<class T, class K>
+__host__ __device__ __forceinline__ int quantizeAxis(T x, const KeyParams<T, K>& p, int k)
+{
+    if constexpr (std::is_same_v<T, double>)
+    {
+        if (p.intForm)
+        {
+#ifdef __CUDA_ARCH__
+            const double y = __dmul_rn(x, p.m[k]);
+            const int f    = __double2int_rd(y);
+#else
+            const double y = x * p.m[k];
+            const double fy = std::floor(y);
+            const int f     = fy >= -0x1p31 && fy < 0x1p31 ? int(fy) : (fy < 0 ? INT_MIN : INT_MAX);
+#endif
+            if (f > -(1 << 30) && f < (1 << 30))
+            {
+                const int d = f - p.oi[k];
+                return p.ofrac[k] && d >= 1 ? d - 1 : d;
+            }
+        }
+    }
+#ifdef __CUDA_ARCH__
+    return RN<T>::toIntRz(RN<T>::sub(RN<T>::floor_(RN<T>::mul(x, p.m[k])), p.o[k]));
+#else
+    const T v = T(std::floor(T(x * p.m[k])) - p.o[k]);
+    return v >= T(-0x1p31) && v < T(0x1p31) ? int(v) : (v < T(0) ? INT_MIN : INT_MAX);
+#endif
 }
 
 // htab: the Hilbert state table in shared memory (iHilbertByTable), or null for the per-level encoder; same keys
@@ -399,9 +510,9 @@ template<class T, class K>
 __device__ __forceinline__ K sfc3D(T x, T y, T z, const KeyParams<T, K>& p, int kind, const uint16_t* htab = nullptr)
 {
     constexpr int mcoord = (1 << KeyTraits<K>::maxLevel) - 1;
-    int ix = RN<T>::toIntRz(RN<T>::sub(RN<T>::floor_(RN<T>::mul(x, p.m[0])), p.o[0]));
-    int iy = RN<T>::toIntRz(RN<T>::sub(RN<T>::floor_(RN<T>::mul(y, p.m[1])), p.o[1]));
-    int iz = RN<T>::toIntRz(RN<T>::sub(RN<T>::floor_(RN<T>::mul(z, p.m[2])), p.o[2]));
+    int ix = quantizeAxis<T, K>(x, p, 0);
+    int iy = quantizeAxis<T, K>(y, p, 1);
+    int iz = quantizeAxis<T, K>(z, p, 2);
     ix     = min(ix, mcoord);
     iy     = min(iy, mcoord);
     iz     = min(iz, mcoord);
