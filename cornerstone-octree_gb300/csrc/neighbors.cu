@@ -1368,9 +1368,8 @@ __global__ void prepParticlesKernel(const double* __restrict__ x, const double* 
 #pragma unroll
         for (int k = 0; k < 3; ++k)
         {
-            h[k] = __double2float_rn(v[k]);
-            l[k] = __double2float_rn(__dsub_rn(v[k], double(h[k])));
-            m    = fmaxf(m, fabsf(h[k]));
+            splitDouble(v[k], h[k], l[k]);
+            m = fmaxf(m, fabsf(h[k]));
         }
         phi[j] = make_float4(h[0], h[1], h[2], 0.f);
         plo[j] = make_float4(l[0], l[1], l[2], 0.f);
@@ -1417,10 +1416,8 @@ __global__ void prepNodesKernel(const double* __restrict__ centers, const double
 #pragma unroll
         for (int k = 0; k < 3; ++k)
         {
-            double c = centers[3 * size_t(i) + k];
-            h[k]     = __double2float_rn(c);
-            l[k]     = __double2float_rn(__dsub_rn(c, double(h[k])));
-            s[k]     = __double2float_rn(sizes[3 * size_t(i) + k]);
+            splitDouble(centers[3 * size_t(i) + k], h[k], l[k]);
+            s[k] = __double2float_rn(sizes[3 * size_t(i) + k]);
             m        = fmaxf(m, fabsf(h[k]) + s[k]);
         }
         float w0, w1, w2;

@@ -261,10 +261,10 @@ __global__ void __launch_bounds__(256) gatherPackedKernel(const uint32_t* __rest
         if constexpr (Shadow)
         {
             // x = hi + lo to about 2^-48 relative; hi is x rounded to float
-            float h0 = __double2float_rn(r.x), h1 = __double2float_rn(r.y), h2 = __double2float_rn(r.z);
-            float l0 = __double2float_rn(__dsub_rn(r.x, double(h0)));
-            float l1 = __double2float_rn(__dsub_rn(r.y, double(h1)));
-            float l2 = __double2float_rn(__dsub_rn(r.z, double(h2)));
+            float h0, h1, h2, l0, l1, l2;
+            splitDouble(r.x, h0, l0);
+            splitDouble(r.y, h1, l1);
+            splitDouble(r.z, h2, l2);
             phi[i]   = make_float4(h0, h1, h2, 0.f);
             plo[i]   = make_float4(l0, l1, l2, 0.f);
             m        = fmaxf(m, fmaxf(fabsf(h0), fmaxf(fabsf(h1), fabsf(h2))));
