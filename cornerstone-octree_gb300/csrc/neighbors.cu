@@ -432,7 +432,7 @@ constexpr int NBG_STACK = 192;
 #endif
 // leaves merged into one candidate range at most (one target per lane), and the longest merged range
 #ifndef NBG_MERGE
-#define NBG_MERGE 4
+#define NBG_MERGE 8
 #endif
 #ifndef NBG_MERGE_SPAN
 #define NBG_MERGE_SPAN 32
