@@ -1131,6 +1131,8 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
     bool loose                = false;
     int expansions            = 0;
     long long t0              = Stats ? clock64() : 0;
+    // absolute part of the child test's margin: the rounding terms and the float centre's missing low part
+    const float childMargin = __fadd_ru(__fmaf_ru(4 * EPS * EPS, C, delta), __fmul_ru(EPS, C));
     float rminW               = Stats ? warpMinF(active ? rr : INFINITY) : 0.f;
     int2* stack               = sStack[warp];
     auto entryCode            = [](int node, int c0) { return c0 > 0 ? c0 : -(2 * node + (c0 < 0 ? 1 : 0)) - 1; };
@@ -1235,10 +1237,12 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
             bool hit       = false;
             if (SUB || lane < 8)
             {
+                // the child's centre in the frame from its float centre alone (the low part, at most EPS C, is
+                // covered by childMargin), so one load of its record is saved
                 const float4* r = prep.nrec + 3 * size_t(c0 + cidx);
-                float4 rA = r[0], rB = r[1], rC = r[2];
-                float cc[3], sz[3];
-                frameOf(rA, rB, rC, cc, sz);
+                const float4 rA = r[0], rC = r[2];
+                const float cc[3] = {__fsub_rn(rA.x, P[0]), __fsub_rn(rA.y, P[1]), __fsub_rn(rA.z, P[2])};
+                const float sz[3] = {rC.x, rC.y, rC.z};
                 childC0     = __float_as_int(rA.w);
                 hit         = true;
                 float dist2 = 0.f;
@@ -1246,8 +1250,7 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                 for (int k = 0; k < 3; ++k)
                 {
                     float ad     = fabsf(cc[k] - gc[k]);
-                    float margin = __fmaf_ru(4 * EPS, fabsf(cc[k]) + sz[k] + fabsf(gc[k]) + gh[k],
-                                             __fmaf_ru(4 * EPS * EPS, C, delta));
+                    float margin = __fmaf_ru(4 * EPS, fabsf(cc[k]) + sz[k] + fabsf(gc[k]) + gh[k], childMargin);
                     hit          = hit && (ad - sz[k] - gh[k] < margin);
                     float dk     = fmaxf(__fsub_rd(__fsub_rd(ad, sz[k]), margin), 0.f);
                     dist2        = __fmaf_rd(dk, dk, dist2);
