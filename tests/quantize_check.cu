@@ -10,11 +10,12 @@
 
 using namespace csg;
 
-int main()
+template<class K>
+static void checkQuantisation(std::mt19937_64& rng, long long& checked, long long& mismatches, long long& boxesInt,
+                              long long& boxes)
 {
-    std::mt19937_64 rng(20261204);
     std::uniform_real_distribution<double> u01(0.0, 1.0);
-    long long checked = 0, mismatches = 0, boxesInt = 0, boxes = 0;
+    const double cells = double(1u << KeyTraits<K>::maxLevel);
     const double los[] = {-100.0, -1.0, 0.0, 0.3, -0.5, 1e-3, -3.7e2, 12345.678, -0.1, 2.0 / 3.0};
     for (int bi = 0; bi < 4000; ++bi)
     {
@@ -30,13 +31,13 @@ int main()
         if (bi % 7 == 0)
         {
             // nudge the offset so that o = lo m lies within a few ulps of an integer
-            const double m = double(1u << 21) / len;
+            const double m = cells / len;
             double o       = std::round(lo * m);
             box.lo[0] = box.lo[1] = box.lo[2] = std::nextafter(o / m, bi % 2 ? 1e300 : -1e300);
             box.hi[0] = box.hi[1] = box.hi[2] = box.lo[0] + len;
         }
         auto bp = makeBoxParams<double>(box);
-        auto p  = makeKeyParams<double, uint64_t>(bp);
+        auto p  = makeKeyParams<double, K>(bp);
         ++boxes;
         if (!p.intForm) continue;
         ++boxesInt;
@@ -50,21 +51,29 @@ int main()
             else if (mode <= 2)
             {
                 // on a cell boundary of the key grid and the neighbouring doubles
-                const double cell = std::floor(u01(rng) * double(1u << 21));
+                const double cell = std::floor(u01(rng) * cells);
                 x                 = bp.lo[0] + cell / p.m[0];
                 for (int s = 0; s < t % 3; ++s)
                     x = std::nextafter(x, mode == 1 ? 1e300 : -1e300);
             }
             else if (mode == 3) x = bp.lo[0] + (u01(rng) * 3.0 - 1.0) * (bp.hi[0] - bp.lo[0]); // outside as well
             else x = t % 2 ? bp.lo[0] : bp.hi[0];
-            const int a = quantizeAxis<double, uint64_t>(x, p, 0);
-            const int b = quantizeAxis<double, uint64_t>(x, ref, 0);
+            const int a = quantizeAxis<double, K>(x, p, 0);
+            const int b = quantizeAxis<double, K>(x, ref, 0);
             ++checked;
             if (a != b && mismatches++ < 5)
                 std::printf("mismatch: lo %.17g len %.17g x %.17g int %d fp64 %d\n", bp.lo[0], bp.hi[0] - bp.lo[0], x,
                             a, b);
         }
     }
+}
+
+int main()
+{
+    std::mt19937_64 rng(20261204);
+    long long checked = 0, mismatches = 0, boxesInt = 0, boxes = 0;
+    checkQuantisation<uint64_t>(rng, checked, mismatches, boxesInt, boxes);
+    checkQuantisation<uint32_t>(rng, checked, mismatches, boxesInt, boxes);
     std::printf("boxes %lld with the integer form %lld checked %lld mismatches %lld\n", boxes, boxesInt, checked,
                 mismatches);
 
