@@ -42,6 +42,11 @@ struct Pipeline final : PipelineBase
     DevBuf prefixes, childOffsets, parents, levelRange, i2l, l2i, linkWs;
     DevBuf centers, sizes, sc, ss, flags;
     DevBuf nbPrepWs, nb, nc, nbStats;
+    // the other set of per-run outputs copied back to the host (counts, halo flags): a pipelined host run writes one
+    // set while the previous run's copy-back still reads the other, so it never waits for that copy (outSlot: the set
+    // in nc / flags now)
+    DevBuf ncAlt, flagsAlt;
+    int outSlot = 0;
     // incremental time steps (step()): the current and the next leaf array with their counts, the current leaf
     // count in device memory, the leaf capacity every buffer of a step is sized for, and one captured graph per
     // direction of the leaf ping-pong
@@ -74,10 +79,12 @@ struct Pipeline final : PipelineBase
     cudaEvent_t inUsed[2]            = {}; // on the compute stream after the keys of the last run that read the set
     bool inUsedRec[2]                = {false, false};
     // results to host: with lists, the compaction first, on the compute stream (outReady after it); then the error
-    // words (errCopied), counts and flags (reuseReady: the next run may overwrite its outputs) on d2hStream, and the
+    // words (errCopied), counts and flags (reuse[s]: a later run may overwrite output set s) on d2hStream, and the
     // offsets and compacted lists (from one of two device buffer sets in turn) on listStream (outDone)
     cudaStream_t d2hStream = nullptr, listStream = nullptr;
-    cudaEvent_t outReady = nullptr, errCopied = nullptr, reuseReady = nullptr, outDone = nullptr;
+    cudaEvent_t outReady = nullptr, errCopied = nullptr, outDone = nullptr;
+    cudaEvent_t reuse[2] = {};  // on d2hStream after the copy of output set s (counts, flags) to the host
+    bool reuseRec[2]     = {false, false};
     cudaEvent_t listCopied[2]  = {};  // on listStream after the copy out of compaction buffer b
     cudaEvent_t cbEv[4]        = {};  // timing: compaction start / end, list copy start / end (cs_pipeline_copy_times)
     bool cbTimed               = false;
@@ -126,7 +133,7 @@ struct Pipeline final : PipelineBase
             if (e) cudaEventDestroy(e);
         if (d2hStream) cudaStreamDestroy(d2hStream);
         if (listStream) cudaStreamDestroy(listStream);
-        for (cudaEvent_t e : {outReady, errCopied, reuseReady, outDone, listCopied[0], listCopied[1], cbEv[0], cbEv[1],
+        for (cudaEvent_t e : {outReady, errCopied, reuse[0], reuse[1], outDone, listCopied[0], listCopied[1], cbEv[0], cbEv[1],
                               cbEv[2], cbEv[3]})
             if (e) cudaEventDestroy(e);
         if (herrHost) cudaFreeHost(herrHost);
@@ -387,7 +394,7 @@ struct Pipeline final : PipelineBase
     {
         int rc;
         if ((rc = flushListCopy())) return rc;
-        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, reuseReady, 0)); // a copy-back still reads the outputs
+        if (reuseRec[outSlot]) CSG_CUDA_TRY(cudaStreamWaitEvent(s, reuse[outSlot], 0)); // a copy-back reads them
         lastNIn = 0; // autotune reruns plain runs only (a step's inputs need not outlive it)
         if (incCur < 0 || nIn != incN)
         {
@@ -511,7 +518,7 @@ struct Pipeline final : PipelineBase
                                 &packed, &shadowHi, &shadowLo, &pout, &sortWs, &errWords, &buildWs, &leaves, &counts,
                                 &layout, &prefixes, &childOffsets,
                                 &parents, &levelRange, &i2l, &l2i, &linkWs, &centers, &sizes, &sc, &ss, &flags,
-                                &nbPrepWs, &nb, &nc})
+                                &nbPrepWs, &nb, &nc, &ncAlt, &flagsAlt})
             t += b->bytes;
         return t;
     }
@@ -530,6 +537,17 @@ struct Pipeline final : PipelineBase
         }
         const T *x = static_cast<const T*>(xv), *y = static_cast<const T*>(yv), *z = static_cast<const T*>(zv),
                 *h = static_cast<const T*>(hv);
+        if (hostIn && outPending)
+        {
+            // the previous run's counts and flags may still be on their way to the host: this run writes the other
+            // set (the graphs of time steps hold the old set's addresses, so a later step captures again)
+            std::swap(nc.p, ncAlt.p);
+            std::swap(nc.bytes, ncAlt.bytes);
+            std::swap(flags.p, flagsAlt.p);
+            std::swap(flags.bytes, flagsAlt.bytes);
+            outSlot ^= 1;
+            dropGraphs();
+        }
         if (hostIn)
         {
             for (DevBuf& b : inBuf[inSet])
@@ -702,7 +720,7 @@ struct Pipeline final : PipelineBase
         // ---- halos for the focus leaves ----
         CSG_CUDA_TRY(cudaEventRecord(ev[ST_HALOS], s));
         if ((rc = flags.ensure(size_t(N)))) return rc;
-        if (outPending) CSG_CUDA_TRY(cudaStreamWaitEvent(s, reuseReady, 0)); // the previous copy-back of flags, counts
+        if (reuseRec[outSlot]) CSG_CUDA_TRY(cudaStreamWaitEvent(s, reuse[outSlot], 0)); // the set's last copy-back
         CSG_CUDA_TRY(cudaMemsetAsync(flags.p, 0, size_t(N), s));
         if (cfg.do_halos && br.focusLast > br.focusFirst)
         {
@@ -832,7 +850,7 @@ struct Pipeline final : PipelineBase
             CSG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lowPrio, &highPrio));
             CSG_CUDA_TRY(cudaStreamCreateWithPriority(&d2hStream, cudaStreamNonBlocking, highPrio));
             CSG_CUDA_TRY(cudaStreamCreateWithPriority(&listStream, cudaStreamNonBlocking, highPrio));
-            for (cudaEvent_t* e : {&outReady, &errCopied, &reuseReady, &outDone, &listCopied[0], &listCopied[1]})
+            for (cudaEvent_t* e : {&outReady, &errCopied, &reuse[0], &reuse[1], &outDone, &listCopied[0], &listCopied[1]})
                 CSG_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
             for (cudaEvent_t& e : cbEv)
                 CSG_CUDA_TRY(cudaEventCreate(&e));
@@ -888,26 +906,41 @@ struct Pipeline final : PipelineBase
         copyWordsKernel<<<1, 32, 0, d2hStream>>>(errWords.as<uint32_t>(), herrDev, 4);
         CSG_CHECK_LAUNCH();
         CSG_CUDA_TRY(cudaEventRecord(errCopied, d2hStream));
-        // counts and flags: the next run waits for them (reuseReady), so they must not queue behind a list copy on
-        // the copy engines; pinned destinations are written by a small kernel instead
+        // counts and flags: the run after next writes this output set again and waits for them (reuse[outSlot]), so
+        // they must not queue behind a list copy on the copy engines; pinned destinations are written by a small
+        // kernel instead
         if (ncHost)
             if (int rc = copyToHostAsync(d2hStream, ncHost, nc.p, n * sizeof(uint32_t))) return rc;
         if (flagsHost)
             if (int rc = copyToHostAsync(d2hStream, flagsHost, flags.p, size_t(last.num_nodes))) return rc;
-        CSG_CUDA_TRY(cudaEventRecord(reuseReady, d2hStream));
+        CSG_CUDA_TRY(cudaEventRecord(reuse[outSlot], d2hStream));
+        reuseRec[outSlot] = true;
         CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, outReady, 0));
         if (listOffsets)
         {
             // the offsets now; the list itself by the copy engine once its length is known on the host, which is
             // when the next call (run, step or wait) has seen this compaction finish (flushListCopy)
-            CSG_CUDA_TRY(cudaMemcpyAsync(listOffsets, csrOff[b].p, (n + 1) * sizeof(uint64_t),
-                                         cudaMemcpyDeviceToHost, listStream));
+            if (int rc = copyToHostInPieces(listStream, listOffsets, csrOff[b].p, (n + 1) * sizeof(uint64_t)))
+                return rc;
             pendingList = PendingList{true, b, listHost, listHost ? listCap : 0};
             csrCur      = 1 - b;
         }
-        CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, reuseReady, 0)); // outDone: the counts and flags too
+        CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, reuse[outSlot], 0)); // outDone: the counts and flags too
         CSG_CUDA_TRY(cudaEventRecord(outDone, listStream));
         outPending = true;
+        return CS_OK;
+    }
+
+    // A large device-to-host copy issued as one cudaMemcpyAsync and the kernels running beside it slowed each other
+    // down (measured on a GB300 host: a 6.9 GB copy beside two 16M runs, both done after 432 ms, against 37 and 45 ms
+    // alone); issued in pieces of 64 MB the two overlap (58 ms for both). So every copy of the lists and offsets goes
+    // in such pieces.
+    static int copyToHostInPieces(cudaStream_t st, void* dst, const void* src, size_t bytes)
+    {
+        constexpr size_t kPiece = size_t(64) << 20;
+        for (size_t off = 0; off < bytes; off += kPiece)
+            CSG_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off,
+                                         std::min(kPiece, bytes - off), cudaMemcpyDeviceToHost, st));
         return CS_OK;
     }
 
@@ -924,9 +957,7 @@ struct Pipeline final : PipelineBase
         const size_t m = size_t(std::min<uint64_t>(total, pl.cap));
         if (total > pl.cap) *listOverflowHost = 1;
         CSG_CUDA_TRY(cudaEventRecord(cbEv[2], listStream));
-        if (m)
-            CSG_CUDA_TRY(cudaMemcpyAsync(pl.dst, csrList[pl.b].p, m * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                         listStream));
+        if (int rc = copyToHostInPieces(listStream, pl.dst, csrList[pl.b].p, m * sizeof(uint32_t))) return rc;
         CSG_CUDA_TRY(cudaEventRecord(cbEv[3], listStream));
         CSG_CUDA_TRY(cudaEventRecord(listCopied[pl.b], listStream));
         listCopiedRec[pl.b] = true;
