@@ -424,7 +424,10 @@ __global__ void __launch_bounds__(NB_THREADS) findNeighborsKernel(NbArgs<T> a, N
 // still met in SFC order and every lane sees its candidates in ascending j. Each reached leaf gets one conservative
 // per-lane test (lower bound of the distance from x_i to the leaf box) that decides which lanes scan it.
 // ---------------------------------------------------------------------------------------------------------------
-constexpr int NBG_STACK = 192;
+// Stack entries per warp. Expanding a node at level d (at most 20: 64-bit keys have 21 levels) leaves at most 7
+// pending siblings on each of the levels 1..d and pushes at most 8 children: 7 * 20 + 8 = 148 entries. The overflow
+// check stays, and the shared memory saved goes to L1 (the kernel's node records and candidates).
+constexpr int NBG_STACK = 152;
 // resident blocks of 4 warps per SM: 64 registers per thread (a few spilled to the L1-cached stack); 7 and 9 measured
 // slower on the 16M Plummer search
 #ifndef NBG_MIN_BLOCKS
