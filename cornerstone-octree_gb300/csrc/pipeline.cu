@@ -40,7 +40,7 @@ struct Pipeline final : PipelineBase
     DevBuf sortWs, errWords;
     DevBuf buildWs, leaves, counts, layout;
     DevBuf prefixes, childOffsets, parents, levelRange, i2l, l2i, linkWs;
-    DevBuf centers, sizes, sc, ss, flags;
+    DevBuf centers, sizes, sc, ss, flags, haloList;
     DevBuf nbPrepWs, nb, nc, nbStats;
     // the other set of per-run outputs copied back to the host (counts, halo flags): a pipelined host run writes one
     // set while the previous run's copy-back still reads the other, so it never waits for that copy (outSlot: the set
@@ -516,7 +516,7 @@ struct Pipeline final : PipelineBase
         for (const DevBuf* b : {&inBuf[0][0], &inBuf[0][1], &inBuf[0][2], &inBuf[0][3], &inBuf[1][0], &inBuf[1][1],
                                 &inBuf[1][2], &inBuf[1][3], &keys, &keysAlt, &order, &orderAlt, &xs, &ys, &zs, &hs,
                                 &packed, &shadowHi, &shadowLo, &pout, &sortWs, &errWords, &buildWs, &leaves, &counts,
-                                &layout, &prefixes, &childOffsets,
+                                &layout, &prefixes, &childOffsets, &haloList,
                                 &parents, &levelRange, &i2l, &l2i, &linkWs, &centers, &sizes, &sc, &ss, &flags,
                                 &nbPrepWs, &nb, &nc, &ncAlt, &flagsAlt})
             t += b->bytes;
@@ -729,13 +729,15 @@ struct Pipeline final : PipelineBase
             T scale = T(2.0f * cfg.halo_search_ext);
             if ((rc = searchBoxes<T, T>(s, xs.as<T>(), ys.as<T>(), zs.as<T>(), hs.as<T>(), layout.as<uint32_t>(),
                                      br.focusFirst, br.focusLast, scale, l2i.as<int32_t>() + I, centers.as<T>(),
-                                     sc.as<T>(), ss.as<T>())))
+                                     sc.as<T>(), ss.as<T>(), prep.phi)))
                 return rc;
             if constexpr (!(std::is_same_v<K, uint32_t> && std::is_same_v<T, double>))
             {
+                if ((rc = haloList.ensure((size_t(br.focusLast - br.focusFirst) + 2) * sizeof(int32_t)))) return rc;
                 if ((rc = findHalos<K, T>(s, prefixes.as<K>(), childOffsets.as<int32_t>(), parents.as<int32_t>(),
                                           centers.as<T>(), sizes.as<T>(), leaves.as<K>(), sc.as<T>(), ss.as<T>(), box,
-                                          br.focusFirst, br.focusLast, flags.as<uint8_t>(), err + 2, prep.nrec)))
+                                          br.focusFirst, br.focusLast, flags.as<uint8_t>(), err + 2, prep.nrec,
+                                          haloList.as<int32_t>())))
                     return rc;
             }
         }
@@ -1032,6 +1034,8 @@ struct Pipeline final : PipelineBase
         o->halo_flags      = flags.as<uint8_t>();
         o->neighbors       = cfg.do_neighbors ? nb.as<uint32_t>() : nullptr;
         o->neighbor_counts = nc.as<uint32_t>();
+        o->search_centers  = sc.p;
+        o->search_sizes    = ss.p;
         return CS_OK;
     }
 };

@@ -354,7 +354,8 @@ class PipelineOutputs(C.Structure):
     _fields_ = [("sorted_keys", C.c_void_p), ("order", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p),
                 ("z", C.c_void_p), ("h", C.c_void_p), ("leaves", C.c_void_p), ("counts", C.c_void_p),
                 ("layout", C.c_void_p), ("octree", OctreeView), ("centers", C.c_void_p), ("sizes", C.c_void_p),
-                ("halo_flags", C.c_void_p), ("neighbors", C.c_void_p), ("neighbor_counts", C.c_void_p)]
+                ("halo_flags", C.c_void_p), ("neighbors", C.c_void_p), ("neighbor_counts", C.c_void_p),
+                ("search_centers", C.c_void_p), ("search_sizes", C.c_void_p)]
 
 
 lib.cs_pipeline_device_bytes.restype = C.c_size_t
@@ -511,6 +512,9 @@ class Pipeline:
                    neighbor_counts=_wrap(o.neighbor_counts, n, torch.int32))
         if o.neighbors:
             out["neighbors"] = _wrap(o.neighbors, n * self.cfg.ngmax, torch.int32).view(n, self.cfg.ngmax)
+        if o.search_centers and r.focus_last > r.focus_first:
+            out["search_centers"] = _wrap(o.search_centers, 3 * L, tdt).view(L, 3)
+            out["search_sizes"] = _wrap(o.search_sizes, 3 * L, tdt).view(L, 3)
         return out
 
 

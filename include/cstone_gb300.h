@@ -515,6 +515,8 @@ typedef struct
     uint8_t* halo_flags;    /* num_nodes */
     uint32_t* neighbors;    /* n * ngmax */
     uint32_t* neighbor_counts; /* n */
+    void* search_centers;   /* 3 * num_leaves; leaves [focus_first, focus_last) hold the halo search boxes */
+    void* search_sizes;     /* 3 * num_leaves, as search_centers */
 } cs_pipeline_outputs;
 
 int cs_pipeline_create(cs_pipeline* out, int coord_bits, int key_bits, const cs_pipeline_config* config);

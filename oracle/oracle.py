@@ -548,20 +548,21 @@ def timed_pipeline(x, y, z, h, box, bucket, ngmax, focus=(0, 0), kind=HILBERT, k
     centers, sizes = node_fp_centers(tree.prefixes, box, x.dtype, kind, key_bits)
     layout = layout_from_counts(counts)
     c6 = time.perf_counter()
-    flags = None
+    flags = sboxes = None
     if focus[1] > focus[0]:
         first = int(np.searchsorted(leaves, np.uint64(focus[0])))
         last = int(np.searchsorted(leaves, np.uint64(focus[1])))
         l2i = tree.leaf_to_internal[tree.num_internal:]
         sc, ss = search_boxes(xs, ys, zs, hs, layout, first, last, 2.0 * halo_ext, l2i, centers)
         flags = find_halos(tree, centers, sizes, sc, ss, box, first, last, key_bits)
+        sboxes = (first, last, sc, ss)
     c7 = time.perf_counter()
     nb, nc = find_neighbors(xs, ys, zs, hs, 0, n, box, tree, layout, centers, sizes, ngmax)
     c8 = time.perf_counter()
     t = dict(keys=c1 - c0, sort=c2 - c1, gather=c3 - c2, build=c4 - c3, link=c5 - c4, geometry=c6 - c5,
              halos=c7 - c6, neighbors=c8 - c7, total=c8 - c0)
     return t, dict(sorted_keys=skeys, perm=perm, leaves=leaves, counts=counts, iterations=iters, tree=tree,
-                   centers=centers, sizes=sizes, flags=flags, nb=nb, nc=nc)
+                   centers=centers, sizes=sizes, flags=flags, search_boxes=sboxes, nb=nb, nc=nc)
 
 
 # ---------------------------------------------------------------------------------------------------------------

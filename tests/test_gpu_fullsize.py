@@ -81,6 +81,8 @@ def test_plummer_16m_headline_config(cs, O):
     assert (res.focus_first, res.focus_last) == (first, last)
     sc, ss = O.search_boxes(xs, ys, zs, hs, layout, first, last, 2.0, otree.leaf_to_internal[otree.num_internal:],
                             centers)
+    assert np.array_equal(out["search_centers"][first:last].cpu().numpy(), sc[first:last])
+    assert np.array_equal(out["search_sizes"][first:last].cpu().numpy(), ss[first:last])
     flags = O.find_halos(otree, centers, sizes, sc, ss, obox, first, last, 64)
     assert np.array_equal(out["halo_flags"].cpu().numpy(), flags)
     compare_neighbors_chunked(O, xs, ys, zs, hs, obox, otree, layout, centers, sizes, ngmax, out["neighbors"],

@@ -58,6 +58,64 @@ def test_halos(cs, O, dtype, bnd, focus):
     assert torch.equal(sc2[first:last], sc[first:last]) and torch.equal(ss2[first:last], ss[first:last])
 
 
+@pytest.mark.parametrize("hkind", ["f64", "f32"])
+@pytest.mark.parametrize("scale", [2.0, 0.75, 2.0 ** -20, 40.0])
+def test_search_boxes_fp64_screen_edges(cs, O, hkind, scale):
+    """FP64 search boxes, whose particles go through an FP32 screen before the exact FP64 min/max: exact ties of
+    x - r across a leaf, a leaf of 700 particles at one point (every particle a candidate on every side), empty
+    leaves, coordinates and h at or beyond the screen's range (2^120), subnormal, zero and negative-zero values,
+    centres outside the screen's range; scale 40 takes the unscreened kernel. Against the oracle, leaf by leaf."""
+    rng = np.random.default_rng(5)
+    sizes = rng.integers(0, 60, 400)
+    sizes[[3, 50, 51]] = 0
+    sizes[7], sizes[8] = 700, 257
+    L = sizes.size
+    layout = np.zeros(L + 1, np.uint32)
+    layout[1:] = np.cumsum(sizes)
+    n = int(layout[-1])
+    x, y, z = (rng.uniform(-1.0, 1.0, n) for _ in range(3))
+    h = rng.uniform(0.001, 0.05, n)
+
+    def seg(leaf):
+        return slice(int(layout[leaf]), int(layout[leaf + 1]))
+
+    s = seg(7)  # one point, one h
+    x[s], y[s], z[s], h[s] = 0.3, -0.2, 0.1, 0.01
+    s = seg(8)  # x - 2h = 0.5 and y + 2h = -0.25 for every particle
+    k = np.arange(sizes[8], dtype=np.float64)
+    x[s], h[s] = 0.5 + k * 2.0 ** -20, k * 2.0 ** -21
+    y[s] = -0.25 - k * 2.0 ** -20
+    s = seg(9)  # magnitudes at and beyond 2^120
+    m = sizes[9]
+    x[s] = np.resize([2.0 ** 120, -2.0 ** 121, 3e300, 1e37, -1e36], m)
+    z[s] = np.resize([-2.0 ** 119.99, 1e200, -0.5], m)
+    s = seg(10)  # zeros, negative zeros, subnormals, h = 0
+    m = sizes[10]
+    x[s] = np.resize([0.0, -0.0, 5e-324, -1e-310, 2.0 ** -121, -(2.0 ** -120)], m)
+    y[s] = np.resize([-0.0, 1e-300, 0.0], m)
+    h[s] = np.resize([0.0, 1e-310, 2.0 ** -121, 0.0, 1e-30], m)
+    s = seg(11)  # h beyond the screen's range
+    h[s] = np.resize([1e36, 2.0 ** 120, 0.01], sizes[11])
+    if hkind == "f32":
+        h = h.astype(np.float32)  # 1e-310 and 2^-121 become float zeros or subnormals
+    init = rng.uniform(-1.0, 1.0, (L, 3))
+    init[12] = (1e200, -3e299, 2.0 ** 120)
+    init[13] = (-0.0, 5e-324, 0.0)
+    init[[3, 50]] = (0.25, -0.125, 1e-300)  # empty leaves keep their centre
+    init[8] = (0.6, -0.3, 0.0)  # so that the tied values are the extrema
+
+    first, last = 2, L - 3
+    rsc, rss = O.search_boxes(x, y, z, h, layout, first, last, scale, np.arange(L, dtype=np.int32), init)
+    tx, ty, tz, th = to_dev(x, y, z, h)
+    tlayout = torch.from_numpy(layout.view(np.int32)).to(dev())
+    sc, ss = cs.search_boxes(tx, ty, tz, th, tlayout, first, last, scale, None, None,
+                             init=torch.from_numpy(init).to(dev()))
+    torch.cuda.synchronize()
+    assert np.array_equal(sc[first:last].cpu().numpy(), rsc[first:last])
+    assert np.array_equal(ss[first:last].cpu().numpy(), rss[first:last])
+    assert np.isfinite(rsc[first:last]).all() and np.isfinite(rss[first:last]).all()
+
+
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("bnd", [0, 1])
 @pytest.mark.parametrize("hmode", ["const", "variable"])

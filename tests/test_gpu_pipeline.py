@@ -30,6 +30,9 @@ def _check_against_oracle(cs, O, x, y, z, h, lo, hi, bnd, bucket, ngmax, focus, 
     assert np.array_equal(out["centers"].cpu().numpy(), ref["centers"])
     assert np.array_equal(out["sizes"].cpu().numpy(), ref["sizes"])
     if ref["flags"] is not None:
+        first, last, rsc, rss = ref["search_boxes"]
+        assert np.array_equal(out["search_centers"][first:last].cpu().numpy(), rsc[first:last])
+        assert np.array_equal(out["search_sizes"][first:last].cpu().numpy(), rss[first:last])
         assert np.array_equal(out["halo_flags"].cpu().numpy(), ref["flags"])
     neighbor_lists_equal(u32(out["neighbors"]), u32(out["neighbor_counts"]), ref["nb"], ref["nc"], ngmax)
     return res
