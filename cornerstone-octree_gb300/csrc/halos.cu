@@ -181,9 +181,10 @@ __device__ __forceinline__ bool sbEstimate(uint32_t i, const double* __restrict_
 // 2^-20 <= scale <= 16 so that rt stays finite and the absolute term covers h below 2^-120.
 constexpr int SB_WARPS = 8;
 constexpr int SB_QCAP  = 256; // a step queues at most 6 x 32 pairs onto fewer than 32
+constexpr int SB_KEEP  = 4;   // particles per lane whose estimates pass 1 keeps for pass 2
 
 template<class Th, bool Shadow>
-__global__ void __launch_bounds__(32 * SB_WARPS, 4)
+__global__ void __launch_bounds__(32 * SB_WARPS, Shadow ? 6 : 5)
     searchBoxesScreenKernel(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
                             const Th* __restrict__ h, const float4* __restrict__ phi,
                             const uint32_t* __restrict__ layout, int firstLeaf, int lastLeaf, Th scale, float scaleF,
@@ -233,9 +234,30 @@ __global__ void __launch_bounds__(32 * SB_WARPS, 4)
             mlo[k] = INF, mhi[k] = -INF;
     }
 
-    // pass 1: upper bound of each minimum, lower bound of each maximum (two particles per lane and round, loaded
-    // before either is used)
-    for (uint32_t j = sub; j < cnt; j += 2 * 8)
+    // pass 1: upper bound of each minimum, lower bound of each maximum. The first SB_KEEP particles of each lane
+    // (SB_KEEP x 8 per leaf, loaded together) keep their estimates in registers for pass 2; the rest of a large leaf
+    // is loaded two particles per lane and round, and again in pass 2.
+    auto fold = [&](const float (&pt)[3], float rt) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            const float E = __fmaf_ru(E24, __fadd_ru(fabsf(pt[k]), fabsf(rt)), EABS);
+            mlo[k]        = fminf(mlo[k], __fadd_ru(__fsub_rn(pt[k], rt), E));
+            mhi[k]        = fmaxf(mhi[k], __fsub_rd(__fadd_rn(pt[k], rt), E));
+        }
+    };
+    float ept[SB_KEEP][3], ert[SB_KEEP];
+    bool eok[SB_KEEP];
+#pragma unroll
+    for (int u = 0; u < SB_KEEP; ++u)
+    {
+        const uint32_t j = sub + 8u * u;
+        eok[u]           = j < cnt && sbEstimate<Th, Shadow>(first + j, x, y, z, h, phi, scaleF, ept[u], ert[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < SB_KEEP; ++u)
+        if (eok[u]) fold(ept[u], ert[u]);
+    for (uint32_t j = sub + 8u * SB_KEEP; j < cnt; j += 2 * 8)
     {
         float pt[2][3], rt[2];
         bool ok[2];
@@ -247,16 +269,7 @@ __global__ void __launch_bounds__(32 * SB_WARPS, 4)
         }
 #pragma unroll
         for (int u = 0; u < 2; ++u)
-        {
-            if (!ok[u]) continue;
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-            {
-                const float E = __fmaf_ru(E24, __fadd_ru(fabsf(pt[u][k]), fabsf(rt[u])), EABS);
-                mlo[k]        = fminf(mlo[k], __fadd_ru(__fsub_rn(pt[u][k], rt[u]), E));
-                mhi[k]        = fmaxf(mhi[k], __fsub_rd(__fadd_rn(pt[u][k], rt[u]), E));
-            }
-        }
+            if (ok[u]) fold(pt[u], rt[u]);
     }
 #pragma unroll
     for (int o = 1; o < 8; o <<= 1)
@@ -287,37 +300,28 @@ __global__ void __launch_bounds__(32 * SB_WARPS, 4)
         __syncwarp();
     };
 
-    // pass 2: queue the (particle, side) pairs the screen cannot rule out
-    const uint32_t maxCnt = __reduce_max_sync(0xffffffffu, cnt);
-    const unsigned below  = (1u << lane) - 1u;
-    int qn                = 0;
-    __syncwarp();
-    for (uint32_t j0 = 0; j0 < maxCnt; j0 += 8)
-    {
-        const uint32_t j = j0 + sub;
-        unsigned m       = 0;
-        if (j < cnt)
-        {
-            float pt[3], rt;
-            if (!sbEstimate<Th, Shadow>(first + j, x, y, z, h, phi, scaleF, pt, rt))
-                m = 63u;
-            else
-            {
+    // pass 2: queue the (particle, side) pairs the screen cannot rule out (bits 0-2: minima, 3-5: maxima; all six
+    // for a particle outside the screen's range); evaluate whenever 32 are queued
+    const unsigned below = (1u << lane) - 1u;
+    int qn               = 0;
+    auto sides           = [&](const float (&pt)[3], float rt) -> unsigned {
+        unsigned m = 0;
 #pragma unroll
-                for (int k = 0; k < 3; ++k)
-                {
-                    const float E = __fmaf_ru(E24, __fadd_ru(fabsf(pt[k]), fabsf(rt)), EABS);
-                    if (__fsub_rd(__fsub_rn(pt[k], rt), E) <= mlo[k]) m |= 1u << k;
-                    if (__fadd_ru(__fadd_rn(pt[k], rt), E) >= mhi[k]) m |= 8u << k;
-                }
-            }
+        for (int k = 0; k < 3; ++k)
+        {
+            const float E = __fmaf_ru(E24, __fadd_ru(fabsf(pt[k]), fabsf(rt)), EABS);
+            if (__fsub_rd(__fsub_rn(pt[k], rt), E) <= mlo[k]) m |= 1u << k;
+            if (__fadd_ru(__fadd_rn(pt[k], rt), E) >= mhi[k]) m |= 8u << k;
         }
+        return m;
+    };
+    auto queue = [&](unsigned m, uint32_t i) {
 #pragma unroll
         for (int sd = 0; sd < 6; ++sd)
         {
             const bool mine   = (m >> sd) & 1u;
             const unsigned bm = __ballot_sync(0xffffffffu, mine);
-            if (mine) sQ[w][qn + __popc(bm & below)] = make_uint2(first + j, unsigned(g << 3 | sd));
+            if (mine) sQ[w][qn + __popc(bm & below)] = make_uint2(i, unsigned(g << 3 | sd));
             qn += __popc(bm);
         }
         __syncwarp();
@@ -326,6 +330,26 @@ __global__ void __launch_bounds__(32 * SB_WARPS, 4)
             qn -= 32;
             evaluate(qn, 32);
         }
+    };
+    const uint32_t maxCnt = __reduce_max_sync(0xffffffffu, cnt);
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < SB_KEEP; ++u)
+    {
+        if (8u * u >= maxCnt) break;
+        const uint32_t j = sub + 8u * u;
+        queue(j < cnt ? (eok[u] ? sides(ept[u], ert[u]) : 63u) : 0u, first + j);
+    }
+    for (uint32_t j0 = 8u * SB_KEEP; j0 < maxCnt; j0 += 8)
+    {
+        const uint32_t j = j0 + sub;
+        unsigned m       = 0;
+        if (j < cnt)
+        {
+            float pt[3], rt;
+            m = sbEstimate<Th, Shadow>(first + j, x, y, z, h, phi, scaleF, pt, rt) ? sides(pt, rt) : 63u;
+        }
+        queue(m, first + j);
     }
     if (qn > 0) evaluate(0, qn);
 
@@ -460,8 +484,8 @@ __device__ __forceinline__ bool haloTraverse(const T (&tc)[3], const T (&ts)[3],
         tsf[k] = float(ts[k]);
     }
 
-    auto overlaps = [&](int idx) -> bool {
-        K pfx         = prefixes[idx];
+    // node test on the node's prefix and (FloatFilter) float records, loaded by the caller
+    auto overlapsLoaded = [&](int idx, K pfx, float4 c4, float4 s4) -> bool {
         K nk1         = decodePlaceholderBit<K>(pfx);
         unsigned plen = decodePrefixLength<K>(pfx);
         K nk2         = nk1 + (K(1) << (3u * KeyTraits<K>::maxLevel - plen));
@@ -470,7 +494,6 @@ __device__ __forceinline__ bool haloTraverse(const T (&tc)[3], const T (&ts)[3],
         bool ov = true;
         if constexpr (FloatFilter)
         {
-            float4 c4    = nrec[3 * size_t(idx)], s4 = nrec[3 * size_t(idx) + 2];
             float cc[3]  = {c4.x, c4.y, c4.z}, sz[3] = {s4.x, s4.y, s4.z};
             bool sureIn  = true, sureOut = false;
 #pragma unroll
@@ -499,6 +522,18 @@ __device__ __forceinline__ bool haloTraverse(const T (&tc)[3], const T (&ts)[3],
         if (ov) flags[idx] = 1;
         return ov;
     };
+    auto records = [&](int idx, float4& c4, float4& s4) {
+        if constexpr (FloatFilter)
+        {
+            c4 = nrec[3 * size_t(idx)];
+            s4 = nrec[3 * size_t(idx) + 2];
+        }
+    };
+    auto overlaps = [&](int idx) -> bool {
+        float4 c4{}, s4{};
+        records(idx, c4, s4);
+        return overlapsLoaded(idx, prefixes[idx], c4, s4);
+    };
 
     // the root is tested by lane 0 alone (a single node)
     bool rootOv = false;
@@ -519,10 +554,15 @@ __device__ __forceinline__ bool haloTraverse(const T (&tc)[3], const T (&ts)[3],
         int child = 0;
         if (g < ng)
         {
-            int node = stack[top + g] + (lane & 7);
-            if (overlaps(node))
+            // every load of the step is issued before the test needs any of them (one round trip per step)
+            const int node = stack[top + g] + (lane & 7);
+            const K pfx    = prefixes[node];
+            const int ch   = childOffsets[node];
+            float4 c4{}, s4{};
+            records(node, c4, s4);
+            if (overlapsLoaded(node, pfx, c4, s4))
             {
-                child = childOffsets[node];
+                child = ch;
                 push  = child != 0;
             }
         }
@@ -626,7 +666,7 @@ __global__ void haloNeedKernel(const K* __restrict__ leaves, const T* __restrict
 }
 
 template<class K, class T, bool FloatFilter>
-__global__ void __launch_bounds__(32 * HALO_WARPS)
+__global__ void __launch_bounds__(32 * HALO_WARPS, 10)
     findHalosListKernel(const K* __restrict__ prefixes, const int32_t* __restrict__ childOffsets,
                         const T* __restrict__ nc, const T* __restrict__ ns, const K* __restrict__ leaves,
                         const T* __restrict__ sc, const T* __restrict__ ss, BoxParams<T> b, int firstNode,
