@@ -959,12 +959,12 @@ def main():
 
 def gpu_launches_per_step(res):
     """kernels this library launches in one pipeline step (memsets and copies not counted): keys 1, sort 1 histogram
-    + 1 scan + one pass per 8 key bits, gather 1, build 1 cooperative, link 1 layout + prefix sort + invert +
-    levelRange + link, geometry 1, halos 2, neighbour node prep 1 + outside-leaf marks 1, neighbours 1 (no periodic
-    axis here)"""
+    + 1 scan + one pass per 8 key bits, gather 1, build 1 cooperative + 1 one-warp read of its result, link 1 layout +
+    prefix sort + invert + levelRange + link, geometry 1, halos 3 (search boxes, containment list, traversals),
+    neighbour node prep 1 + outside-leaf marks 1, neighbours 1 (no periodic axis here)"""
     key_passes = (63 + 7) // 8
     prefix_passes = (3 * res.max_depth + 1 + 7) // 8
-    return 1 + (2 + key_passes) + 1 + 1 + (1 + 2 + prefix_passes + 3) + 1 + 2 + 2 + 1
+    return 1 + (2 + key_passes) + 1 + (1 + 1) + (1 + 2 + prefix_passes + 3) + 1 + 3 + 2 + 1
 
 
 if __name__ == "__main__":

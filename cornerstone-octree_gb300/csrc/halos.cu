@@ -464,6 +464,63 @@ __device__ __noinline__ bool haloOverlapF64(double tc0, double tc1, double tc2, 
 // within 4 * 2^-53 S, so D_f < -8 u S proves the reference's test passes on that axis and D_f >= 8 u S proves it
 // fails; anything in between is decided by haloOverlapF64.
 //
+// The node test of a traversal on the node's prefix and (FloatFilter) float records, loaded by the caller; flags an
+// overlapping node. tcf, tsf: the search box rounded to float.
+template<class K, class T, bool FloatFilter>
+__device__ __forceinline__ bool haloNodeTest(int idx, K pfx, float4 c4, float4 s4, const T (&tc)[3],
+                                             const T (&ts)[3], const float (&tcf)[3], const float (&tsf)[3],
+                                             K lowest, K highest, const T* __restrict__ nc, const T* __restrict__ ns,
+                                             const BoxParams<T>& b, uint8_t* flags)
+{
+    constexpr float U8 = 8.f * 5.9604644775390625e-8f;
+    K nk1         = decodePlaceholderBit<K>(pfx);
+    unsigned plen = decodePrefixLength<K>(pfx);
+    K nk2         = nk1 + (K(1) << (3u * KeyTraits<K>::maxLevel - plen));
+    bool inside   = !(nk1 < lowest || nk2 > highest);
+    if (inside) return false;
+    bool ov = true;
+    if constexpr (FloatFilter)
+    {
+        float cc[3] = {c4.x, c4.y, c4.z}, sz[3] = {s4.x, s4.y, s4.z};
+        bool sureIn = true, sureOut = false;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            float d = __fsub_rn(__fsub_rn(fabsf(__fsub_rn(tcf[k], cc[k])), sz[k]), tsf[k]);
+            float S = __fadd_ru(__fadd_ru(__fadd_ru(fabsf(tcf[k]), fabsf(cc[k])), sz[k]), tsf[k]);
+            float E = __fmul_ru(U8, S);
+            sureIn  = sureIn && d < -E;
+            sureOut = sureOut || d >= E;
+        }
+        ov = !sureOut && (sureIn || haloOverlapF64(tc[0], tc[1], tc[2], ts[0], ts[1], ts[2], nc, ns, idx));
+    }
+    else
+    {
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            T d = RN<T>::sub(tc[k], nc[3 * size_t(idx) + k]);
+            d   = RN<T>::abs_(pbcFold<T>(d, b.pbc[k], b.len[k], b.ilen[k]));
+            d   = RN<T>::sub(d, ns[3 * size_t(idx) + k]);
+            d   = RN<T>::sub(d, ts[k]);
+            ov  = ov && (d < T(0));
+        }
+    }
+    if (ov) flags[idx] = 1;
+    return ov;
+}
+
+template<class T, bool FloatFilter>
+__device__ __forceinline__ void haloRecords(const float4* __restrict__ nrec, int idx, float4& c4, float4& s4)
+{
+    if constexpr (FloatFilter)
+    {
+        c4 = nrec[3 * size_t(idx)];
+        s4 = nrec[3 * size_t(idx) + 2];
+    }
+}
+
+//
 // One leaf's traversal by the whole warp (tc, ts: its search box, the same in every lane): per step the warp pops up
 // to four groups of eight siblings from the per-warp LIFO stack, tests the 32 nodes in parallel, flags the
 // overlapping ones and pushes the child group of every overlapping internal node. Returns false (and sets bit 0 of
@@ -475,7 +532,6 @@ __device__ __forceinline__ bool haloTraverse(const T (&tc)[3], const T (&ts)[3],
                                              const T* __restrict__ ns, const BoxParams<T>& b, uint8_t* flags,
                                              uint32_t* errWord, const float4* __restrict__ nrec)
 {
-    constexpr float U8 = 8.f * 5.9604644775390625e-8f;
     float tcf[3], tsf[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -483,52 +539,10 @@ __device__ __forceinline__ bool haloTraverse(const T (&tc)[3], const T (&ts)[3],
         tcf[k] = float(tc[k]);
         tsf[k] = float(ts[k]);
     }
-
-    // node test on the node's prefix and (FloatFilter) float records, loaded by the caller
     auto overlapsLoaded = [&](int idx, K pfx, float4 c4, float4 s4) -> bool {
-        K nk1         = decodePlaceholderBit<K>(pfx);
-        unsigned plen = decodePrefixLength<K>(pfx);
-        K nk2         = nk1 + (K(1) << (3u * KeyTraits<K>::maxLevel - plen));
-        bool inside   = !(nk1 < lowest || nk2 > highest);
-        if (inside) return false;
-        bool ov = true;
-        if constexpr (FloatFilter)
-        {
-            float cc[3]  = {c4.x, c4.y, c4.z}, sz[3] = {s4.x, s4.y, s4.z};
-            bool sureIn  = true, sureOut = false;
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-            {
-                float d = __fsub_rn(__fsub_rn(fabsf(__fsub_rn(tcf[k], cc[k])), sz[k]), tsf[k]);
-                float S = __fadd_ru(__fadd_ru(__fadd_ru(fabsf(tcf[k]), fabsf(cc[k])), sz[k]), tsf[k]);
-                float E = __fmul_ru(U8, S);
-                sureIn  = sureIn && d < -E;
-                sureOut = sureOut || d >= E;
-            }
-            ov = !sureOut && (sureIn || haloOverlapF64(tc[0], tc[1], tc[2], ts[0], ts[1], ts[2], nc, ns, idx));
-        }
-        else
-        {
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-            {
-                T d = RN<T>::sub(tc[k], nc[3 * size_t(idx) + k]);
-                d   = RN<T>::abs_(pbcFold<T>(d, b.pbc[k], b.len[k], b.ilen[k]));
-                d   = RN<T>::sub(d, ns[3 * size_t(idx) + k]);
-                d   = RN<T>::sub(d, ts[k]);
-                ov  = ov && (d < T(0));
-            }
-        }
-        if (ov) flags[idx] = 1;
-        return ov;
+        return haloNodeTest<K, T, FloatFilter>(idx, pfx, c4, s4, tc, ts, tcf, tsf, lowest, highest, nc, ns, b, flags);
     };
-    auto records = [&](int idx, float4& c4, float4& s4) {
-        if constexpr (FloatFilter)
-        {
-            c4 = nrec[3 * size_t(idx)];
-            s4 = nrec[3 * size_t(idx) + 2];
-        }
-    };
+    auto records = [&](int idx, float4& c4, float4& s4) { haloRecords<T, FloatFilter>(nrec, idx, c4, s4); };
     auto overlaps = [&](int idx) -> bool {
         float4 c4{}, s4{};
         records(idx, c4, s4);
@@ -665,6 +679,12 @@ __global__ void haloNeedKernel(const K* __restrict__ leaves, const T* __restrict
     if (need) scratch[2 + base + __popc(m & ((1u << lane) - 1u))] = int32_t(leaf);
 }
 
+// Per 8-lane group: its own traversal of one list entry at a time, one sibling group of 8 nodes per step from its
+// own LIFO stack, so that a warp keeps four traversals in flight (a traversal's stack is mostly shallow, and each
+// step waits for its node loads). One group popped and at most 8 pushed per step bounds a stack by 7 entries per
+// level plus 8 (7 * 21 + 8 = 155 for 64-bit keys).
+constexpr int HALO_GSTACK = 160;
+
 template<class K, class T, bool FloatFilter>
 __global__ void __launch_bounds__(32 * HALO_WARPS, 10)
     findHalosListKernel(const K* __restrict__ prefixes, const int32_t* __restrict__ childOffsets,
@@ -673,29 +693,89 @@ __global__ void __launch_bounds__(32 * HALO_WARPS, 10)
                         int lastNode, uint8_t* flags, uint32_t* errWord, const float4* __restrict__ nrec,
                         int32_t* scratch)
 {
-    __shared__ int sStack[HALO_WARPS][HALO_STACK];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ int sStack[HALO_WARPS][4][HALO_GSTACK];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 3, sub = lane & 7, lead = lane & ~7;
     const int total = scratch[0];
     if (total == 0) return;
     const K lowest  = leaves[firstNode];
     const K highest = leaves[lastNode];
+    int* stack      = sStack[warp][g];
+    int top         = 0;     // the group's stack height (the same in its 8 lanes)
+    bool done       = false; // the group found the list exhausted
+    T tc[3] = {}, ts[3] = {};
+    float tcf[3] = {}, tsf[3] = {};
     for (;;)
     {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(&scratch[1], 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= total) return;
-        const int leaf = scratch[2 + item];
-        T tc[3], ts[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
+        // a group without work takes the next list entry; its lane 0 tests the root
+        const bool want = !done && top == 0;
+        int item        = 0;
+        if (want && sub == 0) item = atomicAdd(&scratch[1], 1);
+        item = __shfl_sync(0xffffffffu, item, lead);
+        if (want)
         {
-            tc[k] = sc[3 * size_t(leaf) + k];
-            ts[k] = ss[3 * size_t(leaf) + k];
+            if (item >= total)
+                done = true;
+            else
+            {
+                const int leaf = scratch[2 + item];
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                {
+                    tc[k]  = sc[3 * size_t(leaf) + k];
+                    ts[k]  = ss[3 * size_t(leaf) + k];
+                    tcf[k] = float(tc[k]);
+                    tsf[k] = float(ts[k]);
+                }
+            }
         }
-        if (!haloTraverse<K, T, FloatFilter>(tc, ts, sStack[warp], lane, lowest, highest, prefixes, childOffsets, nc,
-                                             ns, b, flags, errWord, nrec))
+        if (__all_sync(0xffffffffu, done)) return;
+        int rootChild = 0;
+        if (want && !done && sub == 0)
+        {
+            float4 c4{}, s4{};
+            haloRecords<T, FloatFilter>(nrec, 0, c4, s4);
+            const int ch = childOffsets[0];
+            if (haloNodeTest<K, T, FloatFilter>(0, prefixes[0], c4, s4, tc, ts, tcf, tsf, lowest, highest, nc, ns, b,
+                                                flags))
+                rootChild = ch;
+        }
+        rootChild = __shfl_sync(0xffffffffu, rootChild, lead);
+        if (rootChild != 0)
+        {
+            if (sub == 0) stack[0] = rootChild;
+            top = 1;
+        }
+        __syncwarp();
+
+        // one step of every group with a non-empty stack: pop one sibling group, test its 8 nodes, push the child
+        // groups of the overlapping internal ones
+        bool push = false;
+        int child = 0;
+        if (top > 0)
+        {
+            --top;
+            const int node = stack[top] + sub;
+            const K pfx    = prefixes[node];
+            const int ch   = childOffsets[node];
+            float4 c4{}, s4{};
+            haloRecords<T, FloatFilter>(nrec, node, c4, s4);
+            if (haloNodeTest<K, T, FloatFilter>(node, pfx, c4, s4, tc, ts, tcf, tsf, lowest, highest, nc, ns, b,
+                                                flags))
+            {
+                child = ch;
+                push  = child != 0;
+            }
+        }
+        __syncwarp();
+        const unsigned pm = (__ballot_sync(0xffffffffu, push) >> lead) & 0xffu;
+        if (__any_sync(0xffffffffu, top + __popc(pm) > HALO_GSTACK))
+        {
+            if (lane == 0 && errWord) atomicOr(errWord, 1u);
             return;
+        }
+        if (push) stack[top + __popc(pm & ((1u << sub) - 1u))] = child;
+        top += __popc(pm);
+        __syncwarp();
     }
 }
 
