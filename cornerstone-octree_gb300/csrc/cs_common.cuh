@@ -468,6 +468,29 @@ __host__ __device__ __forceinline__ void splitDouble(double x, float& hi, float&
 #endif
 }
 
+// Float estimate of a double from its high word (sign, exponent and the top 20 mantissa bits, rounded toward zero):
+// |e - v| <= 2^-20 |v| for 2^-120 <= |v| < 2^120 and e = +-0 (|e - v| < 2^-120) below that range; false for
+// |v| >= 2^120, Inf and NaN. Integer instructions only.
+__host__ __device__ __forceinline__ bool truncEstimate(double v, float& e)
+{
+#ifdef __CUDA_ARCH__
+    const unsigned hw = unsigned(__double2hiint(v));
+#else
+    unsigned long long b;
+    std::memcpy(&b, &v, sizeof b);
+    const unsigned hw = unsigned(b >> 32);
+#endif
+    const unsigned a = hw & 0x7fffffffu;
+    if (a >= 0x47700000u) return false; // biased exponent >= 1023 + 120
+    const unsigned fb = a < 0x38700000u ? hw & 0x80000000u : (hw & 0x80000000u) | ((a - 0x38000000u) << 3);
+#ifdef __CUDA_ARCH__
+    e = __uint_as_float(fb);
+#else
+    std::memcpy(&e, &fb, sizeof e);
+#endif
+    return true;
+}
+
 // One axis of sfc3D's quantisation, int(floor(x m) - o) evaluated as the reference does in T (sfc/sfc.hpp:142-160).
 // Integer form (T = double, intForm): with f = floor(x m) (exact, an int while |x m| < 2^30) and o = oi + phi
 // (oi = floor(o), phi in [0, 1)), the exact difference f - o is d - phi with d = f - oi. The reference rounds it to

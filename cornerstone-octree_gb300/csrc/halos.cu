@@ -119,18 +119,6 @@ __global__ void searchBoxesKernel(const T* __restrict__ x, const T* __restrict__
     }
 }
 
-// Float estimate of a double from its high word (sign, exponent and the top 20 mantissa bits, rounded toward zero):
-// |e - v| <= 2^-20 |v| for 2^-120 <= |v| < 2^120 and e = +-0 (|e - v| < 2^-120) below that range; false for
-// |v| >= 2^120, Inf and NaN. Integer instructions only.
-__device__ __forceinline__ bool truncEstimate(double v, float& e)
-{
-    const unsigned hw = unsigned(__double2hiint(v));
-    const unsigned a  = hw & 0x7fffffffu;
-    if (a >= 0x47700000u) return false; // biased exponent >= 1023 + 120
-    e = __int_as_float(a < 0x38700000u ? hw & 0x80000000u : (hw & 0x80000000u) | ((a - 0x38000000u) << 3));
-    return true;
-}
-
 // FP32 estimates of one particle for the screened search boxes: pt ~ (x, y, z), rt ~ h * scale. Shadow: pt are the
 // coordinates rounded to nearest float (the neighbour search's shadows), else truncEstimate of the doubles. With
 // Th = float, rt is the reference's r itself; with Th = double it comes from truncEstimate(h) times the float
