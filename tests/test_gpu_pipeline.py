@@ -75,6 +75,19 @@ def test_pipeline_periodic_f64(cs, O):
     _check_against_oracle(cs, O, x, y, z, h, 0.0, 1.0, 1, 32, 150, (0, 1 << 61))
 
 
+@pytest.mark.parametrize("key_bits, focus", [(64, (0, 1 << 61)), (32, (0, 1 << 28))])
+def test_pipeline_plummer_f32_halos(cs, O, key_bits, focus):
+    """FP32 coordinates with halos: the plain search boxes and the list-driven halo walks without the FP64 filter,
+    64- and 32-bit keys"""
+    n = 1 << 16
+    x, y, z = (a.astype(np.float32) for a in O.plummer(11, n))
+    lo, hi = (float(x.min()), float(y.min()), float(z.min())), (float(x.max()), float(y.max()), float(z.max()))
+    h = O.h_for_k_neighbors_cpu(x.astype(np.float64), y.astype(np.float64), z.astype(np.float64),
+                                O.make_box(lo, hi), 60).astype(np.float32)
+    res = _check_against_oracle(cs, O, x, y, z, h, lo, hi, 0, 32, 100, focus, coord_bits=32, key_bits=key_bits)
+    assert res.focus_last > res.focus_first
+
+
 def test_pipeline_host_call_matches_device_call(cs, O):
     n = 1 << 16
     x, y, z = O.plummer(8, n)
