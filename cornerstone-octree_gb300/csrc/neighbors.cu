@@ -1079,12 +1079,36 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
                     }
                     if (i >= base && i - base < 32u) inM &= ~(0x80000000u >> (i - base));
                     if constexpr (Stats) hitsThis = __popc(inM);
-                    while (inM)
+                    // the hits in ascending candidate order; while the row has room for all of them (the common
+                    // case) two per round, without a bound check per hit
+                    const unsigned nh = __popc(inM);
+                    if (nc + nh <= ngmax)
                     {
-                        int k = __clz(inM);
-                        inM &= ~(0x80000000u >> k);
-                        if (nc < ngmax) myNb[nc] = base + k;
-                        nc++;
+                        uint32_t* p = myNb + nc;
+                        while (inM)
+                        {
+                            const int k1 = __clz(inM);
+                            inM ^= 0x80000000u >> k1;
+                            p[0] = base + k1;
+                            if (inM)
+                            {
+                                const int k2 = __clz(inM);
+                                inM ^= 0x80000000u >> k2;
+                                p[1] = base + k2;
+                            }
+                            p += 2;
+                        }
+                        nc += nh;
+                    }
+                    else
+                    {
+                        while (inM)
+                        {
+                            int k = __clz(inM);
+                            inM &= ~(0x80000000u >> k);
+                            if (nc < ngmax) myNb[nc] = base + k;
+                            nc++;
+                        }
                     }
                 }
             }
