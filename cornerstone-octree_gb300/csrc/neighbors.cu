@@ -761,14 +761,16 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
 
     // conservative per-lane test: can a particle of this node lie within the search radius of x_i? (a lower
     // bound of |x_i - node box|, the box widened by the particle slack delta)
+    // per axis (D - sz) - u with u = 4.5 EPS (D + sz) + 1.05 A + delta, evaluated as two FMAs with the factors
+    // rounded outward, D (1 - 5 EPS) - (sz (1 + 6 EPS) + c0), the first rounded up and the second down
+    const float hitC0 = __fmaf_ru(1.05f, A, delta);
     auto mayHitBox = [&](const float cc[3], const float sz[3]) -> bool {
         float n2 = 0.f;
 #pragma unroll
         for (int k = 0; k < 3; ++k)
         {
             float D = fabsf(__fsub_rn(cc[k], b[k]));
-            float u = __fmaf_ru(4.5f * EPS, D + sz[k], __fmaf_ru(1.05f, A, delta));
-            float d = fmaxf(__fsub_rd(__fsub_rd(D, sz[k]), u), 0.f);
+            float d = fmaxf(__fmaf_rd(D, 1.f - 5 * EPS, -__fmaf_ru(sz[k], 1.f + 6 * EPS, hitC0)), 0.f);
             n2      = __fmaf_rd(d, d, n2);
         }
         return n2 < r2hi;
