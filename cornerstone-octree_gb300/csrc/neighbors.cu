@@ -1278,10 +1278,12 @@ __global__ void __launch_bounds__(NB_THREADS, NBG_MIN_BLOCKS) findNeighborsGroup
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
                 {
+                    // ad - sz rounded down once for both tests (that only widens the overlap test)
                     float ad     = fabsf(cc[k] - gc[k]);
                     float margin = __fmaf_ru(4 * EPS, fabsf(cc[k]) + sz[k] + fabsf(gc[k]) + gh[k], childMargin);
-                    hit          = hit && (ad - sz[k] - gh[k] < margin);
-                    float dk     = fmaxf(__fsub_rd(__fsub_rd(ad, sz[k]), margin), 0.f);
+                    float t      = __fsub_rd(ad, sz[k]);
+                    hit          = hit && (t - gh[k] < margin);
+                    float dk     = fmaxf(__fsub_rd(t, margin), 0.f);
                     dist2        = __fmaf_rd(dk, dk, dist2);
                 }
                 hit = hit && dist2 <= gR2;
