@@ -80,11 +80,14 @@ struct Pipeline final : PipelineBase
     bool inUsedRec[2]                = {false, false};
     // results to host: with lists, the compaction first, on the compute stream (outReady after it); then the error
     // words (errCopied), counts and flags (reuse[s]: a later run may overwrite output set s) on d2hStream, and the
-    // offsets and compacted lists (from one of two device buffer sets in turn) on listStream (outDone)
+    // offsets and compacted lists (from one of two device buffer sets in turn) on listStream (outDone). The two
+    // streams do not wait for each other (a list copy never queues behind counts); wait() waits for both
+    // (outDone and reuse[lastOutSlot])
     cudaStream_t d2hStream = nullptr, listStream = nullptr;
     cudaEvent_t outReady = nullptr, errCopied = nullptr, outDone = nullptr;
     cudaEvent_t reuse[2] = {};  // on d2hStream after the copy of output set s (counts, flags) to the host
     bool reuseRec[2]     = {false, false};
+    int lastOutSlot      = 0; // the output set of the last copy-back
     cudaEvent_t listCopied[2]  = {};  // on listStream after the copy out of compaction buffer b
     cudaEvent_t cbEv[4]        = {};  // timing: compaction start / end, list copy start / end (cs_pipeline_copy_times)
     bool cbTimed               = false;
@@ -927,9 +930,9 @@ struct Pipeline final : PipelineBase
             pendingList = PendingList{true, b, listHost, listHost ? listCap : 0};
             csrCur      = 1 - b;
         }
-        CSG_CUDA_TRY(cudaStreamWaitEvent(listStream, reuse[outSlot], 0)); // outDone: the counts and flags too
         CSG_CUDA_TRY(cudaEventRecord(outDone, listStream));
-        outPending = true;
+        lastOutSlot = outSlot;
+        outPending  = true;
         return CS_OK;
     }
 
@@ -992,6 +995,7 @@ struct Pipeline final : PipelineBase
         if (outPending)
         {
             CSG_CUDA_TRY(cudaEventSynchronize(outDone));
+            CSG_CUDA_TRY(cudaEventSynchronize(reuse[lastOutSlot]));
             outPending = false;
             rc         = deviceErrors(herrHost);
             if (rc == CS_OK && listOverflowHost && *listOverflowHost)
